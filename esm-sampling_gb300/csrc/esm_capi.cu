@@ -1,0 +1,748 @@
+// C ABI of libesmcuda.so (include/esmcuda.h): context, uploads, and the replica-step entry points.
+#define ESM_COMMON_KERNELS
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/esmcuda.h"
+#include "esm_common.cuh"
+#include "esm_kernels_impl.cuh"
+#include "esm_launch.cuh"
+
+using std::vector;
+
+namespace {
+
+// disp -> knew, others -> kold: the capacities after set_dispatchable_capacity!, before the kop moves
+__global__ void k_mix(int K, const int *u_kind, const double *kold, const double *knew, double *kmid) {
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= K) return;
+    kmid[u] = u_kind[u] == ESM_UNIT_DISP ? knew[u] : kold[u];
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct esm_ctx {
+    int precision = 32;
+    int R = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    bool has_state = false, has_scores = false;
+    int max_warps = 0;
+    esm::DevModel<float> Mf;
+    esm::DevModel<double> Md;
+    vector<void *> allocs;
+    // host copies needed by the entry points
+    int N, L, T, K, D, S, n0, nreg, ngroups;
+    double dt, gamma_k, beta_k, beta_v, kappa0;
+    int physical;
+    uint64_t seed;
+    vector<int> class_len;      // steps per class
+    int ncls;
+    // device (precision-independent)
+    int *d_steps[3] = {nullptr, nullptr, nullptr};
+    int *d_disp = nullptr, *d_ugroup = nullptr, *d_ugidx = nullptr, *d_ukind = nullptr, *d_uloc = nullptr;
+    double *d_lo = nullptr, *d_hi = nullptr, *d_capex = nullptr;
+    double *d_k = nullptr, *d_kold = nullptr, *d_knew = nullptr, *d_k1 = nullptr, *d_kmid = nullptr;
+    double *d_dk = nullptr, *d_sk = nullptr, *d_fk = nullptr, *d_parts = nullptr;
+    double *d_w = nullptr, *d_eta = nullptr, *d_kappa = nullptr, *d_xi = nullptr;
+    int *d_nclip = nullptr;
+    unsigned long long *d_stats = nullptr;
+    int32_t *d_reg = nullptr;
+    void *d_scratch = nullptr;
+    // precision-dependent state pointers (aliases into Mf / Md)
+    void *theta = nullptr, *g = nullptr, *e = nullptr, *r = nullptr, *F = nullptr, *z = nullptr;
+    void *kc_d = nullptr, *kc_s = nullptr, *kc_r = nullptr;
+};
+
+namespace {
+
+int fail(esm_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(c, e_ == cudaErrorMemoryAllocation ? ESM_ENOMEM : ESM_ECUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+    } while (0)
+
+template <class T>
+int dalloc(esm_ctx *c, T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (n ? n : 1));
+    if (e != cudaSuccess) return fail(c, ESM_ENOMEM, "cudaMalloc of %zu bytes: %s", sizeof(T) * n, cudaGetErrorString(e));
+    c->allocs.push_back(q);
+    *p = (T *)q;
+    return ESM_OK;
+}
+
+template <class T>
+int upload(esm_ctx *c, T **p, const T *h, size_t n) {
+    int rc = dalloc(c, p, n);
+    if (rc) return rc;
+    if (n && h) CK(cudaMemcpyAsync(*p, h, sizeof(T) * n, cudaMemcpyHostToDevice, c->stream));
+    return ESM_OK;
+}
+
+template <class real>
+int upload_real(esm_ctx *c, const real **p, const double *h, size_t n) {
+    vector<real> tmp(n ? n : 1);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (real)h[i];
+    real *q;
+    int rc = dalloc(c, &q, n);
+    if (rc) return rc;
+    CK(cudaMemcpy(q, tmp.data(), sizeof(real) * n, cudaMemcpyHostToDevice));
+    *p = q;
+    return ESM_OK;
+}
+
+template <class real>
+int upload_real_vec(esm_ctx *c, const real **p, const vector<double> &h) {
+    return upload_real<real>(c, p, h.data(), h.size());
+}
+
+void class_steps(int T, int cls, vector<int> &out) {
+    out.clear();
+    if (T % 2 == 1) {
+        if (cls == 0)
+            for (int t = 0; t < T - 1; t += 2) out.push_back(t);
+        else if (cls == 1)
+            for (int t = 1; t < T - 1; t += 2) out.push_back(t);
+        else
+            out.push_back(T - 1);
+    } else {
+        for (int t = cls; t < T; t += 2) out.push_back(t);
+    }
+}
+
+template <class real>
+esm::DevModel<real> &dm(esm_ctx *c);
+template <>
+esm::DevModel<float> &dm<float>(esm_ctx *c) { return c->Mf; }
+template <>
+esm::DevModel<double> &dm<double>(esm_ctx *c) { return c->Md; }
+
+// build the device model of one precision
+template <class real>
+int build_model(esm_ctx *c, const esm_model *m, const esm_opts *o) {
+    esm::DevModel<real> &M = dm<real>(c);
+    memset(&M, 0, sizeof M);
+    int N = m->N, L = m->L, K = m->K, D = m->D, S = m->S;
+    M.N = N;
+    M.L = L;
+    M.T = m->T;
+    M.R = o->R;
+    M.K = K;
+    M.D = D;
+    M.S = S;
+    M.n0 = m->n0;
+    M.nreg = m->nreg;
+    M.nfields = m->nfields;
+    M.nlev = m->nlev;
+    M.natoms = m->field_atom_ptr[m->nfields];
+    M.nextra = (int)nearbyint(o->extra * N);
+    M.span = o->span > 0 ? o->span : std::max(1, 32 / o->R);
+    M.maxpts = o->max_points;
+    M.dt = (real)m->dt;
+    M.c_shed = (real)m->c_shed;
+    M.c_dump = (real)m->c_dump;
+    M.c_viol = (real)m->c_viol;
+    M.kappa0 = (real)m->kappa0;
+    M.beta_v = (real)m->beta_v;
+    M.maxnats = (real)o->maxnats;
+    M.kmin = (real)o->kappa_min;
+    M.seed = o->seed;
+    double tot = 0;
+    for (int q = 0; q < ESM_NFAM; ++q) tot += o->family_rates[q];
+    double cum = 0;
+    for (int q = 0; q < ESM_NFAM; ++q) {
+        cum += o->family_rates[q];
+        M.cumw[q] = cum / tot;
+    }
+    int rc;
+    // network
+    vector<int> nlp(N + 1, 0), nl;
+    {
+        vector<vector<int>> lst(N);
+        for (int e = 0; e < L; ++e) {
+            lst[m->bus0[e]].push_back(e);
+            lst[m->bus1[e]].push_back(e);
+        }
+        for (int n = 0; n < N; ++n) {
+            nlp[n + 1] = nlp[n] + (int)lst[n].size();
+            nl.insert(nl.end(), lst[n].begin(), lst[n].end());
+        }
+    }
+    vector<int> lbp(N + 1, 0), lbl;
+    {
+        vector<vector<int>> lst(N);
+        for (int e = 0; e < L; ++e) lst[m->bus0[e]].push_back(e);
+        for (int n = 0; n < N; ++n) {
+            lbp[n + 1] = lbp[n] + (int)lst[n].size();
+            lbl.insert(lbl.end(), lst[n].begin(), lst[n].end());
+        }
+    }
+    int *ip;
+#define UPI(field, src, n)                          \
+    if ((rc = upload(c, &ip, (src), (size_t)(n)))) \
+        return rc;                                  \
+    M.field = ip;
+    UPI(bus0, m->bus0, L);
+    UPI(bus1, m->bus1, L);
+    UPI(nlp, nlp.data(), N + 1);
+    UPI(nl, nl.data(), nl.size());
+    UPI(lb0_ptr, lbp.data(), N + 1);
+    UPI(lb0_line, lbl.data(), lbl.size());
+    UPI(comp, m->comp, N);
+    if ((rc = upload_real<real>(c, &M.lb, m->line_b, L))) return rc;
+    if ((rc = upload_real<real>(c, &M.ls, m->line_s, L))) return rc;
+    if ((rc = upload_real<real>(c, &M.Z, m->reroute, (size_t)N * N))) return rc;
+    // units
+    vector<int> u_loc(K, -1), r_bus, r_series, d_bus, d_group, s_bus;
+    vector<double> r_mc, d_avail, d_mc, s_h, s_ei, s_eo, s_q, s_mc;
+    int nren = 0;
+    for (int u = 0; u < K; ++u) {
+        if (m->unit_kind[u] == ESM_UNIT_REN) {
+            u_loc[u] = nren++;
+            r_bus.push_back(m->unit_bus[u]);
+            r_series.push_back(m->unit_series[u]);
+            r_mc.push_back(m->unit_mc[u]);
+        }
+    }
+    for (int j = 0; j < D; ++j) {
+        int u = m->disp[j];
+        u_loc[u] = j;
+        d_bus.push_back(m->unit_bus[u]);
+        d_group.push_back(m->unit_group[u]);
+        d_avail.push_back(m->unit_avail[u]);
+        d_mc.push_back(m->unit_mc[u]);
+    }
+    for (int j = 0; j < S; ++j) {
+        int u = m->stor[j];
+        u_loc[u] = j;
+        s_bus.push_back(m->unit_bus[u]);
+        s_h.push_back(m->unit_hours[u]);
+        s_ei.push_back(m->unit_eta_in[u]);
+        s_eo.push_back(m->unit_eta_out[u]);
+        s_q.push_back(m->unit_qt[u]);
+        s_mc.push_back(m->unit_mc[u]);
+    }
+    M.Nren = nren;
+    UPI(r_bus, r_bus.data(), nren);
+    UPI(r_series, r_series.data(), nren);
+    UPI(d_bus, d_bus.data(), D);
+    UPI(d_group, d_group.data(), D);
+    UPI(s_bus, s_bus.data(), S);
+    UPI(u_kind, m->unit_kind, K);
+    UPI(u_loc, u_loc.data(), K);
+    if ((rc = upload_real_vec<real>(c, &M.r_mc, r_mc))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.d_avail, d_avail))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.d_mc, d_mc))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.s_hours, s_h))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.s_etain, s_ei))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.s_etaout, s_eo))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.s_qt, s_q))) return rc;
+    if ((rc = upload_real_vec<real>(c, &M.s_mc, s_mc))) return rc;
+    // node -> flat units (ascending)
+    vector<int> nup(N + 1, 0), nuu;
+    {
+        vector<vector<int>> lst(N);
+        for (int u = 0; u < K; ++u) lst[m->unit_bus[u]].push_back(u);
+        for (int n = 0; n < N; ++n) {
+            if (lst[n].size() > 8) return fail(c, ESM_EINVAL, "node %d has %zu units (at most 8)", n, lst[n].size());
+            nup[n + 1] = nup[n] + (int)lst[n].size();
+            nuu.insert(nuu.end(), lst[n].begin(), lst[n].end());
+        }
+    }
+    UPI(nu_ptr, nup.data(), N + 1);
+    UPI(nu_unit, nuu.data(), nuu.size());
+    // weather
+    if ((rc = upload_real<real>(c, &M.xbar, m->xbar, (size_t)m->n0 * m->T))) return rc;
+    if ((rc = upload_real<real>(c, &M.wscale, m->wscale, m->n0))) return rc;
+    // move tables
+    int natoms = M.natoms;
+    UPI(frole, m->field_role, m->nfields);
+    UPI(fap, m->field_atom_ptr, m->nfields + 1);
+    UPI(ap, m->atom_ptr, natoms + 1);
+    UPI(ai, m->atom_idx, m->atom_ptr[natoms]);
+    if ((rc = upload_real<real>(c, &M.av, m->atom_val, m->atom_ptr[natoms]))) return rc;
+    UPI(up, m->units_ptr, N + 1);
+    UPI(ua, m->units_at, m->units_ptr[N]);
+    UPI(sp, m->stor_ptr, N + 1);
+    UPI(sa, m->stor_at, m->stor_ptr[N]);
+    {
+        double *qp;
+        if ((rc = upload(c, &qp, m->qcum, m->nlev))) return rc;
+        M.qcum = qp;
+    }
+    int ncell = m->cell_level_ptr[m->nlev];
+    UPI(clp, m->cell_level_ptr, m->nlev + 1);
+    UPI(cp, m->cell_ptr, ncell + 1);
+    UPI(cu, m->cell_units, m->cell_ptr[ncell]);
+    int npair = m->xpart_ptr[N];
+    UPI(xpp, m->xpart_ptr, N + 1);
+    UPI(xp, m->xpart, npair);
+    UPI(xnp, m->xnod_ptr, npair + 1);
+    UPI(xn, m->xnod, m->xnod_ptr[npair]);
+    if ((rc = upload_real<real>(c, &M.xv, m->xval, m->xnod_ptr[npair]))) return rc;
+    UPI(xlp, m->xlk_ptr, npair + 1);
+    UPI(xln, m->xlkn, m->xlk_ptr[npair]);
+    if ((rc = upload_real<real>(c, &M.xlg, m->xlkg, m->xlk_ptr[npair]))) return rc;
+    vector<int> tnnz(N, 0);
+    for (int f = 0; f < m->nfields; ++f) {
+        if (m->field_role[f] != ESM_ROLE_THETA) continue;
+        for (int a = m->field_atom_ptr[f]; a < m->field_atom_ptr[f + 1]; ++a)
+            for (int q = m->atom_ptr[a]; q < m->atom_ptr[a + 1]; ++q) tnnz[m->atom_idx[q]] += 1;
+    }
+    UPI(theta_nnz, tnnz.data(), N);
+#undef UPI
+    // descriptor capacities
+    int maxatom = 0, maxstu = 1;
+    for (int f = 0; f < m->nfields; ++f)
+        for (int a = m->field_atom_ptr[f]; a < m->field_atom_ptr[f + 1]; ++a) {
+            int nz = m->atom_ptr[a + 1] - m->atom_ptr[a];
+            maxatom = std::max(maxatom, nz);
+            if (m->field_role[f] == ESM_ROLE_SE) maxstu = std::max(maxstu, nz);
+        }
+    int maxcell = 0;
+    for (int q = 0; q < ncell; ++q) maxcell = std::max(maxcell, m->cell_ptr[q + 1] - m->cell_ptr[q]);
+    int maxunits = 1;
+    for (int n = 0; n < N; ++n) maxunits = std::max(maxunits, m->units_ptr[n + 1] - m->units_ptr[n]);
+    int maxleak = 1;
+    for (int p = 0; p < npair; ++p) maxleak = std::max(maxleak, m->xlk_ptr[p + 1] - m->xlk_ptr[p]);
+    M.maxe = std::max(std::max(maxatom, maxcell), 4) + 4;
+    M.maxl = L;
+    M.maxn = N;
+    M.maxk = maxleak;
+    M.maxku = maxleak * maxunits;
+    M.maxstu = maxstu;
+    return ESM_OK;
+}
+
+template <class real>
+int alloc_state(esm_ctx *c) {
+    esm::DevModel<real> &M = dm<real>(c);
+    size_t TR = (size_t)M.T * M.R;
+    real *p;
+    int rc;
+#define AL(field, n)                          \
+    if ((rc = dalloc(c, &p, (size_t)(n)))) \
+        return rc;                            \
+    M.field = p;                              \
+    c->field = p;
+    AL(theta, M.N * TR);
+    AL(g, M.D * TR);
+    AL(e, M.S * TR);
+    AL(r, M.N * TR);
+    AL(F, M.L * TR);
+    AL(z, M.n0 * TR);
+#undef AL
+    real *q;
+    if ((rc = dalloc(c, &q, M.D))) return rc;
+    M.kc_d = q;
+    c->kc_d = q;
+    if ((rc = dalloc(c, &q, M.S))) return rc;
+    M.kc_s = q;
+    c->kc_s = q;
+    if ((rc = dalloc(c, &q, std::max(M.Nren, 1)))) return rc;
+    M.kc_r = q;
+    c->kc_r = q;
+    // line-move scratch for a persistent grid
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    c->max_warps = std::max(4, nsm * 16);
+    size_t per = esm::linemove_scratch_reals<real>(M);
+    if ((rc = dalloc(c, &q, per * (size_t)c->max_warps))) return rc;
+    c->d_scratch = q;
+    return ESM_OK;
+}
+
+template <class real>
+int set_kc(esm_ctx *c, const double *k) {
+    CK(esm::launch_set_kc<real>(c->K, k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (real *)c->kc_d, (real *)c->kc_s,
+                                (real *)c->kc_r, c->stream));
+    c->launches += 1;
+    return ESM_OK;
+}
+
+int set_kc_any(esm_ctx *c, const double *k) { return c->precision == 64 ? set_kc<double>(c, k) : set_kc<float>(c, k); }
+
+template <class real>
+int up_state(esm_ctx *c, void *dst, const double *h, size_t n) {
+    if (!h) return ESM_OK;
+    vector<real> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (real)h[i];
+    CK(cudaMemcpyAsync(dst, tmp.data(), sizeof(real) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return ESM_OK;
+}
+
+template <class real>
+int down_state(esm_ctx *c, const void *src, double *h, size_t n) {
+    if (!h) return ESM_OK;
+    vector<real> tmp(n);
+    CK(cudaMemcpyAsync(tmp.data(), src, sizeof(real) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) h[i] = (double)tmp[i];
+    return ESM_OK;
+}
+
+int rebuild_any(esm_ctx *c) {
+    CK(c->precision == 64 ? esm::launch_rebuild<double>(c->Md, c->stream) : esm::launch_rebuild<float>(c->Mf, c->stream));
+    c->launches += 1;
+    return ESM_OK;
+}
+
+int class_pass_any(esm_ctx *c, uint32_t sweep, int cls) {
+    int ns = c->class_len[cls];
+    if (ns == 0) return ESM_OK;
+    if (c->precision == 64)
+        CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, (double *)c->d_scratch, c->max_warps,
+                                          c->d_stats, c->stream));
+    else
+        CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, (float *)c->d_scratch, c->max_warps,
+                                         c->d_stats, c->stream));
+    c->launches += 1;
+    return ESM_OK;
+}
+
+void class_order(const esm_ctx *c, uint32_t sweep, int order[3], int *ncls) {
+    double u0, u1;
+    esm::uniform2(c->seed, ESM_TAG_SWEEP, 0, 0, 0, sweep, &u0, &u1);
+    if (c->T % 2 == 0) {
+        *ncls = 2;
+        order[0] = u0 < 0.5 ? 0 : 1;
+        order[1] = 1 - order[0];
+    } else {
+        *ncls = 3;
+        order[0] = 0;
+        order[1] = 1;
+        order[2] = 2;
+        int j = std::min(2, (int)floor(u0 * 3));
+        std::swap(order[2], order[j]);
+        j = std::min(1, (int)floor(u1 * 2));
+        std::swap(order[1], order[j]);
+    }
+}
+
+int stats_out(esm_ctx *c, int64_t *stats) {
+    if (!stats) return ESM_OK;
+    unsigned long long h[2 * (ESM_NFAM + 1) + 1];
+    CK(cudaMemcpyAsync(h, c->d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < 2 * (ESM_NFAM + 1) + 1; ++i) stats[i] += (int64_t)h[i];
+    return ESM_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+extern "C" {
+
+int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
+    if (!out) return ESM_EINVAL;
+    *out = nullptr;
+    if (!m || !o) return ESM_EINVAL;
+    esm_ctx *c = new esm_ctx();
+    *out = c;
+    if (o->precision != 32 && o->precision != 64) return fail(c, ESM_EINVAL, "precision must be 32 or 64");
+    if (o->R < 1 || m->N < 2 || m->T < 2 || m->K < 1) return fail(c, ESM_EINVAL, "bad sizes");
+    if (o->max_points < 8) return fail(c, ESM_EINVAL, "max_points must be >= 8");
+    c->precision = o->precision;
+    c->R = o->R;
+    c->N = m->N;
+    c->L = m->L;
+    c->T = m->T;
+    c->K = m->K;
+    c->D = m->D;
+    c->S = m->S;
+    c->n0 = m->n0;
+    c->nreg = m->nreg;
+    c->dt = m->dt;
+    c->gamma_k = m->gamma_k;
+    c->beta_k = m->beta_k;
+    c->beta_v = m->beta_v;
+    c->kappa0 = m->kappa0;
+    c->physical = m->physical;
+    c->seed = o->seed;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    int rc = c->precision == 64 ? build_model<double>(c, m, o) : build_model<float>(c, m, o);
+    if (rc) return rc;
+    rc = c->precision == 64 ? alloc_state<double>(c) : alloc_state<float>(c);
+    if (rc) return rc;
+    // classes
+    c->ncls = c->T % 2 ? 3 : 2;
+    c->class_len.assign(3, 0);
+    vector<int> st;
+    for (int q = 0; q < c->ncls; ++q) {
+        class_steps(c->T, q, st);
+        c->class_len[q] = (int)st.size();
+        if ((rc = upload(c, &c->d_steps[q], st.data(), st.size()))) return rc;
+    }
+    // unit tables (FP64)
+    int K = c->K;
+    vector<int> gidx(K, 0), cnt(64, 0);
+    int ng = 0;
+    for (int u = 0; u < K; ++u) {
+        int gq = m->unit_group[u];
+        if (gq < 0 || gq >= 64) return fail(c, ESM_EINVAL, "unit group out of range");
+        gidx[u] = cnt[gq]++;
+        ng = std::max(ng, gq + 1);
+    }
+    c->ngroups = ng;
+    vector<int> uloc(K, -1);
+    {
+        int nr = 0;
+        for (int u = 0; u < K; ++u)
+            if (m->unit_kind[u] == ESM_UNIT_REN) uloc[u] = nr++;
+        for (int j = 0; j < m->D; ++j) uloc[m->disp[j]] = j;
+        for (int j = 0; j < m->S; ++j) uloc[m->stor[j]] = j;
+    }
+    if ((rc = upload(c, &c->d_disp, m->disp, m->D))) return rc;
+    if ((rc = upload(c, &c->d_ugroup, m->unit_group, K))) return rc;
+    if ((rc = upload(c, &c->d_ugidx, gidx.data(), K))) return rc;
+    if ((rc = upload(c, &c->d_ukind, m->unit_kind, K))) return rc;
+    if ((rc = upload(c, &c->d_uloc, uloc.data(), K))) return rc;
+    if ((rc = upload(c, &c->d_lo, m->unit_lo, K))) return rc;
+    if ((rc = upload(c, &c->d_hi, m->unit_hi, K))) return rc;
+    if ((rc = upload(c, &c->d_capex, m->unit_capex, K))) return rc;
+    double *dp;
+    for (double **pp : {&c->d_k, &c->d_kold, &c->d_knew, &c->d_k1, &c->d_kmid, &c->d_fk, &c->d_xi}) {
+        if ((rc = dalloc(c, &dp, K))) return rc;
+        *pp = dp;
+    }
+    for (double **pp : {&c->d_dk, &c->d_sk}) {
+        if ((rc = dalloc(c, &dp, (size_t)c->R * K))) return rc;
+        *pp = dp;
+    }
+    if ((rc = dalloc(c, &c->d_parts, (size_t)c->R * 8))) return rc;
+    if ((rc = dalloc(c, &c->d_w, c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_eta, 64))) return rc;
+    if ((rc = dalloc(c, &c->d_kappa, 64))) return rc;
+    if ((rc = dalloc(c, &c->d_nclip, 1))) return rc;
+    if ((rc = dalloc(c, &c->d_stats, 2 * (ESM_NFAM + 1) + 1))) return rc;
+    if ((rc = dalloc(c, &c->d_reg, (size_t)c->T * c->R))) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return ESM_OK;
+}
+
+int esm_destroy(esm_ctx *c) {
+    if (!c) return ESM_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ESM_OK;
+}
+
+const char *esm_last_error(const esm_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+int esm_upload_state(esm_ctx *c, const double *theta, const double *g, const double *e, const double *z,
+                     const int32_t *reg, const double *k) {
+    if (!c) return ESM_EINVAL;
+    size_t TR = (size_t)c->T * c->R;
+    int rc;
+    bool f64 = c->precision == 64;
+    rc = f64 ? up_state<double>(c, c->theta, theta, c->N * TR) : up_state<float>(c, c->theta, theta, c->N * TR);
+    if (rc) return rc;
+    rc = f64 ? up_state<double>(c, c->g, g, c->D * TR) : up_state<float>(c, c->g, g, c->D * TR);
+    if (rc) return rc;
+    rc = f64 ? up_state<double>(c, c->e, e, c->S * TR) : up_state<float>(c, c->e, e, c->S * TR);
+    if (rc) return rc;
+    rc = f64 ? up_state<double>(c, c->z, z, c->n0 * TR) : up_state<float>(c, c->z, z, c->n0 * TR);
+    if (rc) return rc;
+    if (reg) CK(cudaMemcpy(c->d_reg, reg, sizeof(int32_t) * TR, cudaMemcpyHostToDevice));
+    if (k) {
+        CK(cudaMemcpy(c->d_k, k, sizeof(double) * c->K, cudaMemcpyHostToDevice));
+        if ((rc = set_kc_any(c, c->d_k))) return rc;
+    }
+    c->has_state = true;
+    c->has_scores = false;
+    CK(cudaStreamSynchronize(c->stream));
+    return ESM_OK;
+}
+
+int esm_download_state(esm_ctx *c, double *theta, double *g, double *e, double *z, int32_t *reg, double *k) {
+    if (!c) return ESM_EINVAL;
+    size_t TR = (size_t)c->T * c->R;
+    bool f64 = c->precision == 64;
+    int rc;
+    rc = f64 ? down_state<double>(c, c->theta, theta, c->N * TR) : down_state<float>(c, c->theta, theta, c->N * TR);
+    if (rc) return rc;
+    rc = f64 ? down_state<double>(c, c->g, g, c->D * TR) : down_state<float>(c, c->g, g, c->D * TR);
+    if (rc) return rc;
+    rc = f64 ? down_state<double>(c, c->e, e, c->S * TR) : down_state<float>(c, c->e, e, c->S * TR);
+    if (rc) return rc;
+    rc = f64 ? down_state<double>(c, c->z, z, c->n0 * TR) : down_state<float>(c, c->z, z, c->n0 * TR);
+    if (rc) return rc;
+    if (reg) CK(cudaMemcpy(reg, c->d_reg, sizeof(int32_t) * TR, cudaMemcpyDeviceToHost));
+    if (k) CK(cudaMemcpy(k, c->d_k, sizeof(double) * c->K, cudaMemcpyDeviceToHost));
+    return ESM_OK;
+}
+
+int esm_rebuild_caches(esm_ctx *c) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    return rebuild_any(c);
+}
+
+int esm_download_caches(esm_ctx *c, double *r, double *F) {
+    if (!c) return ESM_EINVAL;
+    size_t TR = (size_t)c->T * c->R;
+    bool f64 = c->precision == 64;
+    int rc = f64 ? down_state<double>(c, c->r, r, c->N * TR) : down_state<float>(c, c->r, r, c->N * TR);
+    if (rc) return rc;
+    return f64 ? down_state<double>(c, c->F, F, c->L * TR) : down_state<float>(c, c->F, F, c->L * TR);
+}
+
+int esm_class_pass(esm_ctx *c, int64_t sweep, int32_t cls, int64_t *stats) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    if (cls < 0 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * (2 * (ESM_NFAM + 1) + 1), c->stream));
+    int rc = class_pass_any(c, (uint32_t)sweep, cls);
+    if (rc) return rc;
+    c->has_scores = false;
+    return stats_out(c, stats);
+}
+
+int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * (2 * (ESM_NFAM + 1) + 1), c->stream));
+    for (int s = 0; s < n; ++s) {
+        uint32_t sw = (uint32_t)(sweep0 + s);
+        int rc = rebuild_any(c);
+        if (rc) return rc;
+        int order[3], nc;
+        class_order(c, sw, order, &nc);
+        for (int q = 0; q < nc; ++q)
+            if ((rc = class_pass_any(c, sw, order[q]))) return rc;
+    }
+    c->has_scores = false;
+    return stats_out(c, stats);
+}
+
+int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    int rc = rebuild_any(c);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->d_dk, 0, sizeof(double) * c->R * c->K, c->stream));
+    CK(cudaMemsetAsync(c->d_parts, 0, sizeof(double) * c->R * 8, c->stream));
+    if (c->precision == 64) {
+        CK(esm::launch_scores<double>(c->Md, c->d_dk, c->d_parts, c->stream));
+        CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
+                                            c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
+    } else {
+        CK(esm::launch_scores<float>(c->Mf, c->d_dk, c->d_parts, c->stream));
+        CK(esm::launch_score_finish<float>(c->Mf, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
+                                           c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
+    }
+    c->launches += 2;
+    if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * c->R * c->K, cudaMemcpyDeviceToHost, c->stream));
+    if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
+    if (parts) CK(cudaMemcpyAsync(parts, c->d_parts, sizeof(double) * c->R * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_scores = true;
+    return ESM_OK;
+}
+
+int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const double *kappa_s, double kappa_min,
+                      double clip, int32_t box, const double *xi, int64_t it, double *knew_out, int32_t *nclip_out) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_scores) return fail(c, ESM_ESTATE, "esm_capacity_scores must precede esm_langevin_step");
+    if (!w || !eta || !kappa_s) return fail(c, ESM_EINVAL, "w, eta and kappa_s are required");
+    int K = c->K, rc;
+    CK(cudaMemcpyAsync(c->d_w, w, sizeof(double) * c->R, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_eta, eta, sizeof(double) * c->ngroups, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_kappa, kappa_s, sizeof(double) * c->ngroups, cudaMemcpyHostToDevice, c->stream));
+    if (xi) CK(cudaMemcpyAsync(c->d_xi, xi, sizeof(double) * K, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_nclip, 0, sizeof(int), c->stream));
+    CK(cudaMemcpyAsync(c->d_kold, c->d_k, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
+    esm::k_langevin<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->R, c->d_ugroup, c->d_ugidx, c->d_kold, c->d_sk,
+                                                            c->d_fk, c->d_w, c->d_eta, c->d_kappa,
+                                                            c->beta_k / c->beta_v, kappa_min, clip, box,
+                                                            c->d_hi, xi ? c->d_xi : nullptr, c->seed, (uint32_t)it,
+                                                            c->d_knew, c->d_nclip);
+    CK(cudaGetLastError());
+    // follow_capacities! (src/replicas.jl:448): dispatchable at fixed output, rebuild, kop curve, rebuild
+    if (c->precision == 64)
+        CK(esm::launch_follow_disp<double>(c->Md, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
+    else
+        CK(esm::launch_follow_disp<float>(c->Mf, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
+    k_mix<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, c->d_kmid);
+    CK(cudaGetLastError());
+    if ((rc = set_kc_any(c, c->d_kmid))) return rc;
+    if ((rc = rebuild_any(c))) return rc;
+    esm::k_kop_capacity<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, kappa_min,
+                                                                 c->d_k1);
+    CK(cudaGetLastError());
+    if (c->precision == 64)
+        CK(esm::launch_kop<double>(c->Md, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
+    else
+        CK(esm::launch_kop<float>(c->Mf, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
+    CK(cudaMemcpyAsync(c->d_k, c->d_k1, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = set_kc_any(c, c->d_k))) return rc;
+    if ((rc = rebuild_any(c))) return rc;
+    c->launches += 5;
+    if (knew_out) CK(cudaMemcpyAsync(knew_out, c->d_k, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
+    int nclip = 0;
+    CK(cudaMemcpyAsync(&nclip, c->d_nclip, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (nclip_out) *nclip_out = nclip;
+    c->has_scores = false;
+    return ESM_OK;
+}
+
+int esm_weather_step(esm_ctx *c, const int32_t *moved, const double *theta, const int32_t *window,
+                     const int32_t *wstart, const double *xi, int64_t it) {
+    (void)moved;
+    (void)theta;
+    (void)window;
+    (void)wstart;
+    (void)xi;
+    (void)it;
+    return fail(c, ESM_EINVAL, "esm_weather_step: not available in this build");
+}
+
+int esm_sync(esm_ctx *c, double timeout_s) {
+    if (!c) return ESM_EINVAL;
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaStreamQuery(c->stream);
+        if (e == cudaSuccess) return ESM_OK;
+        if (e != cudaErrorNotReady) return fail(c, ESM_ECUDA, "stream: %s", cudaGetErrorString(e));
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > timeout_s) return fail(c, ESM_ETIMEOUT, "stream not idle after %.1f s", timeout_s);
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+int64_t esm_launch_count(const esm_ctx *c) { return c ? c->launches : 0; }
+
+}  // extern "C"

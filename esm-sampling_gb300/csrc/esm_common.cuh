@@ -1,0 +1,155 @@
+// Shared device definitions of libesmcuda: Philox streams, the device model, cost pieces.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/esmcuda.h"
+
+#define ESM_TAG_SWEEP 0x53574550u
+#define ESM_TAG_LIST 0x4C495354u
+#define ESM_TAG_LANE 0x4C414E45u
+#define ESM_TAG_LGV 0x4C475600u
+#define ESM_TAG_WTH 0x57544800u
+
+namespace esm {
+
+// ---------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC11); stream layout documented in include/esmcuda.h and the design doc
+// ---------------------------------------------------------------------------------------------
+__host__ __device__ inline void philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                       uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32), lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+__host__ __device__ inline double u53(uint32_t a, uint32_t b) {
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+__host__ __device__ inline void uniform2(uint64_t seed, uint32_t tag, uint32_t c0, uint32_t c1, uint32_t c2,
+                                         uint32_t c3, double *u0, double *u1) {
+    uint32_t x[4];
+    philox((uint32_t)seed, (uint32_t)(seed >> 32) ^ tag, c0, c1, c2, c3, x);
+    *u0 = u53(x[0], x[1]);
+    *u1 = u53(x[2], x[3]);
+}
+
+__host__ __device__ inline double normal_at(uint64_t seed, uint32_t tag, uint32_t j, uint32_t c1, uint32_t c2,
+                                            uint32_t c3) {
+    double u0, u1;
+    uniform2(seed, tag, j >> 1, c1, c2, c3, &u0, &u1);
+    double rr = sqrt(-2.0 * log(1.0 - u0));
+    double a = 6.283185307179586 * u1;
+    return (j & 1) ? rr * sin(a) : rr * cos(a);
+}
+
+template <class real>
+__host__ __device__ inline real clampr(real x, real lo, real hi) {
+    return x < lo ? lo : (x > hi ? hi : x);
+}
+
+// ---------------------------------------------------------------------------------------------
+// device model: static tables and the state of one chain (R replicas), (X, T, R) layouts
+// ---------------------------------------------------------------------------------------------
+template <class real>
+struct DevModel {
+    int N, L, T, R, K, D, S, n0, nreg, nfields, nlev, natoms, nextra, span, maxpts;
+    int maxe, maxl, maxn, maxk, maxku, maxstu;   // descriptor capacities per move
+    real dt, c_shed, c_dump, c_viol, kappa0, beta_v, maxnats, kmin;
+    uint64_t seed;
+    double cumw[ESM_NFAM];   // family and cell-level draws compare in FP64 in both precisions
+    // network
+    const int *bus0, *bus1;
+    const real *lb, *ls;
+    const int *nlp, *nl;
+    const int *comp, *theta_nnz;
+    const real *Z;
+    // dispatchable units (index j in 0..D-1) and storage units (0..S-1)
+    const int *d_bus, *d_group;
+    const real *d_avail, *d_mc;
+    const real *kc_d;                 // clamped capacities of the dispatchable units
+    const int *s_bus;
+    const real *s_hours, *s_etain, *s_etaout, *s_qt, *s_mc;
+    const real *kc_s;
+    // move tables
+    const int *frole, *fap, *ap, *ai;
+    const real *av;
+    const int *up, *ua, *sp, *sa;
+    const double *qcum;
+    const int *clp, *cp, *cu;
+    const int *xpp, *xp, *xnp, *xn, *xlp, *xln;
+    const real *xv, *xlg;
+    // renewable units (0..Nren-1) and the weather
+    int Nren;
+    const int *r_bus, *r_series;
+    const real *r_mc, *kc_r;
+    const real *xbar, *wscale;   // [n0*T], [n0]; load of node n is series n
+    // flat units (0..K-1): kind, index within its kind, and the units of every node (CSR)
+    const int *u_kind, *u_loc;
+    const int *nu_ptr, *nu_unit;
+    // lines by their first bus (CSR), for node-parallel passes
+    const int *lb0_ptr, *lb0_line;
+    // state
+    real *theta, *g, *e, *r, *F, *z;
+};
+
+__host__ __device__ inline size_t sidx(int x, int t, int rep, int T, int R) { return ((size_t)x * T + t) * R + rep; }
+
+// cost pieces (src/local.jl:760 gen_cost, src/energy.jl:448 soc_cost, src/local.jl:773 phibal)
+template <class real>
+__device__ inline real gen_cost(real mc, real A, real k, real w, real dt, real cv, real y, real *p) {
+    real yc = clampr<real>(y, 0, 1);
+    *p = A * k * yc;
+    return dt * mc * (*p) + cv * dt * w * fabs(y - yc);
+}
+
+template <class real>
+__device__ inline real soc_cost(real h, real qt, real etain, real etaout, real mc, real k, real w, real dt, real cv,
+                                real ye, real ye1, real *dout, real *jout) {
+    real ec = clampr<real>(ye, 0, 1), ec1 = clampr<real>(ye1, 0, 1);
+    real d = h * (ec1 - ec) / dt - qt;
+    real pc, mcx;
+    if (d >= 0) {
+        pc = etain > 0 ? d / etain : real(0);
+        mcx = 0;
+    } else {
+        pc = 0;
+        mcx = fmin(-d * etaout, real(1));
+    }
+    real c = dt * mc * k * (pc + mcx) + cv * w * h * fabs(ye - ec);
+    if (pc > 1) c += cv * dt * w * (pc - 1);
+    if (d < 0 && qt <= 0) {
+        real ex = -d * etaout - real(1);
+        if (ex > 0) c += cv * dt * w * ex;
+    }
+    if (d >= 0 && etain <= 0) c += cv * dt * w * d;
+    *dout = d;
+    *jout = k * (pc - mcx);
+    return c;
+}
+
+template <class real>
+__device__ inline real phibal(real x, real cs, real cd) {
+    return x > 0 ? cs * x : -cd * x;
+}
+
+}  // namespace esm

@@ -1,0 +1,22 @@
+// Explicit instantiation of the kernels for float.
+#include "esm_kernels_impl.cuh"
+#include "esm_launch.cuh"
+#include "esm_linemove_impl.cuh"
+
+namespace esm {
+template size_t linemove_scratch_reals<float>(const DevModel<float> &);
+template size_t linemove_smem_per_warp<float>(const DevModel<float> &);
+template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int *, int, uint32_t, int, float *, int,
+                                              unsigned long long *, cudaStream_t);
+template cudaError_t launch_rebuild<float>(const DevModel<float> &, cudaStream_t);
+template cudaError_t launch_scores<float>(const DevModel<float> &, double *, double *, cudaStream_t);
+template cudaError_t launch_score_finish<float>(const DevModel<float> &, const double *, const double *, const double *,
+                                                const double *, double, double, int, double *, double *, double *,
+                                                double *, cudaStream_t);
+template cudaError_t launch_follow_disp<float>(const DevModel<float> &, const int *, const double *, const double *,
+                                               const double *, const double *, cudaStream_t);
+template cudaError_t launch_kop<float>(const DevModel<float> &, const double *, const double *, const double *,
+                                       const double *, double, cudaStream_t);
+template cudaError_t launch_set_kc<float>(int, const double *, const double *, const double *, const int *,
+                                          const int *, float *, float *, float *, cudaStream_t);
+}  // namespace esm

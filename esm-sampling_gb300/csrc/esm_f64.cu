@@ -1,0 +1,22 @@
+// Explicit instantiation of the kernels for double.
+#include "esm_kernels_impl.cuh"
+#include "esm_launch.cuh"
+#include "esm_linemove_impl.cuh"
+
+namespace esm {
+template size_t linemove_scratch_reals<double>(const DevModel<double> &);
+template size_t linemove_smem_per_warp<double>(const DevModel<double> &);
+template cudaError_t launch_class_pass<double>(const DevModel<double> &, const int *, int, uint32_t, int, double *, int,
+                                              unsigned long long *, cudaStream_t);
+template cudaError_t launch_rebuild<double>(const DevModel<double> &, cudaStream_t);
+template cudaError_t launch_scores<double>(const DevModel<double> &, double *, double *, cudaStream_t);
+template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *, const double *,
+                                                const double *, double, double, int, double *, double *, double *,
+                                                double *, cudaStream_t);
+template cudaError_t launch_follow_disp<double>(const DevModel<double> &, const int *, const double *, const double *,
+                                               const double *, const double *, cudaStream_t);
+template cudaError_t launch_kop<double>(const DevModel<double> &, const double *, const double *, const double *,
+                                       const double *, double, cudaStream_t);
+template cudaError_t launch_set_kc<double>(int, const double *, const double *, const double *, const int *,
+                                          const int *, double *, double *, double *, cudaStream_t);
+}  // namespace esm

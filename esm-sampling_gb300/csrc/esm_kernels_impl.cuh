@@ -1,0 +1,424 @@
+// HBM-bound node-parallel passes of the replica step: cache rebuild, energy and capacity score,
+// Langevin step, dispatch following. One thread per (node, step, replica) or (node, step-chunk,
+// replica), the replica index fastest so that every load is coalesced over a warp.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "esm_common.cuh"
+
+namespace esm {
+
+template <class real>
+__device__ inline real wraw(const DevModel<real> &M, int s, int t, int rep) {
+    return M.xbar[(size_t)s * M.T + t] + M.wscale[s] * M.z[sidx(s, t, rep, M.T, M.R)];
+}
+template <class real>
+__device__ inline real avail_map(real x) {  // logistic availability map (builder decision of the synthetic model)
+    return real(1) / (real(1) + exp(-x));
+}
+
+// ---------------------------------------------------------------------------------------------
+// LocalCost rebuild (src/local.jl:313, rebuild_step! :332): residual per node, flows per line.
+// Accumulation order per node as the reference: load, lines, generators, storage.
+// ---------------------------------------------------------------------------------------------
+template <class real>
+__global__ void k_rebuild(DevModel<real> M) {
+    size_t TR = (size_t)M.T * M.R;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M.N * TR) return;
+    int n = (int)(i / TR);
+    size_t tr = i % TR;
+    int t = (int)(tr / M.R), rep = (int)(tr % M.R);
+    int T = M.T, R = M.R;
+    real x = wraw(M, n, t, rep);
+    real r = x > 0 ? x : real(0);
+    for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) {
+        int e = M.nl[p];
+        int a = M.bus0[e], b = M.bus1[e];
+        real fl = M.lb[e] * (M.theta[sidx(a, t, rep, T, R)] - M.theta[sidx(b, t, rep, T, R)]);
+        if (a == n) {
+            M.F[sidx(e, t, rep, T, R)] = fl;
+            r += fl + real(0.5) * real(0);
+        } else {
+            r += -fl + real(0.5) * real(0);
+        }
+    }
+    for (int p = M.nu_ptr[n]; p < M.nu_ptr[n + 1]; ++p) {
+        int u = M.nu_unit[p], j = M.u_loc[u];
+        int kd = M.u_kind[u];
+        if (kd == ESM_UNIT_REN) {
+            real A = avail_map<real>(wraw(M, M.r_series[j], t, rep));
+            r -= A * M.kc_r[j] * real(1);
+        } else if (kd == ESM_UNIT_DISP) {
+            real y = clampr<real>(M.g[sidx(j, t, rep, T, R)], 0, 1);
+            r -= M.d_avail[j] * M.kc_d[j] * y;
+        }
+    }
+    for (int p = M.nu_ptr[n]; p < M.nu_ptr[n + 1]; ++p) {
+        int u = M.nu_unit[p], j = M.u_loc[u];
+        if (M.u_kind[u] != ESM_UNIT_STOR) continue;
+        real ec = clampr<real>(M.e[sidx(j, t, rep, T, R)], 0, 1);
+        real ec1 = clampr<real>(M.e[sidx(j, (t + 1) % T, rep, T, R)], 0, 1);
+        real d = M.s_hours[j] * (ec1 - ec) / M.dt - M.s_qt[j];
+        real pc, mcx;
+        if (d >= 0) {
+            pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : real(0);
+            mcx = 0;
+        } else {
+            pc = 0;
+            mcx = fmin(-d * M.s_etaout[j], real(1));
+        }
+        r += M.kc_s[j] * (pc - mcx);
+    }
+    M.r[i] = r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// energy cost and capacity gradient (src/energy.jl:551-757: gen_grad :835, soc_grad :466), per
+// (node, step chunk, replica), partial sums in FP64 added atomically per (replica, unit).
+// acc layout: dk [R*K], then parts [R*8] (capex, op, gen, storage, shed, dump, penalty, -)
+// ---------------------------------------------------------------------------------------------
+template <class real>
+__global__ void k_scores(DevModel<real> M, int tchunk, double *dk_out, double *parts_out) {
+    int n = blockIdx.x;
+    int c = blockIdx.y;
+    int rep = blockIdx.z * blockDim.x + threadIdx.x;
+    if (rep >= M.R) return;
+    int T = M.T, R = M.R;
+    int t0 = c * tchunk, t1 = min(T, t0 + tchunk);
+    real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
+    const int MAXU = 8;
+    double dk[MAXU];
+    double dkbox[MAXU];
+    int nu = M.nu_ptr[n + 1] - M.nu_ptr[n];
+    for (int q = 0; q < MAXU; ++q) dk[q] = dkbox[q] = 0;
+    double cgen = 0, cst = 0, pen = 0, shed = 0, dump = 0;
+    for (int t = t0; t < t1; ++t) {
+        real rr = M.r[sidx(n, t, rep, T, R)];
+        real Gn = dt * (rr > 0 ? M.c_shed : (rr < 0 ? -M.c_dump : real(0)));
+        if (rr > 0)
+            shed += (double)(dt * rr);
+        else
+            dump -= (double)(dt * rr);
+        for (int p = M.lb0_ptr[n]; p < M.lb0_ptr[n + 1]; ++p) {
+            int e = M.lb0_line[p];
+            real fe = M.F[sidx(e, t, rep, T, R)];
+            pen += (double)(cv * dt * (M.ls[e] * fmax(fabs(fe) / M.ls[e] - real(1), real(0))));
+        }
+        for (int q = 0; q < nu && q < MAXU; ++q) {
+            int u = M.nu_unit[M.nu_ptr[n] + q], j = M.u_loc[u];
+            int kd = M.u_kind[u];
+            if (kd == ESM_UNIT_REN) {
+                real A = avail_map<real>(wraw(M, M.r_series[j], t, rep));
+                real p_ = A * M.kc_r[j] * real(1);
+                cgen += (double)(dt * (M.r_mc[j] * p_));
+                real dck = M.r_mc[j] * A * real(1);
+                dk[q] += (double)(dt * dck - A * real(1) * Gn);
+            } else if (kd == ESM_UNIT_DISP) {
+                real A = M.d_avail[j], kv = M.kc_d[j];
+                real Y = M.g[sidx(j, t, rep, T, R)];
+                real Yc = clampr<real>(Y, 0, 1);
+                real p_ = A * kv * Yc;
+                cgen += (double)(dt * (M.d_mc[j] * p_));
+                real ex = fabs(Y - Yc);
+                if (ex > 0) pen += (double)(cv * dt * (kv + k0) * ex);
+                if (!(real(0) < Y && Y < real(1))) dk[q] += (double)(cv * dt * fabs(Y - Yc));
+                real dck = M.d_mc[j] * A * Yc;
+                dk[q] += (double)(dt * dck - A * Yc * Gn);
+            } else {
+                real kv = M.kc_s[j];
+                real h = M.s_hours[j];
+                real ye = M.e[sidx(j, t, rep, T, R)], ye1 = M.e[sidx(j, (t + 1) % T, rep, T, R)];
+                real dd, jj;
+                real cc = soc_cost<real>(h, M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], kv, kv + k0, dt, cv, ye,
+                                         ye1, &dd, &jj);
+                real Ec = clampr<real>(ye, 0, 1), Ec1 = clampr<real>(ye1, 0, 1);
+                real d = h * (Ec1 - Ec) / dt - M.s_qt[j];
+                real pc, mcx;
+                if (d >= 0) {
+                    pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : real(0);
+                    mcx = 0;
+                } else {
+                    pc = 0;
+                    mcx = fmin(-d * M.s_etaout[j], real(1));
+                }
+                real run = dt * M.s_mc[j] * kv * (pc + mcx);
+                cst += (double)run;
+                pen += (double)(cc - run);
+                // soc_grad (src/energy.jl:470-491)
+                real g = Gn;
+                if (d >= 0 && M.s_etain[j] <= 0) {
+                    dk[q] += (double)(cv * dt * d);
+                } else if (d >= 0) {
+                    real pcc = d / M.s_etain[j];
+                    dk[q] += (double)(dt * M.s_mc[j] * pcc + g * pcc + (pcc > 1 ? cv * dt * (pcc - 1) : real(0)));
+                } else {
+                    real mc_ = -d * M.s_etaout[j];
+                    real mcc = fmin(mc_, real(1));
+                    dk[q] += (double)(dt * M.s_mc[j] * mcc - g * mcc +
+                                      ((mc_ > 1 && M.s_qt[j] <= 0) ? cv * dt * (mc_ - 1) : real(0)));
+                }
+                if (!(real(0) < ye && ye < real(1))) dkbox[q] += (double)(cv * h * fabs(ye - Ec));
+            }
+        }
+    }
+    for (int q = 0; q < nu && q < MAXU; ++q) {
+        int u = M.nu_unit[M.nu_ptr[n] + q];
+        atomicAdd(&dk_out[(size_t)rep * M.K + u], dk[q] + dkbox[q]);
+    }
+    double *P = parts_out + (size_t)rep * 8;
+    atomicAdd(&P[2], cgen);
+    atomicAdd(&P[3], cst);
+    atomicAdd(&P[4], shed);
+    atomicAdd(&P[5], dump);
+    atomicAdd(&P[6], pen);
+}
+
+// capacity_scores (src/replicas.jl:329): sk = -beta_v mask dk + log-measure gradient; fk = beta_k dK/dk;
+// parts: capex and op. One thread per (replica, unit); k_raw in FP64.
+template <class real>
+__global__ void k_score_finish(DevModel<real> M, const double *k_raw, const double *u_lo, const double *u_hi,
+                               const double *u_capex, double gamma_k, double beta_k, int physical, double *dk,
+                               double *sk, double *fk, double *parts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int K = M.K;
+    if (i < M.R * K) {
+        int rep = i / K, u = i % K;
+        double y = k_raw[u];
+        bool in = u_lo[u] < y && y < u_hi[u];
+        double s = -(double)M.beta_v * ((in ? 1.0 : 0.0) * dk[i]);
+        double lm = 0.0;
+        if (physical && M.u_kind[u] != ESM_UNIT_REN && in) lm = (double)M.T / (y + (double)M.kappa0);
+        sk[i] = s + lm;
+        (void)rep;
+    }
+    if (i < K) {
+        double kc = fmin(fmax(k_raw[i], u_lo[i]), u_hi[i]);
+        double ex = k_raw[i] - kc;
+        double sg = ex > 0 ? 1.0 : (ex < 0 ? -1.0 : 0.0);
+        fk[i] = beta_k * (u_capex[i] + gamma_k * u_capex[i] * sg);
+    }
+    if (i < M.R) {
+        double capex = 0.0;
+        for (int u = 0; u < K; ++u) {
+            double kc = fmin(fmax(k_raw[u], u_lo[u]), u_hi[u]);
+            capex += u_capex[u] * k_raw[u] + gamma_k * u_capex[u] * fabs(k_raw[u] - kc);
+        }
+        double *P = parts + (size_t)i * 8;
+        P[0] = capex;
+        P[1] = P[2] + P[3] + ((double)M.c_shed * P[4] + (double)M.c_dump * P[5]) + P[6];
+        P[7] = 0.0;
+    }
+}
+
+// set_dispatchable_capacity! (src/replicas.jl:412): utilisations scaled by c(k0)/c(k1) at every step
+template <class real>
+__global__ void k_follow_disp(DevModel<real> M, const int *disp, const double *kold, const double *knew,
+                              const double *u_lo, const double *u_hi) {
+    size_t TR = (size_t)M.T * M.R;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M.D * TR) return;
+    int j = (int)(i / TR);
+    int u = disp[j];
+    double kc0 = fmin(fmax(kold[u], u_lo[u]), u_hi[u]), kc1 = fmin(fmax(knew[u], u_lo[u]), u_hi[u]);
+    double sc = kc0 == kc1 ? 1.0 : kc0 / kc1;  // kc_ratio (src/local.jl:2119)
+    if (sc == 1.0) return;
+    real y = M.g[i];
+    M.g[i] = y + y * (real)(sc - 1);
+}
+
+// kop curve of the renewable and storage units of one node (kop_term / kop_eval with commit,
+// src/kop.jl:79-160; follow_capacities! src/replicas.jl:456-470), per (node, step, replica), units in
+// flat order. kold/knew raw capacities (FP64); kc of the dispatchable units already updated.
+template <class real>
+__global__ void k_kop(DevModel<real> M, const double *kold, const double *k1v, const double *u_lo,
+                      const double *u_hi, double kmin) {
+    size_t TR = (size_t)M.T * M.R;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M.N * TR) return;
+    int n = (int)(i / TR);
+    size_t tr = i % TR;
+    int t = (int)(tr / M.R), rep = (int)(tr % M.R);
+    int T = M.T, R = M.R;
+    for (int p = M.nu_ptr[n]; p < M.nu_ptr[n + 1]; ++p) {
+        int u = M.nu_unit[p], j = M.u_loc[u];
+        int kd = M.u_kind[u];
+        if (kd == ESM_UNIT_DISP) continue;
+        double k0raw = kold[u];
+        double kc0 = fmin(fmax(k0raw, u_lo[u]), u_hi[u]);
+        double kc1 = fmin(fmax(k1v[u], u_lo[u]), u_hi[u]);
+        real jinj;
+        if (kd == ESM_UNIT_REN) {
+            jinj = avail_map<real>(wraw(M, M.r_series[j], t, rep));
+        } else {
+            real ec = clampr<real>(M.e[sidx(j, t, rep, T, R)], 0, 1);
+            real ec1 = clampr<real>(M.e[sidx(j, (t + 1) % T, rep, T, R)], 0, 1);
+            real d = M.s_hours[j] * (ec1 - ec) / M.dt - M.s_qt[j];
+            real pc, mcx;
+            if (d >= 0) {
+                pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : real(0);
+                mcx = 0;
+            } else {
+                pc = 0;
+                mcx = fmin(-d * M.s_etaout[j], real(1));
+            }
+            jinj = mcx - pc;
+        }
+        real dkc = (real)(kc1 - kc0);
+        real dinj = jinj * dkc;
+        real dS = -dinj;
+        if (k0raw >= kmin) {  // below kmin: the capacity alone, no following (src/replicas.jl:461)
+            real Pt = 0, Qs = 0;
+            int nu = 0;
+            for (int q = M.up[n]; q < M.up[n + 1]; ++q) {
+                int jd = M.ua[q];
+                real kap = M.d_avail[jd] * M.kc_d[jd];
+                if (!(fabs(kap) >= (real)kmin)) continue;
+                real om = M.g[sidx(jd, t, rep, T, R)];
+                Pt += kap * om;
+                Qs += kap * clampr<real>(om, 0, 1);
+                nu += 1;
+            }
+            if (!(nu == 0 || fabs(Pt) < real(1e-6))) {
+                real Q = M.r[i] + Qs;
+                real e = Pt - fmax(Q, real(0));
+                real P1 = fmax(Q - dinj, real(0)) + e;
+                for (int q = M.up[n]; q < M.up[n + 1]; ++q) {
+                    int jd = M.ua[q];
+                    real kap = M.d_avail[jd] * M.kc_d[jd];
+                    if (!(fabs(kap) >= (real)kmin)) continue;
+                    size_t gi = sidx(jd, t, rep, T, R);
+                    real y0 = M.g[gi];
+                    real sigma = kap * y0 / Pt;
+                    real y1 = sigma * P1 / kap;
+                    dS -= kap * (clampr<real>(y1, 0, 1) - clampr<real>(y0, 0, 1));
+                    M.g[gi] = y1;
+                }
+            }
+        }
+        M.r[i] += dS;
+    }
+}
+
+// refresh the clamped capacities (real) from the raw FP64 capacities
+template <class real>
+__global__ void k_set_kc(int K, const double *k_raw, const double *u_lo, const double *u_hi, const int *u_kind,
+                         const int *u_loc, real *kc_d, real *kc_s, real *kc_r) {
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= K) return;
+    real kc = (real)fmin(fmax(k_raw[u], u_lo[u]), u_hi[u]);
+    int j = u_loc[u];
+    if (u_kind[u] == ESM_UNIT_DISP)
+        kc_d[j] = kc;
+    else if (u_kind[u] == ESM_UNIT_STOR)
+        kc_s[j] = kc;
+    else
+        kc_r[j] = kc;
+}
+
+#ifdef ESM_COMMON_KERNELS
+// ---------------------------------------------------------------------------------------------
+// Langevin step of the shared capacities (langevin_capacities / langevin_update,
+// src/replicas.jl:368-403), FP64, one thread per unit; replica average in replica order (:697)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_langevin(int K, int R, const int *u_group, const int *u_gidx, const double *k_raw, const double *sk,
+                           const double *fk, const double *w, const double *eta, const double *kappa_s, double ratio,
+                           double kmin, double clip, int box, const double *u_hi, const double *xi, uint64_t seed,
+                           uint32_t it, double *knew, int *nclip) {
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= K) return;
+    int gidx = u_group[u];
+    double k = k_raw[u];
+    if (eta[gidx] == 0) {
+        knew[u] = k;
+        return;
+    }
+    double sbar = 0.0;
+    for (int rep = 0; rep < R; ++rep) sbar += w[rep] * sk[(size_t)rep * K + u];
+    double g = -fk[u] + ratio * sbar;
+    double x = xi ? xi[u] : normal_at(seed, ESM_TAG_LGV, (uint32_t)u_gidx[u], (uint32_t)gidx, it, 0);
+    double ks = kappa_s[gidx], et = eta[gidx];
+    double wv = log(k + ks);
+    double dw0 = et * ((k + ks) * g + 1);
+    if (fabs(dw0) > clip) atomicAdd(nclip, 1);
+    double w1 = wv + fmin(fmax(dw0, -clip), clip) + sqrt(2 * et) * x;
+    double wmin = log(kmin + ks);
+    w1 = w1 < wmin ? 2 * wmin - w1 : w1;
+    if (box) {
+        double wmax = log(fmax(u_hi[u], kmin + 1.0) + ks);
+        if (w1 > wmax && wv <= wmax) w1 = fmax(2 * wmax - w1, wmin);
+    }
+    knew[u] = exp(w1) - ks;
+}
+
+// k after following: renewables and storage k0 exp(log(k'/k0)) (kop_commit!, src/kop.jl:254),
+// or k' when k0 < kmin; dispatchable k'
+__global__ void k_kop_capacity(int K, const int *u_kind, const double *kold, const double *knew, double kmin,
+                               double *k1) {
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= K) return;
+    if (u_kind[u] == ESM_UNIT_DISP || kold[u] < kmin)
+        k1[u] = knew[u];
+    else
+        k1[u] = kold[u] * exp(log(knew[u] / kold[u]));
+}
+
+#endif
+
+// ---------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------
+template <class real>
+cudaError_t launch_rebuild(const DevModel<real> &M, cudaStream_t s) {
+    size_t n = (size_t)M.N * M.T * M.R;
+    k_rebuild<real><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_scores(const DevModel<real> &M, double *dk, double *parts, cudaStream_t s) {
+    int tchunk = 128;
+    int nch = (M.T + tchunk - 1) / tchunk;
+    int bx = M.R < 64 ? M.R : 64;
+    dim3 grid(M.N, nch, (M.R + bx - 1) / bx);
+    k_scores<real><<<grid, bx, 0, s>>>(M, tchunk, dk, parts);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_score_finish(const DevModel<real> &M, const double *k_raw, const double *lo, const double *hi,
+                                const double *capex, double gamma_k, double beta_k, int physical, double *dk,
+                                double *sk, double *fk, double *parts, cudaStream_t s) {
+    int n = M.R * M.K;
+    if (n < M.K) n = M.K;
+    k_score_finish<real><<<(n + 127) / 128, 128, 0, s>>>(M, k_raw, lo, hi, capex, gamma_k, beta_k, physical, dk, sk,
+                                                          fk, parts);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_follow_disp(const DevModel<real> &M, const int *disp, const double *kold, const double *knew,
+                               const double *lo, const double *hi, cudaStream_t s) {
+    size_t n = (size_t)M.D * M.T * M.R;
+    k_follow_disp<real><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M, disp, kold, knew, lo, hi);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_kop(const DevModel<real> &M, const double *kold, const double *k1, const double *lo,
+                       const double *hi, double kmin, cudaStream_t s) {
+    size_t n = (size_t)M.N * M.T * M.R;
+    k_kop<real><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M, kold, k1, lo, hi, kmin);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_set_kc(int K, const double *k_raw, const double *lo, const double *hi, const int *u_kind,
+                          const int *u_loc, real *kc_d, real *kc_s, real *kc_r, cudaStream_t s) {
+    k_set_kc<real><<<(K + 127) / 128, 128, 0, s>>>(K, k_raw, lo, hi, u_kind, u_loc, kc_d, kc_s, kc_r);
+    return cudaGetLastError();
+}
+
+}  // namespace esm

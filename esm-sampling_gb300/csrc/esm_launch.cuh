@@ -1,0 +1,27 @@
+// Launchers of the templated kernels, instantiated for float in esm_f32.cu and for double in
+// esm_f64.cu (compiled without FMA contraction, the parity build).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "esm_common.cuh"
+#include "esm_linemove.cuh"
+
+namespace esm {
+template <class real>
+cudaError_t launch_rebuild(const DevModel<real> &M, cudaStream_t s);
+template <class real>
+cudaError_t launch_scores(const DevModel<real> &M, double *dk, double *parts, cudaStream_t s);
+template <class real>
+cudaError_t launch_score_finish(const DevModel<real> &M, const double *k_raw, const double *lo, const double *hi,
+                                const double *capex, double gamma_k, double beta_k, int physical, double *dk,
+                                double *sk, double *fk, double *parts, cudaStream_t s);
+template <class real>
+cudaError_t launch_follow_disp(const DevModel<real> &M, const int *disp, const double *kold, const double *knew,
+                               const double *lo, const double *hi, cudaStream_t s);
+template <class real>
+cudaError_t launch_kop(const DevModel<real> &M, const double *kold, const double *k1, const double *lo,
+                       const double *hi, double kmin, cudaStream_t s);
+template <class real>
+cudaError_t launch_set_kc(int K, const double *k_raw, const double *lo, const double *hi, const int *u_kind,
+                          const int *u_loc, real *kc_d, real *kc_s, real *kc_r, cudaStream_t s);
+}  // namespace esm

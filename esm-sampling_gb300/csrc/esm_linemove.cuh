@@ -1,0 +1,16 @@
+// Host entry points of the line-move class kernel (esm_linemove.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "esm_common.cuh"
+
+namespace esm {
+template <class real>
+size_t linemove_scratch_reals(const DevModel<real> &M);  // per warp
+template <class real>
+size_t linemove_smem_per_warp(const DevModel<real> &M);
+template <class real>
+cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
+                              real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s);
+}  // namespace esm

@@ -1,0 +1,1206 @@
+// Line-move colour-class kernel: the exact line-conditional dispatch moves of one parity class of
+// the local sweep (src/local.jl:1927 local_sweep!, the threaded body :1954-2051) for every replica.
+//
+// Mapping. A warp owns one "tile" (span consecutive steps of the class) and 32 (step, replica)
+// tasks of it, the replica index fastest, so that every state access of the warp is one coalesced
+// 128-byte line of the (X, T, R) arrays. All tasks of a tile run the same move list (the move
+// selection reads only capacities and static tables, src/local.jl:14 "selection uses only (k, x)"),
+// so the move's structure -- entries, lines, touched nodes, storage terms -- is warp-uniform and
+// is built once in shared memory; each lane then walks its own piecewise-exponential line
+// conditional (walk!, src/local.jl:1294) and draws t (sample_line!, :1501) with its own uniforms.
+// Per-lane walk buffers live in a global scratch slab, interleaved by lane (coalesced).
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "esm_common.cuh"
+#include "esm_linemove.cuh"
+
+namespace esm {
+
+// ---------------------------------------------------------------------------------------------
+// shared-memory descriptor of the current move of a warp
+// ---------------------------------------------------------------------------------------------
+struct Carve {
+    char *p;
+    __host__ __device__ explicit Carve(char *b) : p(b) {}
+    template <class U>
+    __host__ __device__ U *take(int n) {
+        size_t a = (size_t)p;
+        a = (a + 15) & ~(size_t)15;
+        U *out = (U *)a;
+        p = (char *)(a + sizeof(U) * (size_t)(n > 0 ? n : 1));
+        return out;
+    }
+};
+
+template <class real>
+struct Desc {
+    int *moves;
+    int *hdr;  // [0] ng, [1] nse, [2] nl, [3] nk, [4] nku, [5] nns, [6] nga, [7] nna, [8] nth, [9] valid, [10] fam
+    int *gi, *gpos;
+    real *ga;
+    int *si, *spos, *sposa;
+    real *sa;
+    int *thn;
+    real *tha;
+    int *li, *lpa, *lpb;
+    real *ldf;
+    int *kn;
+    real *kg;
+    int *ku, *kk, *kupos;
+    int *nds, *nda;
+    int *gia, *gposa;
+    real *gaa;
+    real *dth;
+    unsigned char *lmark, *nmarks, *nmarka;
+    int *posn_s, *posn_a;  // node -> position in the node lists (-1)
+};
+
+template <class real>
+__host__ __device__ inline Desc<real> carve_desc(char *base, const DevModel<real> &M, int nmoves) {
+    Carve c(base);
+    Desc<real> d;
+    d.moves = c.take<int>(nmoves);
+    d.hdr = c.take<int>(16);
+    d.gi = c.take<int>(M.maxe);
+    d.gpos = c.take<int>(M.maxe);
+    d.ga = c.take<real>(M.maxe);
+    d.si = c.take<int>(M.maxstu);
+    d.spos = c.take<int>(M.maxstu);
+    d.sposa = c.take<int>(M.maxstu);
+    d.sa = c.take<real>(M.maxstu);
+    d.thn = c.take<int>(M.N);
+    d.tha = c.take<real>(M.N);
+    d.li = c.take<int>(M.L);
+    d.lpa = c.take<int>(M.L);
+    d.lpb = c.take<int>(M.L);
+    d.ldf = c.take<real>(M.L);
+    d.kn = c.take<int>(M.maxk);
+    d.kg = c.take<real>(M.maxk);
+    d.ku = c.take<int>(M.maxku);
+    d.kk = c.take<int>(M.maxku);
+    d.kupos = c.take<int>(M.maxku);
+    d.nds = c.take<int>(M.N);
+    d.nda = c.take<int>(M.N);
+    d.gia = c.take<int>(4);
+    d.gposa = c.take<int>(4);
+    d.gaa = c.take<real>(4);
+    d.dth = c.take<real>(M.N);
+    d.lmark = c.take<unsigned char>(M.L);
+    d.nmarks = c.take<unsigned char>(M.N);
+    d.nmarka = c.take<unsigned char>(M.N);
+    d.posn_s = c.take<int>(M.N);
+    d.posn_a = c.take<int>(M.N);
+    return d;
+}
+
+template <class real>
+size_t desc_bytes(const DevModel<real> &M, int nmoves) {
+    // size by carving from an aligned base
+    char *base = (char *)(uintptr_t)4096;
+    Carve c(base);
+    c.take<int>(nmoves);
+    c.take<int>(16);
+    c.take<int>(M.maxe);
+    c.take<int>(M.maxe);
+    c.take<real>(M.maxe);
+    c.take<int>(M.maxstu);
+    c.take<int>(M.maxstu);
+    c.take<int>(M.maxstu);
+    c.take<real>(M.maxstu);
+    c.take<int>(M.N);
+    c.take<real>(M.N);
+    c.take<int>(M.L);
+    c.take<int>(M.L);
+    c.take<int>(M.L);
+    c.take<real>(M.L);
+    c.take<int>(M.maxk);
+    c.take<real>(M.maxk);
+    c.take<int>(M.maxku);
+    c.take<int>(M.maxku);
+    c.take<int>(M.maxku);
+    c.take<int>(M.N);
+    c.take<int>(M.N);
+    c.take<int>(4);
+    c.take<int>(4);
+    c.take<real>(4);
+    c.take<real>(M.N);
+    c.take<unsigned char>(M.L);
+    c.take<unsigned char>(M.N);
+    c.take<unsigned char>(M.N);
+    c.take<int>(M.N);
+    c.take<int>(M.N);
+    return (size_t)(c.p - base) + 16;
+}
+
+// per-lane scratch layout (reals), interleaved by lane within a warp slab
+struct LaneLayout {
+    int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua, total;
+};
+__host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxstu, int maxroots, int maxk, int maxku) {
+    LaneLayout L;
+    int o = 0;
+    L.pr = o; o += maxpts;
+    L.cr = o; o += maxpts;
+    L.pl = o; o += maxpts;
+    L.cl = o; o += maxpts;
+    L.lm = o; o += 2 * maxpts + 1;
+    L.drs = o; o += maxn;
+    L.dra = o; o += maxn;
+    L.sps = o; o += maxn;
+    L.spa = o; o += maxn;
+    L.dcs = o; o += maxstu;
+    L.dca = o; o += maxstu;
+    L.dps = o; o += maxstu;
+    L.dpa = o; o += maxstu;
+    L.ro = o; o += maxroots;
+    L.gro = o; o += maxroots;
+    L.kq = o; o += maxk;
+    L.ke = o; o += maxk;
+    L.kp = o; o += maxk;
+    L.knm = o; o += maxk;
+    L.kph = o; o += maxk;
+    L.kv = o; o += maxk;
+    L.kua = o; o += maxku;
+    L.total = o;
+    return L;
+}
+
+#define ESM_MAXROOTS 64
+
+// ---------------------------------------------------------------------------------------------
+// per-lane context
+// ---------------------------------------------------------------------------------------------
+template <class real>
+struct Lane {
+    const DevModel<real> &M;
+    Desc<real> &d;
+    real *slab;  // this warp's scratch slab
+    int lane;
+    LaneLayout LL;
+    int tau, taum, tau1, rep;
+    bool active;
+
+    __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int lane_, LaneLayout LL_)
+        : M(M_), d(d_), slab(slab_), lane(lane_), LL(LL_) {}
+
+    __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * 32 + lane]; }
+    __device__ inline size_t ix(int x, int t) const { return sidx(x, t, rep, M.T, M.R); }
+
+    // ------------------------------------------------------------------ evaluation of the move
+    // eval_move! (src/local.jl:789) of both steps (the later step first, as mv_eval! of a block
+    // move, :1219). Returns beta * DeltaC(t); fills d (storage) and dr (nodes) at t.
+    __device__ real eval(real t) const {
+        const int *hdr = d.hdr;
+        int ng = hdr[0], nse = hdr[1], nl = hdr[2], nk = hdr[3], nku = hdr[4], nns = hdr[5], nga = hdr[6],
+            nna = hdr[7];
+        real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
+        real D = 0;
+        // kinks (src/local.jl:605 update_kinks!)
+        for (int q = 0; q < nk; ++q) {
+            real Q = S(LL.kq, q);
+            S(LL.kph, q) = fmax(Q + d.kg[q] * t, real(0)) - fmax(Q, real(0));
+        }
+        // ---- step tau
+        for (int q = 0; q < nns; ++q) S(LL.drs, q) = 0;
+        for (int q = 0; q < ng; ++q) {
+            int j = d.gi[q];
+            real y0 = M.g[ix(j, tau)];
+            real k = M.kc_d[j], A = M.d_avail[j];
+            real y1 = y0 + t * d.ga[q];
+            real p0, p1;
+            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
+            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
+            D += c1 - c0;
+            S(LL.drs, d.gpos[q]) -= p1 - p0;
+        }
+        for (int q = 0; q < nku; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
+            real ak = S(LL.kua, q);
+            if (ak == 0) continue;
+            int j = d.ku[q];
+            real y0 = M.g[ix(j, tau)];
+            real k = M.kc_d[j], A = M.d_avail[j];
+            real y1 = y0 + (t * real(0) + ak * S(LL.kph, d.kk[q]));
+            real p0, p1;
+            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
+            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
+            D += c1 - c0;
+            S(LL.drs, d.kupos[q]) -= p1 - p0;
+        }
+        for (int q = 0; q < nl; ++q) {
+            int e = d.li[q];
+            real f0 = M.F[ix(e, tau)], f1 = f0 + t * d.ldf[q];
+            real se = M.ls[e];
+            D += cv * dt * (fmax(fabs(f1) - se, real(0)) - fmax(fabs(f0) - se, real(0)));
+            S(LL.drs, d.lpa[q]) += f1 - f0;
+            S(LL.drs, d.lpb[q]) -= f1 - f0;
+        }
+        for (int q = 0; q < nse; ++q) {
+            int j = d.si[q];
+            real k = M.kc_s[j], w = k + k0;
+            real ye = M.e[ix(j, tau)], ye1 = M.e[ix(j, tau1)];
+            real d0, j0, d1, j1;
+            real c0 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv, ye,
+                                     ye1, &d0, &j0);
+            real c1 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
+                                     ye + t * d.sa[q], ye1 + t * real(0), &d1, &j1);
+            D += c1 - c0;
+            S(LL.drs, d.spos[q]) += j1 - j0;
+            S(LL.dcs, q) = d1;
+        }
+        for (int q = 0; q < nns; ++q) {
+            real S0 = M.r[ix(d.nds[q], tau)];
+            real S1 = S0 + S(LL.drs, q);
+            D += dt * (phibal<real>(S1, M.c_shed, M.c_dump) - phibal<real>(S0, M.c_shed, M.c_dump));
+        }
+        // ---- step tau - 1 (linked storage terms: the end value moves with step tau)
+        for (int q = 0; q < nna; ++q) S(LL.dra, q) = 0;
+        for (int q = 0; q < nga; ++q) {
+            int j = d.gia[q];
+            real y0 = M.g[ix(j, taum)];
+            real k = M.kc_d[j], A = M.d_avail[j];
+            real y1 = y0 + t * d.gaa[q];
+            real p0, p1;
+            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
+            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
+            D += c1 - c0;
+            S(LL.dra, d.gposa[q]) -= p1 - p0;
+        }
+        for (int q = 0; q < nse; ++q) {
+            int j = d.si[q];
+            real k = M.kc_s[j], w = k + k0;
+            real ye = M.e[ix(j, taum)], ye1 = M.e[ix(j, tau)];
+            real d0, j0, d1, j1;
+            real c0 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv, ye,
+                                     ye1, &d0, &j0);
+            real c1 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
+                                     ye + t * real(0), ye1 + t * d.sa[q], &d1, &j1);
+            D += c1 - c0;
+            S(LL.dra, d.sposa[q]) += j1 - j0;
+            S(LL.dca, q) = d1;
+        }
+        for (int q = 0; q < nna; ++q) {
+            real S0 = M.r[ix(d.nda[q], taum)];
+            real S1 = S0 + S(LL.dra, q);
+            D += dt * (phibal<real>(S1, M.c_shed, M.c_dump) - phibal<real>(S0, M.c_shed, M.c_dump));
+        }
+        return M.beta_v * D;
+    }
+
+    // secondary quantities at the current point into the "previous" buffers
+    __device__ void save_prev() const {
+        int nse = d.hdr[1], nns = d.hdr[5], nna = d.hdr[7];
+        for (int q = 0; q < nse; ++q) {
+            S(LL.dps, q) = S(LL.dcs, q);
+            S(LL.dpa, q) = S(LL.dca, q);
+        }
+        for (int q = 0; q < nns; ++q) S(LL.sps, q) = M.r[ix(d.nds[q], tau)] + S(LL.drs, q);
+        for (int q = 0; q < nna; ++q) S(LL.spa, q) = M.r[ix(d.nda[q], taum)] + S(LL.dra, q);
+    }
+
+    // the three storage secondaries of a storage term (src/local.jl:885)
+    __device__ inline void stor_sec(int j, real dd, real out[3]) const {
+        real ein = M.s_etain[j];
+        out[0] = dd;
+        out[1] = ein > 0 ? dd - ein : real(1);
+        out[2] = -dd * M.s_etaout[j] - real(1);
+    }
+
+    __device__ inline static bool root_of(real a, real b, real lo, real hi, real sgn, real *x) {
+        if ((a < 0) != (b < 0) && a != b) {
+            real xx = lo + (hi - lo) * a / (a - b);
+            if (sgn * (xx - lo) > 0 && sgn * (hi - xx) > 0) {
+                *x = xx;
+                return true;
+            }
+        }
+        return false;
+    }
+
+    // collect sign changes between prev (at lo) and cur (at hi): storage ones into gro (if
+    // storage splitting applies), the others into ro. Returns false on root-buffer overflow.
+    __device__ bool collect(real lo, real hi, real sgn, bool stor, bool want_stor, bool want_other, int *nro,
+                            int *ngro) const {
+        int nse = d.hdr[1], nns = d.hdr[5], nna = d.hdr[7];
+        real x;
+        if (want_stor || !stor) {
+            for (int side = 0; side < 2; ++side)
+                for (int q = 0; q < nse; ++q) {
+                    real a3[3], b3[3];
+                    int j = d.si[q];
+                    stor_sec(j, side == 0 ? S(LL.dps, q) : S(LL.dpa, q), a3);
+                    stor_sec(j, side == 0 ? S(LL.dcs, q) : S(LL.dca, q), b3);
+                    for (int h = 0; h < 3; ++h)
+                        if (root_of(a3[h], b3[h], lo, hi, sgn, &x)) {
+                            if (stor) {
+                                if (*ngro >= ESM_MAXROOTS) return false;
+                                S(LL.gro, (*ngro)++) = x;
+                            } else {
+                                if (*nro >= ESM_MAXROOTS) return false;
+                                S(LL.ro, (*nro)++) = x;
+                            }
+                        }
+                }
+        }
+        if (want_other) {
+            for (int q = 0; q < nns; ++q) {
+                real b = M.r[ix(d.nds[q], tau)] + S(LL.drs, q);
+                if (root_of(S(LL.sps, q), b, lo, hi, sgn, &x)) {
+                    if (*nro >= ESM_MAXROOTS) return false;
+                    S(LL.ro, (*nro)++) = x;
+                }
+            }
+            for (int q = 0; q < nna; ++q) {
+                real b = M.r[ix(d.nda[q], taum)] + S(LL.dra, q);
+                if (root_of(S(LL.spa, q), b, lo, hi, sgn, &x)) {
+                    if (*nro >= ESM_MAXROOTS) return false;
+                    S(LL.ro, (*nro)++) = x;
+                }
+            }
+        }
+        return true;
+    }
+
+    __device__ void sort_buf(int off, int n, real sgn) const {  // insertion sort in walking order
+        for (int i = 1; i < n; ++i) {
+            real x = S(off, i);
+            int j = i - 1;
+            while (j >= 0 && (sgn > 0 ? x < S(off, j) : x > S(off, j))) {
+                S(off, j + 1) = S(off, j);
+                --j;
+            }
+            S(off, j + 1) = x;
+        }
+    }
+
+    // next primary breakpoint beyond tp in walking direction (finalize!, src/local.jl:656, scanned
+    // instead of sorted: the same sequence); returns false if none
+    __device__ bool next_bp(real tp, real sgn, real *out) const {
+        int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nk = d.hdr[3], nku = d.hdr[4], nga = d.hdr[6];
+        bool have = false;
+        real best = 0;
+        auto consider = [&](real x) {
+            if (!isfinite(x)) return;
+            if (!(sgn * x > 0)) return;
+            if (!(sgn * (x - tp) > 0)) return;
+            if (!have || sgn * (x - best) < 0) {
+                best = x;
+                have = true;
+            }
+        };
+        for (int q = 0; q < nk; ++q)
+            if (S(LL.kv, q) != 0 && d.kg[q] != 0) consider(-S(LL.kq, q) / d.kg[q]);
+        for (int q = 0; q < ng; ++q) {
+            real a = d.ga[q];
+            real y0 = M.g[ix(d.gi[q], tau)];
+            consider((real(0) - y0) / a);
+            consider((real(1) - y0) / a);
+        }
+        for (int q = 0; q < nse; ++q) {
+            real a = d.sa[q];
+            real y0 = M.e[ix(d.si[q], tau)];
+            consider((real(0) - y0) / a);
+            consider((real(1) - y0) / a);
+        }
+        for (int q = 0; q < nku; ++q) {
+            real ak = S(LL.kua, q);
+            if (ak == 0) continue;
+            int kq = d.kk[q];
+            real Q = S(LL.kq, kq), gk = d.kg[kq];
+            real y0 = M.g[ix(d.ku[q], tau)];
+            real a = 0;
+            real offs[4] = {real(0), real(0), -ak * Q, ak * Q};
+            real sls[4] = {a + ak * gk, a, a, a + ak * gk};
+            for (int h = 0; h < 4; ++h) {
+                if (sls[h] == 0) continue;
+                consider((real(0) - y0 - offs[h]) / sls[h]);
+                consider((real(1) - y0 - offs[h]) / sls[h]);
+            }
+        }
+        for (int q = 0; q < nga; ++q) {
+            real a = d.gaa[q];
+            real y0 = M.g[ix(d.gia[q], taum)];
+            consider((real(0) - y0) / a);
+            consider((real(1) - y0) / a);
+        }
+        for (int q = 0; q < nl; ++q) {
+            int e = d.li[q];
+            real f0 = M.F[ix(e, tau)], df = d.ldf[q], se = M.ls[e];
+            consider((real(1) * se - f0) / df);
+            consider((real(-1) * se - f0) / df);
+        }
+        *out = best;
+        return have;
+    }
+
+    // piece_roots! (src/local.jl:1267) between prev (at a) and cur (at b); evaluates the roots
+    __device__ bool piece_roots(int pofs, int cofs, int *np, real a, real b, real sgn, real *cmin) const {
+        int nro = 0, ngro = 0;
+        if (!collect(a, b, sgn, true, false, true, &nro, &ngro)) return false;
+        if (nro == 0) return true;
+        sort_buf(LL.ro, nro, sgn);
+        for (int i = 0; i < nro; ++i) {
+            real x = S(LL.ro, i);
+            real cx = eval(x);
+            if (*np >= M.maxpts) return false;
+            S(pofs, *np) = x;
+            S(cofs, *np) = cx;
+            ++*np;
+            *cmin = fmin(*cmin, cx);
+        }
+        return true;
+    }
+
+    // walk! (src/local.jl:1294), plain model. Returns 1 proper, 0 improper, -1 buffer overflow.
+    __device__ int walk(int pofs, int cofs, int *np, real sgn) const {
+        bool stor = d.hdr[1] > 0;
+        real tp = 0, cmin = 0, delta = 0;
+        int nx = 0;
+        *np = 0;
+        eval(real(0));
+        save_prev();
+        while (true) {
+            real t;
+            if (!next_bp(tp, sgn, &t)) {
+                real cprev = *np == 0 ? real(0) : S(cofs, *np - 1);
+                real hp = real(1e-6) * fmax(real(1), fabs(tp));
+                real sl = (eval(tp + sgn * hp) + real(0) - cprev - real(0)) / hp;
+                if (sl > 0)
+                    delta = fmin(real(2) * M.maxnats / sl, real(1e3) * fmax(fabs(tp), real(1e-3)));
+                else
+                    delta = delta == 0 ? fmax(fabs(tp), real(1e-6)) : real(2) * delta;
+                t = tp + sgn * delta;
+                nx += 1;
+                if (nx > 80) return 0;
+            }
+            real c = eval(t);
+            int nro = 0, ngro = 0;
+            if (!collect(tp, t, sgn, stor, true, !stor, &nro, &ngro)) return -1;
+            // when storage splitting applies, the other roots are found per piece below
+            if (stor && ngro > 0) {
+                sort_buf(LL.gro, ngro, sgn);
+                real a0 = tp;
+                for (int i = 0; i < ngro; ++i) {
+                    real x = S(LL.gro, i);
+                    real cx = eval(x);
+                    if (!piece_roots(pofs, cofs, np, a0, x, sgn, &cmin)) return -1;
+                    eval(x);  // restore the secondaries at x
+                    if (*np >= M.maxpts) return -1;
+                    S(pofs, *np) = x;
+                    S(cofs, *np) = cx;
+                    ++*np;
+                    cmin = fmin(cmin, cx);
+                    save_prev();
+                    a0 = x;
+                }
+                eval(t);
+                if (!piece_roots(pofs, cofs, np, a0, t, sgn, &cmin)) return -1;
+                eval(t);
+                save_prev();
+            } else {
+                if (stor) {  // no storage root: the other secondaries over the whole segment
+                    if (!collect(tp, t, sgn, true, false, true, &nro, &ngro)) return -1;
+                }
+                save_prev();
+                if (nro > 0) {
+                    sort_buf(LL.ro, nro, sgn);
+                    for (int i = 0; i < nro; ++i) {
+                        real x = S(LL.ro, i);
+                        real cx = eval(x);
+                        if (*np >= M.maxpts) return -1;
+                        S(pofs, *np) = x;
+                        S(cofs, *np) = cx;
+                        ++*np;
+                        cmin = fmin(cmin, cx);
+                    }
+                }
+            }
+            if (*np >= M.maxpts) return -1;
+            S(pofs, *np) = t;
+            S(cofs, *np) = c;
+            ++*np;
+            cmin = fmin(cmin, c);
+            if (c + real(0) - cmin > M.maxnats) return 1;
+            tp = t;
+        }
+    }
+
+    // logseg, trexp_offset (src/local.jl:1099, :1106)
+    __device__ static real logseg(real L, real x) {
+        if (fabs(x) < real(1e-10)) return log(L) - x / 2;
+        if (x > 0) return log(L) + log(-expm1(-x)) - log(x);
+        return log(L) - x + log(-expm1(x)) - log(-x);
+    }
+    __device__ static real trexp_offset(real u, real g, real L) {
+        real x = g * L;
+        if (fabs(x) < real(1e-10)) return u * L;
+        if (g > 0) return -log1p(-u * (-expm1(-x))) / g;
+        return L + log1p(-u * (-expm1(x))) / (-g);
+    }
+
+    __device__ inline real P(int i, int nl) const {  // merged points: left reversed, 0, right
+        if (i < nl) return S(LL.pl, nl - 1 - i);
+        if (i == nl) return 0;
+        return S(LL.pr, i - nl - 1);
+    }
+    __device__ inline real Cc(int i, int nl) const {
+        if (i < nl) return S(LL.cl, nl - 1 - i);
+        if (i == nl) return 0;
+        return S(LL.cr, i - nl - 1);
+    }
+
+    // sample_line! (src/local.jl:1501); *guard on buffer overflow (t = 0)
+    __device__ real sample_line(real ucat, real uoff, bool *guard) const {
+        *guard = false;
+        int nr = 0, nl = 0;
+        int w = walk(LL.pr, LL.cr, &nr, real(1));
+        if (w < 0) {
+            *guard = true;
+            return 0;
+        }
+        if (w == 0) return 0;
+        w = walk(LL.pl, LL.cl, &nl, real(-1));
+        if (w < 0) {
+            *guard = true;
+            return 0;
+        }
+        if (w == 0) return 0;
+        int npt = nl + 1 + nr;
+        int nseg = npt - 1;
+        real mx = -INFINITY;
+        for (int j = 0; j < nseg; ++j) {
+            real p0 = P(j, nl), p1 = P(j + 1, nl), c0 = Cc(j, nl), c1 = Cc(j + 1, nl);
+            real L = p1 - p0;
+            real lm = L > 0 ? -fmin(c0, c1) + logseg(L, fabs(c1 - c0)) : real(-INFINITY);
+            S(LL.lm, j) = lm;
+            mx = fmax(mx, lm);
+        }
+        real tot = 0;
+        for (int j = 0; j < nseg; ++j) tot += exp(S(LL.lm, j) - mx);
+        real u = ucat * tot, acc = 0;
+        int jj = nseg - 1;
+        for (int q = 0; q < nseg; ++q) {
+            acc += exp(S(LL.lm, q) - mx);
+            if (u <= acc) {
+                jj = q;
+                break;
+            }
+        }
+        real p0 = P(jj, nl), p1 = P(jj + 1, nl);
+        real L = p1 - p0;
+        real g = (Cc(jj + 1, nl) - Cc(jj, nl)) / L;
+        return (g >= 0 || fabs(g * L) < real(1e-10)) ? p0 + trexp_offset(uoff, g, L) : p1 - trexp_offset(uoff, -g, L);
+    }
+
+    // commit_block! / apply_step! (src/local.jl:2495, :2507)
+    __device__ void commit(real t) const {
+        eval(t);
+        int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nku = d.hdr[4], nns = d.hdr[5], nga = d.hdr[6],
+            nna = d.hdr[7], nth = d.hdr[8];
+        for (int q = 0; q < nga; ++q) M.g[ix(d.gia[q], taum)] += t * d.gaa[q];
+        for (int q = 0; q < nna; ++q) M.r[ix(d.nda[q], taum)] += S(LL.dra, q);
+        for (int q = 0; q < ng; ++q) M.g[ix(d.gi[q], tau)] += t * d.ga[q];
+        for (int q = 0; q < nku; ++q) {
+            real ak = S(LL.kua, q);
+            if (ak != 0) M.g[ix(d.ku[q], tau)] += t * real(0) + ak * S(LL.kph, d.kk[q]);
+        }
+        for (int q = 0; q < nse; ++q) M.e[ix(d.si[q], tau)] += t * d.sa[q];
+        for (int q = 0; q < nth; ++q) M.theta[ix(d.thn[q], tau)] += t * d.tha[q];
+        for (int q = 0; q < nl; ++q) M.F[ix(d.li[q], tau)] += t * d.ldf[q];
+        for (int q = 0; q < nns; ++q) M.r[ix(d.nds[q], tau)] += S(LL.drs, q);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// warp-uniform move construction
+// ---------------------------------------------------------------------------------------------
+struct Stream {  // the tile stream (TAG_LIST), every lane holds the same copy
+    uint64_t seed;
+    uint32_t tile, cls, sweep, j;
+    __device__ double next() {
+        double u0, u1;
+        uniform2(seed, ESM_TAG_LIST, j >> 1, tile, cls, sweep, &u0, &u1);
+        double u = (j & 1) ? u1 : u0;
+        ++j;
+        return u;
+    }
+    __device__ int pick(int n) {
+        int i = (int)floor(next() * n);
+        return i >= n ? n - 1 : i;
+    }
+};
+
+// the move list of a tile (local_sweep!, src/local.jl:1964-1974): atoms, then nextra family draws,
+// shuffled (Fisher-Yates). Encoding: atom a -> a, family f -> -(f + 1).
+template <class real>
+__device__ void build_list(const DevModel<real> &M, Desc<real> &d, Stream &st, int lane) {
+    int na = M.natoms, n = na + M.nextra;
+    __syncwarp();
+    for (int i = lane; i < na; i += 32) d.moves[i] = i;
+    __syncwarp();
+    // family draws: every lane draws the same numbers; lane 0 writes
+    for (int i = 0; i < M.nextra; ++i) {
+        double u = st.next();
+        int kd = ESM_NFAM - 1;
+        for (int q = 0; q < ESM_NFAM; ++q)
+            if (M.cumw[q] >= u) {
+                kd = q;
+                break;
+            }
+        if (lane == 0) d.moves[na + i] = -(kd + 1);
+    }
+    __syncwarp();
+    for (int i = n - 1; i >= 1; --i) {
+        int j = st.pick(i + 1);
+        if (lane == 0) {
+            int tmp = d.moves[i];
+            d.moves[i] = d.moves[j];
+            d.moves[j] = tmp;
+        }
+    }
+    __syncwarp();
+}
+
+template <class real>
+__device__ inline void add_node(Desc<real> &d, int side, int n, int *cnt, int *pos_out) {
+    unsigned char *mk = side == 0 ? d.nmarks : d.nmarka;
+    int *lst = side == 0 ? d.nds : d.nda;
+    int *pos = side == 0 ? d.posn_s : d.posn_a;
+    if (!mk[n]) {
+        mk[n] = 1;
+        pos[n] = *cnt;
+        lst[(*cnt)++] = n;
+    }
+    if (pos_out) *pos_out = pos[n];
+}
+
+template <class real>
+__device__ inline real kappa_d(const DevModel<real> &M, int j) {
+    return M.d_avail[j] * M.kc_d[j];
+}
+
+// Build the warp-uniform part of move `mv` (lane 0 writes shared memory). Returns the family
+// index for the statistics (ESM_NFAM for atoms) or -1 when the selection rejects the move.
+template <class real>
+__device__ int prep_move(const DevModel<real> &M, Desc<real> &d, Stream &st, int mv, int lane) {
+    int N = M.N;
+    int *h = d.hdr;
+    // every lane computes the same selection; lane 0 writes (after every lane left the last move)
+    bool w0 = lane == 0;
+    __syncwarp();
+    if (w0)
+        for (int i = 0; i < 16; ++i) h[i] = 0;
+    __syncwarp();
+    int fam = mv >= 0 ? ESM_NFAM : -mv - 1;
+    int ng = 0, nse = 0, nth = 0, nk = 0, nku = 0, nga = 0;
+    real kmin = M.kmin;
+    auto nun = [&](int n) { return M.up[n + 1] - M.up[n]; };
+    bool ok = true;
+    if (mv >= 0) {  // prep_atom! (src/local.jl:1567)
+        int f = 0;
+        while (f + 1 < M.nfields && M.fap[f + 1] <= mv) ++f;
+        int role = M.frole[f];
+        for (int q = M.ap[mv] + lane; q < M.ap[mv + 1]; q += 32) {
+            int i = q - M.ap[mv];
+            if (role == ESM_ROLE_THETA) {
+                d.thn[i] = M.ai[q];
+                d.tha[i] = M.av[q];
+            } else if (role == ESM_ROLE_GEN) {
+                d.gi[i] = M.ai[q];
+                d.ga[i] = M.av[q];
+            } else {
+                d.si[i] = M.ai[q];
+                d.sa[i] = M.av[q];
+            }
+        }
+        int cnt = M.ap[mv + 1] - M.ap[mv];
+        if (role == ESM_ROLE_THETA)
+            nth = cnt;
+        else if (role == ESM_ROLE_GEN)
+            ng = cnt;
+        else
+            nse = cnt;
+    } else {
+        switch (fam) {
+            case ESM_FAM_UNIT: {
+                int n = st.pick(N);
+                if (nun(n) == 0) {
+                    ok = false;
+                    break;
+                }
+                int j = M.ua[M.up[n] + st.pick(nun(n))];
+                if (w0) {
+                    d.gi[0] = j;
+                    d.ga[0] = 1;
+                }
+                ng = 1;
+                break;
+            }
+            case ESM_FAM_PAIR:
+            case ESM_FAM_XPAIR: {
+                int n = st.pick(N);
+                int m = fam == ESM_FAM_PAIR ? n : st.pick(N);
+                if (fam == ESM_FAM_XPAIR && (m == n || M.comp[m] != M.comp[n])) {
+                    ok = false;
+                    break;
+                }
+                if (nun(n) == 0 || nun(m) == 0) {
+                    ok = false;
+                    break;
+                }
+                int u1 = M.ua[M.up[n] + st.pick(nun(n))];
+                int u2 = M.ua[M.up[m] + st.pick(nun(m))];
+                if (u1 == u2) {
+                    ok = false;
+                    break;
+                }
+                real k1 = kappa_d(M, u1), k2 = kappa_d(M, u2);
+                if (fabs(k1) < kmin || fabs(k2) < kmin) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.gi[0] = u1;
+                    d.ga[0] = real(1) / k1;
+                    d.gi[1] = u2;
+                    d.ga[1] = real(-1) / k2;
+                }
+                ng = 2;
+                if (fam == ESM_FAM_XPAIR) {  // prep_reroute! (src/local.jl:1592)
+                    int c = 0;
+                    for (int i = 0; i < N; ++i) {
+                        if (M.comp[i] != M.comp[n]) continue;
+                        real x = M.Z[(size_t)i * N + n] - M.Z[(size_t)i * N + m];
+                        if (fabs(x) < real(1e-15)) continue;
+                        if (w0) {
+                            d.thn[c] = i;
+                            d.tha[c] = x;
+                        }
+                        ++c;
+                    }
+                    nth = c;
+                }
+                break;
+            }
+            case ESM_FAM_XLOC:
+            case ESM_FAM_XLOCC: {
+                int n = st.pick(N);
+                int np = M.xpp[n + 1] - M.xpp[n];
+                if (np == 0) {
+                    ok = false;
+                    break;
+                }
+                int pair = M.xpp[n] + st.pick(np);
+                int m = M.xp[pair];
+                if (nun(n) == 0 || nun(m) == 0) {
+                    ok = false;
+                    break;
+                }
+                int u1 = M.ua[M.up[n] + st.pick(nun(n))];
+                int u2 = M.ua[M.up[m] + st.pick(nun(m))];
+                real k1 = kappa_d(M, u1), k2 = kappa_d(M, u2);
+                if (fabs(k1) < kmin || fabs(k2) < kmin) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.gi[0] = u1;
+                    d.ga[0] = real(1) / k1;
+                    d.gi[1] = u2;
+                    d.ga[1] = real(-1) / k2;
+                }
+                ng = 2;
+                nth = M.xnp[pair + 1] - M.xnp[pair];
+                for (int q = lane; q < nth; q += 32) {
+                    d.thn[q] = M.xn[M.xnp[pair] + q];
+                    d.tha[q] = M.xv[M.xnp[pair] + q];
+                }
+                if (fam == ESM_FAM_XLOCC) {  // leak compensated pro rata (prorata!, src/local.jl:1782)
+                    for (int q = M.xlp[pair]; q < M.xlp[pair + 1]; ++q) {
+                        real gq = M.xlg[q];
+                        if (gq == 0) continue;
+                        int ln = M.xln[q];
+                        if (w0) {
+                            d.kn[nk] = ln;
+                            d.kg[nk] = gq;
+                        }
+                        for (int p = M.up[ln]; p < M.up[ln + 1]; ++p) {
+                            int j = M.ua[p];
+                            if (!(fabs(kappa_d(M, j)) >= kmin)) continue;
+                            if (w0) {
+                                d.ku[nku] = j;
+                                d.kk[nku] = nk;
+                            }
+                            ++nku;
+                        }
+                        ++nk;
+                    }
+                }
+                break;
+            }
+            case ESM_FAM_POTENTIAL: {
+                int n = st.pick(N);
+                if (M.theta_nnz[n] == 0) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.thn[0] = n;
+                    d.tha[0] = 1;
+                }
+                nth = 1;
+                break;
+            }
+            case ESM_FAM_CELLPAIR:
+            case ESM_FAM_CELL: {
+                double u = st.next();
+                int q = M.nlev - 1;
+                for (int l = 0; l < M.nlev; ++l)
+                    if (M.qcum[l] >= u) {
+                        q = l;
+                        break;
+                    }
+                int ncell = M.clp[q + 1] - M.clp[q];
+                int cidx = M.clp[q] + st.pick(ncell);
+                // distinct injecting groups of the cell, ascending
+                int fl[8], nfl = 0;
+                for (int p = M.cp[cidx]; p < M.cp[cidx + 1]; ++p) {
+                    int gg = M.d_group[M.cu[p]];
+                    bool seen = false;
+                    for (int i = 0; i < nfl; ++i) seen |= fl[i] == gg;
+                    if (!seen && nfl < 8) fl[nfl++] = gg;
+                }
+                for (int i = 1; i < nfl; ++i)
+                    for (int j = i; j > 0 && fl[j] < fl[j - 1]; --j) {
+                        int tmp = fl[j];
+                        fl[j] = fl[j - 1];
+                        fl[j - 1] = tmp;
+                    }
+                if (nfl == 0) {
+                    ok = false;
+                    break;
+                }
+                if (fam == ESM_FAM_CELL) {
+                    int f = fl[st.pick(nfl)];
+                    int c = 0;
+                    for (int p = M.cp[cidx]; p < M.cp[cidx + 1]; ++p)
+                        if (M.d_group[M.cu[p]] == f) {
+                            if (w0) {
+                                d.gi[c] = M.cu[p];
+                                d.ga[c] = 1;
+                            }
+                            ++c;
+                        }
+                    ng = c;
+                    break;
+                }
+                if (nfl < 2) {
+                    ok = false;
+                    break;
+                }
+                int f1 = fl[st.pick(nfl)], f2 = fl[st.pick(nfl)];
+                if (f1 == f2) {
+                    ok = false;
+                    break;
+                }
+                real K1 = 0, K2 = 0;
+                for (int p = M.cp[cidx]; p < M.cp[cidx + 1]; ++p) {
+                    int j = M.cu[p];
+                    if (M.d_group[j] == f1) K1 += kappa_d(M, j);
+                    if (M.d_group[j] == f2) K2 += kappa_d(M, j);
+                }
+                if (fabs(K1) < kmin || fabs(K2) < kmin) {
+                    ok = false;
+                    break;
+                }
+                int c = 0;
+                for (int p = M.cp[cidx]; p < M.cp[cidx + 1]; ++p)
+                    if (M.d_group[M.cu[p]] == f1) {
+                        if (w0) {
+                            d.gi[c] = M.cu[p];
+                            d.ga[c] = real(1) / K1;
+                        }
+                        ++c;
+                    }
+                for (int p = M.cp[cidx]; p < M.cp[cidx + 1]; ++p)
+                    if (M.d_group[M.cu[p]] == f2) {
+                        if (w0) {
+                            d.gi[c] = M.cu[p];
+                            d.ga[c] = real(-1) / K2;
+                        }
+                        ++c;
+                    }
+                ng = c;
+                break;
+            }
+            case ESM_FAM_SPAIR: {
+                int n = st.pick(N);
+                int ns = M.sp[n + 1] - M.sp[n];
+                if (ns == 0 || nun(n) == 0) {
+                    ok = false;
+                    break;
+                }
+                int sj = M.sa[M.sp[n] + st.pick(ns)];
+                real ks = M.kc_s[sj] * M.s_hours[sj] / M.dt;
+                if (ks < kmin) {
+                    ok = false;
+                    break;
+                }
+                int u1 = M.ua[M.up[n] + st.pick(nun(n))];
+                int u2 = M.ua[M.up[n] + st.pick(nun(n))];
+                real k1 = kappa_d(M, u1), k2 = kappa_d(M, u2);
+                if (fabs(k1) < kmin || fabs(k2) < kmin) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.gia[0] = u1;
+                    d.gaa[0] = ks / k1;
+                    d.si[0] = sj;
+                    d.sa[0] = 1;
+                    d.gi[0] = u2;
+                    d.ga[0] = -ks / k2;
+                }
+                nga = 1;
+                nse = 1;
+                ng = 1;
+                break;
+            }
+        }
+    }
+    __syncwarp();
+    if (!ok) return -1;
+    // ---- finalize! (src/local.jl:656): zero tiny coefficients, lines, touched nodes
+    if (w0) {
+        int c = 0;
+        for (int q = 0; q < ng; ++q)
+            if (!(fabs(d.ga[q]) < real(1e-14))) {
+                d.gi[c] = d.gi[q];
+                d.ga[c] = d.ga[q];
+                ++c;
+            }
+        ng = c;
+        c = 0;
+        for (int q = 0; q < nse; ++q)
+            if (!(fabs(d.sa[q]) < real(1e-14))) {
+                d.si[c] = d.si[q];
+                d.sa[c] = d.sa[q];
+                ++c;
+            }
+        nse = c;
+        c = 0;
+        for (int q = 0; q < nth; ++q)
+            if (!(fabs(d.tha[q]) < real(1e-14))) {
+                d.thn[c] = d.thn[q];
+                d.tha[c] = d.tha[q];
+                ++c;
+            }
+        nth = c;
+        // node lists: ws entries (gens, storage, kinked units), then line ends; wa entries, linked storage
+        int nns = 0, nna = 0;
+        for (int q = 0; q < ng; ++q) add_node(d, 0, M.d_bus[d.gi[q]], &nns, &d.gpos[q]);
+        for (int q = 0; q < nse; ++q) add_node(d, 0, M.s_bus[d.si[q]], &nns, &d.spos[q]);
+        for (int q = 0; q < nku; ++q) add_node(d, 0, M.d_bus[d.ku[q]], &nns, &d.kupos[q]);
+        int nl = 0;
+        for (int q = 0; q < nth; ++q) d.dth[d.thn[q]] = d.tha[q];
+        for (int q = 0; q < nth; ++q) {
+            int n = d.thn[q];
+            for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) {
+                int e = M.nl[p];
+                if (d.lmark[e]) continue;
+                d.lmark[e] = 1;
+                real df = M.lb[e] * (d.dth[M.bus0[e]] - d.dth[M.bus1[e]]);
+                if (fabs(df) <= real(1e-14)) continue;
+                d.li[nl] = e;
+                d.ldf[nl] = df;
+                ++nl;
+            }
+        }
+        for (int q = 0; q < nl; ++q) {
+            add_node(d, 0, M.bus0[d.li[q]], &nns, &d.lpa[q]);
+            add_node(d, 0, M.bus1[d.li[q]], &nns, &d.lpb[q]);
+        }
+        for (int q = 0; q < nth; ++q) {  // reset the dense marks
+            int n = d.thn[q];
+            d.dth[n] = 0;
+            for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) d.lmark[M.nl[p]] = 0;
+        }
+        for (int q = 0; q < nga; ++q) add_node(d, 1, M.d_bus[d.gia[q]], &nna, &d.gposa[q]);
+        for (int q = 0; q < nse; ++q) add_node(d, 1, M.s_bus[d.si[q]], &nna, &d.sposa[q]);
+        for (int q = 0; q < nns; ++q) d.nmarks[d.nds[q]] = 0;
+        for (int q = 0; q < nna; ++q) d.nmarka[d.nda[q]] = 0;
+        h[0] = ng;
+        h[1] = nse;
+        h[2] = nl;
+        h[3] = nk;
+        h[4] = nku;
+        h[5] = nns;
+        h[6] = nga;
+        h[7] = nna;
+        h[8] = nth;
+        h[9] = (ng + nse + nth + nku) > 0;
+        h[10] = fam;
+    }
+    __syncwarp();
+    if (!d.hdr[9]) return -1;
+    return fam;
+}
+
+// per-lane part of the kinks (prorata!, src/local.jl:1782): Q, e, P per leak node and the
+// kinked coefficients sigma/kappa; a lane without dispatch at a node has no kink there
+template <class real>
+__device__ void lane_kinks(const Lane<real> &Ln) {
+    const DevModel<real> &M = Ln.M;
+    const Desc<real> &d = Ln.d;
+    int nk = d.hdr[3], nku = d.hdr[4];
+    for (int q = 0; q < nk; ++q) {
+        int m = d.kn[q];
+        real Pm = 0, Qs = 0;
+        int nu = 0;
+        for (int p = M.up[m]; p < M.up[m + 1]; ++p) {
+            int j = M.ua[p];
+            real kap = kappa_d(M, j);
+            if (!(fabs(kap) >= M.kmin)) continue;
+            real om = M.g[Ln.ix(j, Ln.tau)];
+            Pm += kap * om;
+            Qs += kap * clampr<real>(om, 0, 1);
+            nu += 1;
+        }
+        bool valid = nu > 0 && !(fabs(Pm) < real(1e-6));
+        real Q = M.r[Ln.ix(m, Ln.tau)] + Qs + real(0);
+        Ln.S(Ln.LL.kq, q) = valid ? Q : real(0);
+        Ln.S(Ln.LL.kp, q) = valid ? Pm : real(1);
+        Ln.S(Ln.LL.ke, q) = valid ? Pm - fmax(Q, real(0)) : real(0);
+        Ln.S(Ln.LL.knm, q) = valid ? real(nu - 1) : real(0);
+        Ln.S(Ln.LL.kv, q) = valid ? real(1) : real(0);
+        Ln.S(Ln.LL.kph, q) = 0;
+    }
+    for (int q = 0; q < nku; ++q) {
+        int kq = d.kk[q];
+        real ak = 0;
+        if (Ln.S(Ln.LL.kv, kq) != 0) {
+            int j = d.ku[q];
+            real kap = kappa_d(M, j);
+            real sigma = kap * M.g[Ln.ix(j, Ln.tau)] / Ln.S(Ln.LL.kp, kq);
+            if (sigma != 0) ak = sigma / kap;
+        }
+        Ln.S(Ln.LL.kua, q) = ak;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// the kernel: one colour class of one sweep
+// ---------------------------------------------------------------------------------------------
+template <class real>
+__global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int *steps, int nsteps, int ntile,
+                                                   int wpt, uint32_t sweep, int cls, real *scratch,
+                                                   unsigned long long *stats, size_t smem_per_warp) {
+    extern __shared__ __align__(16) char smem[];
+    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int nmoves = M.natoms + M.nextra;
+    Desc<real> d = carve_desc<real>(smem + wib * smem_per_warp, M, nmoves);
+    LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+    int nw = gridDim.x * (blockDim.x >> 5);
+    real *slab = scratch + (size_t)gw * LL.total * 32;
+    // zero the dense marks once
+    for (int i = lane; i < M.N; i += 32) {
+        d.dth[i] = 0;
+        d.nmarks[i] = 0;
+        d.nmarka[i] = 0;
+    }
+    for (int i = lane; i < M.L; i += 32) d.lmark[i] = 0;
+    __syncwarp();
+    unsigned long long loc_tried[ESM_NFAM + 1], loc_moved[ESM_NFAM + 1], loc_guard = 0;
+    for (int i = 0; i <= ESM_NFAM; ++i) loc_tried[i] = loc_moved[i] = 0;
+    Lane<real> Ln(M, d, slab, lane, LL);
+    for (int item = gw; item < ntile * wpt; item += nw) {
+        int tile = item / wpt, grp = item % wpt;
+        int task = grp * 32 + lane;
+        int sit = task / M.R;
+        Ln.rep = task % M.R;
+        int q = tile * M.span + sit;
+        Ln.active = sit < M.span && q < nsteps;
+        int T = M.T;
+        Ln.tau = Ln.active ? steps[q] : 0;
+        Ln.taum = (Ln.tau - 1 + T) % T;
+        Ln.tau1 = (Ln.tau + 1) % T;
+        Stream st{M.seed, (uint32_t)tile, (uint32_t)cls, sweep, 0u};
+        build_list(M, d, st, lane);
+        for (int mi = 0; mi < nmoves; ++mi) {
+            int fi = prep_move(M, d, st, d.moves[mi], lane);
+            if (fi < 0) continue;
+            if (!Ln.active) continue;
+            lane_kinks(Ln);
+            double uc, uo, uj, un;
+            uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
+            bool guard;
+            real t = Ln.sample_line((real)uc, (real)uo, &guard);
+            if (guard) ++loc_guard;
+            if (fi == ESM_FAM_XLOCC && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
+                int nk = d.hdr[3];
+                bool any = false;
+                real lj = 0;
+                for (int k = 0; k < nk; ++k) {
+                    if (Ln.S(LL.kv, k) == 0) continue;
+                    any = true;
+                    real Q = Ln.S(LL.kq, k);
+                    lj += Ln.S(LL.knm, k) *
+                          log(fabs((fmax(Q + d.kg[k] * t, real(0)) + Ln.S(LL.ke, k)) / Ln.S(LL.kp, k)));
+                }
+                if (any) {
+                    uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep,
+                             &uj, &un);
+                    if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+                }
+            }
+            if (t != 0) Ln.commit(t);
+            loc_tried[fi] += 1;
+            loc_moved[fi] += t != 0;
+        }
+        __syncwarp();
+    }
+    for (int i = 0; i <= ESM_NFAM; ++i) {
+        if (loc_tried[i]) atomicAdd(&stats[2 * i], loc_tried[i]);
+        if (loc_moved[i]) atomicAdd(&stats[2 * i + 1], loc_moved[i]);
+    }
+    if (loc_guard) atomicAdd(&stats[2 * (ESM_NFAM + 1)], loc_guard);
+}
+
+// ---------------------------------------------------------------------------------------------
+// host launcher
+// ---------------------------------------------------------------------------------------------
+template <class real>
+size_t linemove_scratch_reals(const DevModel<real> &M) {
+    LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    return (size_t)LL.total * 32;
+}
+
+template <class real>
+size_t linemove_smem_per_warp(const DevModel<real> &M) {
+    return (desc_bytes(M, M.natoms + M.nextra) + 15) & ~(size_t)15;
+}
+
+template <class real>
+cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
+                              real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s) {
+    int ntile = (nsteps + M.span - 1) / M.span;
+    int wpt = (M.span * M.R + 31) / 32;
+    int items = ntile * wpt;
+    int nwarps = items < max_warps ? items : max_warps;
+    int wpb = 4;
+    int blocks = (nwarps + wpb - 1) / wpb;
+    size_t spw = linemove_smem_per_warp(M);
+    size_t smem = spw * wpb;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_class_pass<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_class_pass<real><<<blocks, wpb * 32, smem, s>>>(M, steps, nsteps, ntile, wpt, sweep, cls, scratch, stats, spw);
+    return cudaGetLastError();
+}
+
+}  // namespace esm

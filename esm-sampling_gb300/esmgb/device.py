@@ -1,0 +1,166 @@
+"""ctypes binding of libesmcuda.so (the C ABI of ``include/esmcuda.h``) and the replica-chain object
+that drives it. This is the product path: there is no CPU fallback -- if the library cannot be
+loaded, or no GPU is present, the calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .cabi import EsmOpts, ModelBuffers, make_opts
+from .model import SynthModel
+
+P_f64 = C.POINTER(C.c_double)
+P_i32 = C.POINTER(C.c_int32)
+P_i64 = C.POINTER(C.c_int64)
+NSTAT = 2 * (9 + 1) + 1
+
+# the symbols declared in include/esmcuda.h
+EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
+           "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
+           "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count")
+
+_lib = None
+
+
+class EsmError(RuntimeError):
+    pass
+
+
+def lib_path():
+    from .build import LIB
+    return LIB
+
+
+def load(build_if_missing=True):
+    """Load libesmcuda.so (building it in-tree if it is missing); raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise EsmError(f"{path} is missing: run esmgb.build.build()")
+        from .build import build
+        build()
+    L = C.CDLL(path)
+    L.esm_create.restype = C.c_int
+    L.esm_create.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
+    L.esm_destroy.argtypes = [C.c_void_p]
+    L.esm_last_error.restype = C.c_char_p
+    L.esm_last_error.argtypes = [C.c_void_p]
+    L.esm_upload_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
+    L.esm_download_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
+    L.esm_rebuild_caches.argtypes = [C.c_void_p]
+    L.esm_download_caches.argtypes = [C.c_void_p, P_f64, P_f64]
+    L.esm_operation_sweeps.argtypes = [C.c_void_p, C.c_int32, C.c_int64, P_i64]
+    L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, P_i64]
+    L.esm_capacity_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
+    L.esm_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int32, P_f64,
+                                    C.c_int64, P_f64, P_i32]
+    L.esm_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64]
+    L.esm_sync.argtypes = [C.c_void_p, C.c_double]
+    L.esm_launch_count.restype = C.c_int64
+    L.esm_launch_count.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _p(a, t=P_f64):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class DeviceChain:
+    """One chain of R replicas on the GPU (an ``esm_ctx``)."""
+
+    def __init__(self, model: SynthModel, R: int, precision: int = 32, seed: int = 1, extra: float = 4.0,
+                 maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 192, span: int = 0):
+        self.L = load()
+        self.m = model
+        self.R = R
+        self.buf = ModelBuffers(model)
+        self.opts: EsmOpts = make_opts(R, precision, seed, extra, maxnats, kappa_min, max_points, span)
+        h = C.c_void_p()
+        rc = self.L.esm_create(C.byref(self.buf.struct), C.byref(self.opts), C.byref(h))
+        self.h = h
+        self._check(rc, "esm_create")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.L.esm_last_error(self.h).decode() if self.h else ""
+            raise EsmError(f"{what}: status {rc}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.esm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shapes(self):
+        m, R = self.m, self.R
+        return {"theta": (m.N, m.T, R), "g": (m.D, m.T, R), "e": (m.S, m.T, R), "z": (m.n0, m.T, R),
+                "reg": (m.T, R), "k": (m.Kunits,)}
+
+    def upload(self, st):
+        arr = {k: np.ascontiguousarray(getattr(st, k) if not isinstance(st, dict) else st[k],
+                                       dtype=np.int32 if k == "reg" else np.float64)
+               for k in ("theta", "g", "e", "z", "reg", "k")}
+        self._check(self.L.esm_upload_state(self.h, _p(arr["theta"]), _p(arr["g"]), _p(arr["e"]), _p(arr["z"]),
+                                            _p(arr["reg"], P_i32), _p(arr["k"])), "esm_upload_state")
+
+    def download(self):
+        out = {k: np.zeros(s, dtype=np.int32 if k == "reg" else np.float64) for k, s in self.shapes().items()}
+        self._check(self.L.esm_download_state(self.h, _p(out["theta"]), _p(out["g"]), _p(out["e"]), _p(out["z"]),
+                                              _p(out["reg"], P_i32), _p(out["k"])), "esm_download_state")
+        return out
+
+    def rebuild(self):
+        self._check(self.L.esm_rebuild_caches(self.h), "esm_rebuild_caches")
+
+    def caches(self):
+        m, R = self.m, self.R
+        r = np.zeros((m.N, m.T, R))
+        F = np.zeros((m.L, m.T, R))
+        self._check(self.L.esm_download_caches(self.h, _p(r), _p(F)), "esm_download_caches")
+        return r, F
+
+    def class_pass(self, sweep, cls):
+        st = np.zeros(NSTAT, np.int64)
+        self._check(self.L.esm_class_pass(self.h, sweep, cls, _p(st, P_i64)), "esm_class_pass")
+        return st
+
+    def sweeps(self, n, sweep0=0, stats=True):
+        st = np.zeros(NSTAT, np.int64)
+        self._check(self.L.esm_operation_sweeps(self.h, n, sweep0, _p(st, P_i64) if stats else None),
+                    "esm_operation_sweeps")
+        return st
+
+    def scores(self):
+        m, R = self.m, self.R
+        sk = np.zeros((R, m.Kunits))
+        fk = np.zeros(m.Kunits)
+        parts = np.zeros((R, 8))
+        self._check(self.L.esm_capacity_scores(self.h, _p(sk), _p(fk), _p(parts)), "esm_capacity_scores")
+        return sk, fk, parts
+
+    def langevin_step(self, w, eta, kappa_s, kmin=1.0, clip=0.02, box=True, xi=None, it=0):
+        w, eta, kappa_s = (np.ascontiguousarray(x, dtype=np.float64) for x in (w, eta, kappa_s))
+        xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+        knew = np.zeros(self.m.Kunits)
+        nclip = np.zeros(1, np.int32)
+        self._check(self.L.esm_langevin_step(self.h, _p(w), _p(eta), _p(kappa_s), kmin, clip, int(box), _p(xi), it,
+                                             _p(knew), _p(nclip, P_i32)), "esm_langevin_step")
+        return knew, int(nclip[0])
+
+    def sync(self, timeout_s=60.0):
+        self._check(self.L.esm_sync(self.h, timeout_s), "esm_sync")
+
+    def launch_count(self):
+        return int(self.L.esm_launch_count(self.h))

@@ -1,0 +1,192 @@
+"""Host side of the replica sampler: controls, weather schedule, gate, drift weights and the step
+adaptation (src/replicas.jl sections 4-5), mirroring the reference's names and semantics.
+
+These are the pieces the reference keeps on the host in its GPU port as well
+(device/src/replica_run.jl:309): scalar bookkeeping per replica and step. The hot path (sweeps,
+scores, Langevin step with dispatch following, weather draws) runs in libesmcuda.so through
+:mod:`esmgb.device`.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class ReplicaCtl:
+    """Settings of the replica sampler (``src/replicas.jl:484`` ReplicaCtl, defaults as there)."""
+    M: int = 8
+    inner: int = 1
+    theta: float = 0.0
+    burst_every: int = 40
+    phi: float = 0.3
+    window: int = 60
+    window_prob: float = 0.5
+    ffbs: bool = False
+    comp: bool = True
+    gate_min: int = 10
+    gate_max: int = 30
+    gate_min_window: int = 20
+    gate_max_window: int = 60
+    gate_win: int = 8
+    gate_tol: float = 0.3
+    eta_w: list = field(default_factory=list)
+    kappa_s: list = field(default_factory=list)
+    kappa_min: float = 1.0
+    clip: float = 0.02
+    box: bool = True
+    probe_every: int = 20
+    probe_len: int = 30
+    probe_tail: int = 15
+    probe_win: int = 10
+    probe_avg: int = 3
+    adapt: bool = True
+    gap_hi: float = 0.10
+    gap_lo: float = 0.05
+    eta_min: float = 2e-5
+    eta_max: float = 2e-3
+    shrink: float = 0.7
+    grow: float = 1.2
+    lam: float = 0.0
+    Phi: object = None
+
+
+def weather_schedule(ctl: ReplicaCtl, it: int, j: int):
+    """(angle, burst) of replica j (1-based) at step ``it`` (``src/replicas.jl:571``)."""
+    nb = ctl.burst_every
+    burst = nb > 0 and (it + (j - 1) * (nb // ctl.M)) % nb == 0
+    if burst:
+        th = math.acos(max(-1.0, min(1.0, math.cos(ctl.theta) * math.cos(ctl.phi)))) if ctl.theta > 0 else ctl.phi
+    else:
+        th = ctl.theta
+    return th, burst
+
+
+def categorical(p, u):
+    """First index k (1-based) with u sum(p) <= sum_{i<=k} p_i (``src/replicas.jl:115``)."""
+    t = u * sum(p)
+    c = 0.0
+    for k, pk in enumerate(p):
+        c += pk
+        if t <= c:
+            return k + 1
+    return len(p)
+
+
+def window_bounds(T0: int, B: int, u: float):
+    """Window [a, b] (1-based) of length B with a uniform start (``src/replicas.jl:167``)."""
+    a = min(T0, 1 + math.floor(u * T0))
+    return a, min(T0, a + B - 1)
+
+
+def relaxation_indicator(gbuf, win: int):
+    """``src/replicas.jl:634``: largest difference of the halves' mean normalised scores."""
+    h = win // 2
+    if not (len(gbuf) >= 2 * h and h >= 1):
+        return math.inf
+    n = len(gbuf)
+    a = np.mean(np.asarray(gbuf[n - 2 * h:n - h], float), axis=0)
+    b = np.mean(np.asarray(gbuf[n - h:n], float), axis=0)
+    d = [abs(x - y) for x, y in zip(a, b) if math.isfinite(x) and math.isfinite(y)]
+    return 0.0 if not d else max(d)
+
+
+@dataclass
+class ReplicaSet:
+    """Per-chain replica bookkeeping (``src/replicas.jl:549``); the states live on the device."""
+    M: int
+    eta_w: list
+    since: list = None
+    window: list = None
+    active: list = None
+    gbuf: list = None
+    hist: list = None
+    gaps: list = None
+
+    def __post_init__(self):
+        self.since = [10 ** 9] * self.M if self.since is None else self.since
+        self.window = [False] * self.M if self.window is None else self.window
+        self.active = [True] * self.M if self.active is None else self.active
+        self.gbuf = [[] for _ in range(self.M)] if self.gbuf is None else self.gbuf
+        self.hist = [[] for _ in range(self.M)] if self.hist is None else self.hist
+        self.gaps = [] if self.gaps is None else self.gaps
+        self.eta_w = list(self.eta_w)
+
+
+def update_gate(R: ReplicaSet, j: int, g, ctl: ReplicaCtl) -> bool:
+    """``src/replicas.jl:651`` update_gate! (j 0-based)."""
+    if ctl.burst_every == 0:
+        R.active[j] = True
+        return True
+    if R.active[j]:
+        return True
+    R.gbuf[j].append(list(g))
+    if len(R.gbuf[j]) > ctl.gate_win:
+        R.gbuf[j].pop(0)
+    gmin, gmax = (ctl.gate_min_window, ctl.gate_max_window) if R.window[j] else (ctl.gate_min, ctl.gate_max)
+    if not R.since[j] >= gmin:
+        return False
+    R.active[j] = R.since[j] >= gmax or relaxation_indicator(R.gbuf[j], ctl.gate_win) < ctl.gate_tol
+    if R.active[j]:
+        R.gbuf[j].clear()
+    return R.active[j]
+
+
+def tilt_weights(lam: float, Phis, active):
+    """``src/replicas.jl:303``: exp(lam Phi_j) over the active replicas, normalised."""
+    active = list(active)
+    if not any(active):
+        active = [True] * len(active)
+    a = np.array([lam * P if act else -math.inf for act, P in zip(active, Phis)])
+    w = np.exp(a - a.max())
+    return w / w.sum()
+
+
+def uniform_weights(active):
+    """``src/replicas.jl:310``: 1/M_active over the active replicas (all if none)."""
+    active = list(active)
+    if not any(active):
+        active = [True] * len(active)
+    w = np.array([1.0 if a else 0.0 for a in active])
+    return w / w.sum()
+
+
+def drift_weights(ctl: ReplicaCtl, Phis, active):
+    """``src/replicas.jl:664``."""
+    return uniform_weights(active) if ctl.Phi is None else tilt_weights(ctl.lam, Phis, active)
+
+
+def adapt_step(R: ReplicaSet, gap, ctl: ReplicaCtl) -> bool:
+    """``src/replicas.jl:758`` adapt_step!: shrink/grow eta_w per k field from probe_avg probes."""
+    R.gaps.append(list(gap))
+    if len(R.gaps) < ctl.probe_avg:
+        return False
+    for f in range(len(R.eta_w)):
+        v = [g[f] for g in R.gaps if math.isfinite(g[f])]
+        if not v:
+            continue
+        gbar = sum(v) / len(v)
+        if abs(gbar) > ctl.gap_hi:
+            R.eta_w[f] = max(ctl.eta_min, R.eta_w[f] * ctl.shrink)
+        elif abs(gbar) < ctl.gap_lo:
+            R.eta_w[f] = min(ctl.eta_max, R.eta_w[f] * ctl.grow)
+    R.gaps.clear()
+    return True
+
+
+def langevin_drift_w(k, g, eta, kappa_s):
+    """``src/replicas.jl:357``: eta ((k + kappa_s) g + 1)."""
+    return eta * ((np.asarray(k) + kappa_s) * np.asarray(g) + 1)
+
+
+def interior_nodes(k, hi, lo=50.0):
+    """``src/replicas.jl:475``: capacity above ``lo`` MW and below the box."""
+    k = np.asarray(k)
+    return (k > lo) & (k < np.asarray(hi) - 1)
+
+
+def masked_mean(v, mask):
+    v = np.asarray(v)
+    return float(v[mask].mean()) if mask.any() else math.nan

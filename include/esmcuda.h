@@ -1,0 +1,190 @@
+/*
+ * esmcuda.h -- C ABI of libesmcuda.so, the GB300 (sm_103a) replica-sampler hot path.
+ *
+ * The reference (a Julia package) has no FFI on this path; the seam this library replaces is
+ * the body of the replica step `replica_step!` (src/replicas.jl:676-707) and `init_replicas`
+ * (src/replicas.jl:785), i.e. the per-replica operation sweeps, the capacity scores, the
+ * replica-averaged Langevin capacity step with dispatch following, and the weather process.
+ * The host keeps the run loop, the gate, the weights and the probe bookkeeping
+ * (src/replicas.jl:841-1000 run_replicas), as the reference's GPU port does
+ * (device/src/replica_run.jl:309 replica_device_step!).
+ *
+ * Conventions
+ *  - Every entry point returns an int status: ESM_OK (0) or a negative ESM_E* code; the
+ *    message of the last failure of a context is `esm_last_error(ctx)`. Nothing aborts or traps.
+ *  - Host arrays are caller-owned and copied at call time. Device buffers are owned by the
+ *    context and freed by esm_destroy.
+ *  - State arrays are (X, T, R) with the replica index fastest: element (x, t, r) at
+ *    (x*T + t)*R + r. X is N (angles), D (dispatchable units), S (storage units) or n0 (weather
+ *    series). This is the layout of the reference port's DeviceState (device/src/core.jl).
+ *  - One context per host thread; one CUDA stream per context.
+ *  - Random numbers: counter-based Philox4x32-10 streams keyed by the context seed; the exact
+ *    stream layout is part of the contract so that the CPU oracle can replay it.
+ */
+#ifndef ESMCUDA_H
+#define ESMCUDA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ESM_OK = 0,
+    ESM_EINVAL = -1,      /* bad argument or model */
+    ESM_ECUDA = -2,       /* CUDA runtime error */
+    ESM_ENOMEM = -3,      /* device allocation failed */
+    ESM_ETIMEOUT = -4,    /* a bounded device wait ran out */
+    ESM_ESTATE = -5       /* call out of order (e.g. no state uploaded) */
+};
+
+/* unit kinds of the flat capacity vector */
+enum { ESM_UNIT_REN = 0, ESM_UNIT_DISP = 1, ESM_UNIT_STOR = 2 };
+/* v-field roles (src/local.jl:36) */
+enum { ESM_ROLE_THETA = 1, ESM_ROLE_GEN = 3, ESM_ROLE_SE = 6 };
+/* the plain local families (src/local.jl:1912 plain_families), in this order */
+enum { ESM_FAM_UNIT = 0, ESM_FAM_PAIR, ESM_FAM_XPAIR, ESM_FAM_XLOCC, ESM_FAM_XLOC, ESM_FAM_POTENTIAL,
+       ESM_FAM_CELLPAIR, ESM_FAM_CELL, ESM_FAM_SPAIR, ESM_NFAM };
+
+/*
+ * Static model: network, units, prices, weather prior and the move tables.
+ * Reference: EnergyModel (src/energy.jl:219), LocalModel (src/local.jl:193), WeatherModel
+ * (src/weather.jl:22). Index arrays are 0-based.
+ */
+typedef struct esm_model {
+    int32_t N, L, T;            /* nodes, lines, steps of the year */
+    double dt;                  /* step length (h) */
+    /* lines: flow b (theta_a - theta_b), hard limit s (src/energy.jl:590) */
+    const int32_t *bus0, *bus1;
+    const double *line_b, *line_s;
+    /* capacity units, flat; kind ESM_UNIT_* */
+    int32_t K;
+    const int32_t *unit_kind, *unit_group, *unit_bus, *unit_series;
+    const double *unit_mc, *unit_capex, *unit_lo, *unit_hi, *unit_avail;
+    const double *unit_hours, *unit_eta_in, *unit_eta_out, *unit_qt;
+    int32_t D, S;               /* dispatchable and storage units */
+    const int32_t *disp, *stor; /* their flat capacity indices */
+    /* weather: n0 series (load per node, then availability series), single-level
+       regime-switching VAR(1) with diagonal coefficients (src/weather.jl:22) */
+    int32_t n0, nreg;
+    const int32_t *series_field; /* 0 = load, > 0 availability */
+    const int32_t *series_node;
+    const double *xbar;          /* [n0*T] climatology */
+    const double *wscale;        /* [n0] */
+    const double *Ptr, *pi0;     /* [nreg*nreg], [nreg] */
+    const double *phi;           /* [nreg*n0] diagonal AR coefficient */
+    const double *mu;            /* [nreg*n0*3] harmonic regime mean (1, cos, sin) */
+    const double *sig;           /* [nreg*n0] innovation sd */
+    const double *sig0;          /* [n0] sd of the first step */
+    /* prices and temperatures (src/run.jl:14-16,54-55; src/energy.jl:279) */
+    double c_shed, c_dump, c_viol, gamma_k, kappa0, beta_v, beta_k;
+    int32_t physical;            /* reference measure "physical" (src/energy.jl:811) */
+    /* v fields: theta, g per dispatchable carrier, se per storage carrier; atoms are the
+       node-space columns of their graph-Haar bases (src/spatial.jl:112) */
+    int32_t nfields;
+    const int32_t *field_role;   /* [nfields] ESM_ROLE_* */
+    const int32_t *field_atom_ptr; /* [nfields+1] -> atoms */
+    const int32_t *atom_ptr;     /* [natoms+1] -> entries */
+    const int32_t *atom_idx;     /* node (theta) or index into disp/stor */
+    const double *atom_val;
+    /* incidence and unit lists (src/local.jl:248-285) */
+    const int32_t *nodelines_ptr, *nodelines;
+    const int32_t *units_ptr, *units_at;   /* dispatchable units per node (index into disp) */
+    const int32_t *stor_ptr, *stor_at;     /* storage units per node (index into stor) */
+    /* cell moves (src/local.jl:265-283) */
+    int32_t nlev;
+    const double *qcum;                    /* [nlev] cumulative level probabilities */
+    const int32_t *cell_level_ptr;         /* [nlev+1] -> cells */
+    const int32_t *cell_ptr, *cell_units;  /* cells -> dispatchable units */
+    /* xloc templates (src/local.jl:122 xloc_directions), per node and partner */
+    const int32_t *xpart_ptr, *xpart;
+    const int32_t *xnod_ptr, *xnod;        /* per pair: re-routing angle changes */
+    const double *xval;
+    const int32_t *xlk_ptr, *xlkn;         /* per pair: leak nodes and requirement change */
+    const double *xlkg;
+    /* global re-routing (src/local.jl:44 GridSolver): column n of the grounded inverse */
+    const double *reroute;                 /* [N*N], element (i, n) at i*N + n */
+    const int32_t *comp;                   /* AC component per node */
+} esm_model;
+
+/* Sampler options (src/run.jl:20 local_extra; src/local.jl:1294 maxnats; ReplicaCtl defaults
+   src/replicas.jl:484-519). */
+typedef struct esm_opts {
+    int32_t R;                 /* replicas per chain */
+    int32_t precision;         /* 32: FP32 evaluations (production), 64: FP64 (parity) */
+    uint64_t seed;
+    double extra;              /* random moves per node, step and sweep (4.0) */
+    double maxnats;            /* walk stop (40.0) */
+    double kappa_min;          /* move validity and reflection floor (1.0) */
+    int32_t max_points;        /* walk points per direction; beyond: t = 0, counted (guard) */
+    int32_t span;              /* class steps sharing one move list (0: max(1, 32/R)) */
+    double family_rates[ESM_NFAM];
+} esm_opts;
+
+typedef struct esm_ctx esm_ctx;
+
+/* Create a context: uploads the model, allocates the state for R replicas. */
+int esm_create(const esm_model *model, const esm_opts *opts, esm_ctx **out);
+int esm_destroy(esm_ctx *ctx);
+const char *esm_last_error(const esm_ctx *ctx);
+
+/* Upload / download the state (host arrays in double, layouts as above):
+   theta [N*T*R], g [D*T*R], e [S*T*R], z [n0*T*R] (weather anomaly), reg [T*R], k [K]
+   (capacities shared by the replicas; State in src/hierarchy.jl:28). Any pointer may be NULL
+   to skip that array on download. */
+int esm_upload_state(esm_ctx *ctx, const double *theta, const double *g, const double *e,
+                     const double *z, const int32_t *reg, const double *k);
+int esm_download_state(esm_ctx *ctx, double *theta, double *g, double *e, double *z,
+                       int32_t *reg, double *k);
+
+/* Caches (residual r [N*T*R], flows F [L*T*R]) rebuilt from the state; as LocalCost
+   (src/local.jl:313, rebuild_step! :332). */
+int esm_rebuild_caches(esm_ctx *ctx);
+int esm_download_caches(esm_ctx *ctx, double *r, double *F);
+
+/* `n` operation sweeps of every replica: local_sweep! (src/local.jl:1927) with the plain
+   families; sweep counters start at `sweep0` (the Philox counter of the sweep). stats (may be
+   NULL): [ESM_NFAM+1][2] moves tried / moved per family (last row: atoms) and, at index
+   2*(ESM_NFAM+1), the number of guard events (walk beyond max_points). */
+int esm_operation_sweeps(esm_ctx *ctx, int32_t n, int64_t sweep0, int64_t *stats);
+
+/* One colour class of one sweep (parity tests): class index in the sweep's class order. */
+int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int64_t *stats);
+
+/* Capacity scores per replica: sk [R*K] (s_k = -beta_v dC/dk + dlogJ/dk, node space) and the
+   capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with
+   grad (src/energy.jl:551) and log_measure_grad (:811). parts (may be NULL): [R*8] cost parts
+   per replica: capex, op, gen, storage, shed, dump, penalty, 0 (CostParts, src/energy.jl:531). */
+int esm_capacity_scores(esm_ctx *ctx, double *sk, double *fk, double *parts);
+
+/* The Langevin step of the shared capacities from the replica-weighted score
+   (src/replicas.jl:697 sbar = sum_j w_j sk_j; langevin_capacities :391, langevin_update :368)
+   followed by the dispatch following of every replica (follow_capacities! :448:
+   set_dispatchable_capacity! :412 and the kop curve of renewables and storage, src/kop.jl).
+   w [R] replica weights; eta [nkf], kappa_s [nkf] per capacity group; xi [K] standard normals
+   (NULL: drawn from the context's Philox stream at counter `it`); knew_out [K] (may be NULL);
+   nclip_out (may be NULL). */
+int esm_langevin_step(esm_ctx *ctx, const double *w, const double *eta, const double *kappa_s,
+                      double kappa_min, double clip, int32_t box, const double *xi, int64_t it,
+                      double *knew_out, int32_t *nclip_out);
+
+/* Weather step of the replicas flagged in `moved` [R] (0/1): pCN of angle theta[r] in the VAR
+   innovations (src/replicas.jl:105 pcn_weather), then with window[r] > 0 a regime window move of
+   that length starting at wstart[r] (:156 regime_window, uniforms from the stream), then the
+   compensated initialisation of the operation (:207 compensate_weather!). xi (may be NULL):
+   injected normals [R*n0*T]. */
+int esm_weather_step(esm_ctx *ctx, const int32_t *moved, const double *theta,
+                     const int32_t *window, const int32_t *wstart, const double *xi, int64_t it);
+
+/* Synchronise the context's stream with a bounded wait (ESM_ETIMEOUT after timeout_s). */
+int esm_sync(esm_ctx *ctx, double timeout_s);
+
+/* Device launches recorded since creation (kernels of this library). */
+int64_t esm_launch_count(const esm_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ESMCUDA_H */

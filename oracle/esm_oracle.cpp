@@ -1,0 +1,1479 @@
+/*
+ * CPU ORACLE of the replica-sampler hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain FP64 restatement of the reference's algorithms (FHell/ESM-Sampling, Julia), function by
+ * function, for the synthetic model of this repository (no losses, soft limits, links, unit
+ * commitment, vintages or weather entries: the cacheable "plain model" of src/local.jl:984).
+ * It is the checker of the CUDA library and the timed CPU baseline; nothing in the product links
+ * or calls it. Random numbers follow the Philox stream contract of philox.h, so that the CUDA
+ * path can be replayed move by move.
+ *
+ * Reference files cited as path:line within the reference project.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../include/esmcuda.h"
+#include "philox.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+using std::vector;
+
+// ------------------------------------------------------------------------------------------
+// model copy
+// ------------------------------------------------------------------------------------------
+struct Model {
+    int N, L, T, K, D, S, n0, nreg, nfields, nlev;
+    double dt, c_shed, c_dump, c_viol, gamma_k, kappa0, beta_v, beta_k;
+    bool physical;
+    vector<int> bus0, bus1;
+    vector<double> lb, ls;
+    vector<int> ukind, ugroup, ubus, useries;
+    vector<double> umc, ucapex, ulo, uhi, uavail, uhours, uetain, uetaout, uqt;
+    vector<int> disp, stor;
+    vector<int> sfield, snode;
+    vector<double> xbar, wscale, Ptr, pi0, phi, mu, sig, sig0;
+    vector<int> frole, fap, ap, ai;
+    vector<double> av;
+    vector<int> nlp, nl, up, ua, sp, sa;
+    vector<double> qcum;
+    vector<int> clp, cp, cu;
+    vector<int> xpp, xp, xnp, xn, xlp, xln;
+    vector<double> xv, xlg, Z;
+    vector<int> comp;
+    vector<int> theta_nnz;  // theta atoms touching node n
+    vector<int> disp_of_unit, stor_of_unit;
+};
+
+template <class T>
+static vector<T> cp_(const T *p, size_t n) {
+    return p ? vector<T>(p, p + n) : vector<T>(n, T(0));
+}
+
+struct Opts {
+    int R, max_points, span;
+    uint64_t seed;
+    double extra, maxnats, kmin;
+    double rates[ESM_NFAM];
+};
+
+struct Ctx {
+    Model m;
+    Opts o;
+    // state (X, T, R), replica fastest
+    vector<double> theta, g, e, z, k, r, F;
+    vector<int> reg;
+    vector<double> sk_last, fk_last;  // scores of the last capacity_scores call
+    bool has_scores = false;
+};
+
+static inline size_t ix(const Ctx &c, int x, int t, int rep) {
+    return ((size_t)x * c.m.T + t) * c.o.R + rep;
+}
+static inline double clampd(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+static inline double kcl(const Ctx &c, int u) { return clampd(c.k[u], c.m.ulo[u], c.m.uhi[u]); }
+
+// weather data map (src/energy.jl:515 datamap; the logistic availability map is the builder
+// decision of the synthetic model)
+static inline double wraw(const Ctx &c, int s, int t, int rep) {
+    return c.m.xbar[(size_t)s * c.m.T + t] + c.m.wscale[s] * c.z[ix(c, s, t, rep)];
+}
+static inline double avail_map(double x) { return 1.0 / (1.0 + exp(-x)); }
+static inline double load_map(double x) { return x > 0.0 ? x : 0.0; }
+
+// ------------------------------------------------------------------------------------------
+// cost pieces (src/local.jl:760 gen_cost, src/energy.jl:448 soc_cost, src/local.jl:773 phibal)
+// ------------------------------------------------------------------------------------------
+static inline double gen_cost(double mc, double A, double k, double w, double dt, double cv, double y, double *p) {
+    double yc = clampd(y, 0.0, 1.0);
+    *p = A * k * yc;
+    return dt * mc * (*p) + cv * dt * w * fabs(y - yc);
+}
+
+static inline double soc_cost(const Model &m, int u, double k, double w, double dt, double cv, double ye, double ye1,
+                              double *dout, double *jout) {
+    double ec = clampd(ye, 0.0, 1.0), ec1 = clampd(ye1, 0.0, 1.0);
+    double h = m.uhours[u];
+    double d = h * (ec1 - ec) / dt - m.uqt[u];
+    double eta = m.uetain[u];
+    double pc, mcx;
+    if (d >= 0) {
+        pc = eta > 0 ? d / eta : 0.0;
+        mcx = 0.0;
+    } else {
+        pc = 0.0;
+        mcx = std::min(-d * m.uetaout[u], 1.0);
+    }
+    double c = dt * m.umc[u] * k * (pc + mcx) + cv * w * h * fabs(ye - ec);
+    if (pc > 1) c += cv * dt * w * (pc - 1);
+    if (d < 0 && m.uqt[u] <= 0) {
+        double ex = -d * m.uetaout[u] - 1.0;
+        if (ex > 0) c += cv * dt * w * ex;
+    }
+    if (d >= 0 && eta <= 0) c += cv * dt * w * d;
+    *dout = d;
+    *jout = k * (pc - mcx);
+    return c;
+}
+
+// soc_power (src/energy.jl:437)
+static inline void soc_power(const Model &m, int u, double dt, double ec, double ec1, double *pc, double *mcx) {
+    double d = m.uhours[u] * (ec1 - ec) / dt - m.uqt[u];
+    if (d >= 0) {
+        *pc = m.uetain[u] > 0 ? d / m.uetain[u] : 0.0;
+        *mcx = 0.0;
+    } else {
+        *pc = 0.0;
+        *mcx = std::min(-d * m.uetaout[u], 1.0);
+    }
+}
+
+static inline double phibal(const Model &m, double x) { return x > 0 ? m.c_shed * x : -m.c_dump * x; }
+
+// logseg (src/local.jl:1099), trexp_offset (src/local.jl:1106) with the uniform given
+static inline double logseg(double L, double x) {
+    if (fabs(x) < 1e-10) return log(L) - x / 2;
+    if (x > 0) return log(L) + log(-expm1(-x)) - log(x);
+    return log(L) - x + log(-expm1(x)) - log(-x);
+}
+static inline double trexp_offset(double u, double g, double L) {
+    double x = g * L;
+    if (fabs(x) < 1e-10) return u * L;
+    if (g > 0) return -log1p(-u * (-expm1(-x))) / g;
+    return L + log1p(-u * (-expm1(x))) / (-g);
+}
+
+// ------------------------------------------------------------------------------------------
+// caches: LocalCost / rebuild_step! (src/local.jl:313-374)
+// ------------------------------------------------------------------------------------------
+static void rebuild_step(Ctx &c, int t, int rep) {
+    const Model &m = c.m;
+    int T = m.T;
+    for (int n = 0; n < m.N; ++n) c.r[ix(c, n, t, rep)] = load_map(wraw(c, n, t, rep));
+    for (int e = 0; e < m.L; ++e) {
+        int a = m.bus0[e], b = m.bus1[e];
+        double fl = m.lb[e] * (c.theta[ix(c, a, t, rep)] - c.theta[ix(c, b, t, rep)]);
+        c.F[ix(c, e, t, rep)] = fl;
+        c.r[ix(c, a, t, rep)] += fl + 0.5 * 0.0;
+        c.r[ix(c, b, t, rep)] += -fl + 0.5 * 0.0;
+    }
+    for (int u = 0; u < m.K; ++u) {  // generators in group order (renewables, dispatchable)
+        if (m.ukind[u] == ESM_UNIT_STOR) continue;
+        double A, y;
+        if (m.ukind[u] == ESM_UNIT_REN) {
+            A = avail_map(wraw(c, m.useries[u], t, rep));
+            y = 1.0;
+        } else {
+            A = m.uavail[u];
+            y = clampd(c.g[ix(c, m.disp_of_unit[u], t, rep)], 0.0, 1.0);
+        }
+        c.r[ix(c, m.ubus[u], t, rep)] -= A * kcl(c, u) * y;
+    }
+    for (int j = 0; j < m.S; ++j) {
+        int u = m.stor[j];
+        double pc, mcx;
+        soc_power(m, u, m.dt, clampd(c.e[ix(c, j, t, rep)], 0.0, 1.0), clampd(c.e[ix(c, j, (t + 1) % T, rep)], 0.0, 1.0),
+                  &pc, &mcx);
+        c.r[ix(c, m.ubus[u], t, rep)] += kcl(c, u) * (pc - mcx);
+    }
+}
+
+static void rebuild(Ctx &c, int nthreads) {
+    int T = c.m.T, R = c.o.R;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int q = 0; q < T * R; ++q) rebuild_step(c, q / R, q % R);
+}
+
+// ------------------------------------------------------------------------------------------
+// move workspace (MoveWS, src/local.jl:451) restricted to the plain model
+// ------------------------------------------------------------------------------------------
+enum { EK_THETA = 0, EK_GEN = 1, EK_SE = 2 };
+struct Ent {
+    int kind, idx;
+    double a, ak;
+    int kid;
+};
+struct Kink {
+    double Q, g, phi, Pm, e, nm;
+};
+struct WS {
+    int tau;
+    vector<Ent> ent;
+    vector<int> pos[3];  // entry position per (kind, idx), -1 none
+    vector<Kink> kinks;
+    vector<int> lines;
+    vector<char> lmark;
+    vector<double> dfl;
+    vector<int> nodes;
+    vector<char> nmark;
+    vector<double> dr;
+    vector<int> stu;
+    vector<char> smark;
+    vector<double> bps, sec;
+    void init(const Model &m) {
+        pos[0].assign(m.N, -1);
+        pos[1].assign(m.D, -1);
+        pos[2].assign(m.S, -1);
+        lmark.assign(m.L, 0);
+        dfl.assign(m.L, 0.0);
+        nmark.assign(m.N, 0);
+        dr.assign(m.N, 0.0);
+        smark.assign(m.S, 0);
+    }
+    void clear() {  // clear! (src/local.jl:536)
+        for (auto &en : ent) pos[en.kind][en.idx] = -1;
+        ent.clear();
+        kinks.clear();
+        for (int e : lines) lmark[e] = 0;
+        lines.clear();
+        for (int n : nodes) {
+            nmark[n] = 0;
+            dr[n] = 0.0;
+        }
+        nodes.clear();
+        for (int s : stu) smark[s] = 0;
+        stu.clear();
+        bps.clear();
+        sec.clear();
+    }
+    double dy(int kind, int idx) const {
+        int p = pos[kind][idx];
+        return p < 0 ? 0.0 : ent[p].a;
+    }
+    Ent *find_or_add(int kind, int idx) {
+        int &p = pos[kind][idx];
+        if (p < 0) {
+            p = (int)ent.size();
+            ent.push_back(Ent{kind, idx, 0.0, 0.0, -1});
+        }
+        return &ent[p];
+    }
+    void add_entry(int kind, int idx, double a) {  // add_entry! (src/local.jl:558)
+        if (a == 0.0) return;
+        find_or_add(kind, idx)->a += a;
+    }
+    void add_kentry(int j, double a, int kid) {  // add_kentry! (src/local.jl:583)
+        if (a == 0.0) return;
+        Ent *en = find_or_add(EK_GEN, j);
+        en->kid = kid;
+        en->ak += a;
+    }
+    void touch(int n) {
+        if (nmark[n]) return;
+        nmark[n] = 1;
+        nodes.push_back(n);
+    }
+};
+
+static inline double yval(const Ctx &c, int kind, int idx, int t, int rep) {
+    if (kind == EK_THETA) return c.theta[ix(c, idx, t, rep)];
+    if (kind == EK_GEN) return c.g[ix(c, idx, t, rep)];
+    return c.e[ix(c, idx, t, rep)];
+}
+static inline int ent_bus(const Model &m, int kind, int idx) {
+    if (kind == EK_THETA) return idx;
+    if (kind == EK_GEN) return m.ubus[m.disp[idx]];
+    return m.ubus[m.stor[idx]];
+}
+
+// finalize! (src/local.jl:656), plain model
+static void finalize_ws(const Ctx &c, WS &w, int rep) {
+    const Model &m = c.m;
+    int t = w.tau;
+    for (auto &k : w.kinks)
+        if (k.g != 0.0) w.bps.push_back(-k.Q / k.g);
+    for (auto &en : w.ent) {
+        double a = en.a, ak = en.ak;
+        if (fabs(a) < 1e-14) {
+            en.a = 0.0;
+            a = 0.0;
+        }
+        if (a == 0.0 && ak == 0.0) continue;
+        double y0 = yval(c, en.kind, en.idx, t, rep);
+        if (ak != 0.0) {
+            w.touch(ent_bus(m, en.kind, en.idx));
+            const Kink &k = w.kinks[en.kid];
+            double Q = k.Q, gk = k.g;
+            double offs[4][2] = {{0.0, a + ak * gk}, {0.0, a}, {-ak * Q, a}, {ak * Q, a + ak * gk}};
+            for (auto &os : offs) {
+                double off = os[0], sl = os[1];
+                if (sl == 0.0) continue;
+                w.bps.push_back((0.0 - y0 - off) / sl);
+                w.bps.push_back((1.0 - y0 - off) / sl);
+            }
+            continue;
+        }
+        if (en.kind == EK_THETA) {
+            for (int q = m.nlp[en.idx]; q < m.nlp[en.idx + 1]; ++q) {
+                int e = m.nl[q];
+                if (!w.lmark[e]) {
+                    w.lmark[e] = 1;
+                    w.lines.push_back(e);
+                }
+            }
+            continue;
+        }
+        w.bps.push_back((0.0 - y0) / a);
+        w.bps.push_back((1.0 - y0) / a);
+        if (en.kind == EK_GEN) {
+            w.touch(ent_bus(m, en.kind, en.idx));
+        } else {
+            if (!w.smark[en.idx]) {
+                w.smark[en.idx] = 1;
+                w.stu.push_back(en.idx);
+            }
+            w.touch(ent_bus(m, en.kind, en.idx));
+        }
+    }
+    size_t keep = 0;
+    for (size_t q = 0; q < w.lines.size(); ++q) {
+        int e = w.lines[q];
+        int a = m.bus0[e], b = m.bus1[e];
+        double df = m.lb[e] * (w.dy(EK_THETA, a) - w.dy(EK_THETA, b));
+        if (fabs(df) <= 1e-14) {
+            w.lmark[e] = 0;
+            continue;
+        }
+        w.lines[keep++] = e;
+        w.dfl[e] = df;
+        w.touch(a);
+        w.touch(b);
+        double f0 = c.F[ix(c, e, t, rep)];
+        double se = m.ls[e];
+        w.bps.push_back((1.0 * se - f0) / df);
+        w.bps.push_back((-1.0 * se - f0) / df);
+    }
+    w.lines.resize(keep);
+}
+
+// link_soc! (src/local.jl:630)
+static void link_soc(const Model &m, WS &wa, const WS &wb) {
+    for (auto &en : wb.ent) {
+        if (en.kind != EK_SE) continue;
+        if (en.a == 0.0) continue;
+        if (!wa.smark[en.idx]) {
+            wa.smark[en.idx] = 1;
+            wa.stu.push_back(en.idx);
+        }
+        wa.touch(m.ubus[m.stor[en.idx]]);
+    }
+}
+
+// eval_move! / eval_cached! (src/local.jl:789, :926) for one step workspace
+static double eval_ws(const Ctx &c, WS &w, int rep, double t, const WS *next, vector<double> &sec) {
+    const Model &m = c.m;
+    int tau = w.tau, T = m.T;
+    double dt = m.dt, cv = m.c_viol, k0 = m.kappa0;
+    double D = 0.0;
+    for (int n : w.nodes) w.dr[n] = 0.0;
+    for (auto &k : w.kinks) k.phi = std::max(k.Q + k.g * t, 0.0) - std::max(k.Q, 0.0);
+    for (auto &en : w.ent) {
+        if (en.kind != EK_GEN) continue;
+        if (en.a == 0.0 && en.kid < 0) continue;
+        int u = m.disp[en.idx];
+        double y0 = c.g[ix(c, en.idx, tau, rep)];
+        double k = kcl(c, u), A = m.uavail[u];
+        double y1 = y0 + (t * en.a + (en.kid >= 0 ? en.ak * w.kinks[en.kid].phi : 0.0));
+        double p0, p1;
+        double c0 = gen_cost(m.umc[u], A, k, k + k0, dt, cv, y0, &p0);
+        double c1 = gen_cost(m.umc[u], A, k, k + k0, dt, cv, y1, &p1);
+        D += c1 - c0;
+        w.dr[m.ubus[u]] -= p1 - p0;
+    }
+    for (int e : w.lines) {
+        double df = w.dfl[e];
+        double f0 = c.F[ix(c, e, tau, rep)], f1 = f0 + t * df;
+        double se = m.ls[e];
+        D += cv * dt * (std::max(fabs(f1) - se, 0.0) - std::max(fabs(f0) - se, 0.0));
+        w.dr[m.bus0[e]] += f1 - f0;
+        w.dr[m.bus1[e]] -= f1 - f0;
+    }
+    int t1 = (tau + 1) % T;
+    for (int j : w.stu) {
+        int u = m.stor[j];
+        double k = kcl(c, u), ww = k + k0;
+        double ye = c.e[ix(c, j, tau, rep)], ye1 = c.e[ix(c, j, t1, rep)];
+        double dye1 = next ? next->dy(EK_SE, j) : 0.0;
+        double d0, j0, d1, j1;
+        double c0 = soc_cost(m, u, k, ww, dt, cv, ye, ye1, &d0, &j0);
+        double c1 = soc_cost(m, u, k, ww, dt, cv, ye + t * w.dy(EK_SE, j), ye1 + t * dye1, &d1, &j1);
+        D += c1 - c0;
+        w.dr[m.ubus[u]] += j1 - j0;
+        sec.push_back(d1);
+        sec.push_back(m.uetain[u] > 0 ? d1 - m.uetain[u] : 1.0);
+        sec.push_back(-d1 * m.uetaout[u] - 1.0);
+    }
+    for (int n : w.nodes) {  // balance cells = nodes at the complete level
+        double S0 = c.r[ix(c, n, tau, rep)];
+        double S1 = S0 + (0.0 + w.dr[n]);
+        D += dt * 1 * (phibal(m, S1 / 1) - phibal(m, S0 / 1));
+        sec.push_back(S1);
+    }
+    return D;
+}
+
+// a prepared block move over (tau-1, tau) (BlockMove, src/local.jl:1196): ws = step tau, wa = tau-1
+struct Mover {
+    const Ctx *c;
+    WS *ws, *wa;
+    int rep;
+    double beta;
+    vector<double> sec;
+    double eval(double t) {  // mv_eval! (src/local.jl:1219): later step first
+        sec.clear();
+        double D = 0.0;
+        D += eval_ws(*c, *ws, rep, t, nullptr, sec);
+        D += eval_ws(*c, *wa, rep, t, ws, sec);
+        return D;
+    }
+    bool hasstor() const { return !ws->stu.empty() || !wa->stu.empty(); }
+    void mask(vector<char> &g) const {  // storage_mask! (src/local.jl:1244)
+        g.clear();
+        for (const WS *w : {ws, wa}) {
+            for (size_t j = 0; j < w->stu.size() * 3; ++j) g.push_back(1);
+            for (size_t j = 0; j < w->nodes.size(); ++j) g.push_back(0);
+        }
+    }
+};
+
+static inline bool wlt(double a, double b, double s) { return s > 0 ? a < b : a > b; }
+static void sort_walk(vector<double> &v, double s) {
+    std::stable_sort(v.begin(), v.end(), [s](double a, double b) { return wlt(a, b, s); });
+}
+
+struct Walk {
+    vector<double> pts, cs;
+    int cap;
+    bool full = false;
+    void push(double x, double cx) {
+        if ((int)pts.size() >= cap) {
+            full = true;
+            return;
+        }
+        pts.push_back(x);
+        cs.push_back(cx);
+    }
+};
+
+// piece_roots! (src/local.jl:1267)
+static double piece_roots(Walk &W, Mover &mv, double cmin, const vector<double> &A, const vector<double> &B, double a,
+                          double b, const vector<char> &gmask, double sgn) {
+    vector<double> sroots;
+    for (size_t j = 0; j < B.size(); ++j) {
+        if (gmask[j]) continue;
+        double u = A[j], v = B[j];
+        if ((u < 0) != (v < 0) && u != v) {
+            double x = a + (b - a) * u / (u - v);
+            if (sgn * (x - a) > 0 && sgn * (b - x) > 0) sroots.push_back(x);
+        }
+    }
+    if (sroots.empty()) return cmin;
+    sort_walk(sroots, sgn);
+    for (double x : sroots) {
+        double cx = mv.beta * mv.eval(x);
+        W.push(x, cx);
+        cmin = std::min(cmin, cx);
+    }
+    return cmin;
+}
+
+// walk! (src/local.jl:1294) for the plain model (no requirement-tracking kinks, no Gaussian part)
+// returns 1 proper, 0 improper (ray steps exhausted)
+static int walk(Walk &W, Mover &mv, vector<double> &bp, double sgn, double maxnats, const vector<double> &sec0) {
+    double tp = 0.0;
+    vector<double> secprev = sec0, secB, secE, roots, groots;
+    bool stor = mv.hasstor();
+    vector<char> gmask;
+    if (stor) mv.mask(gmask);
+    double cmin = 0.0;
+    size_t idx = 0;
+    double delta = 0.0;
+    int nx = 0;
+    sort_walk(bp, sgn);
+    while (true) {
+        double t;
+        if (idx < bp.size()) {
+            t = bp[idx++];
+            if (t == tp) continue;
+        } else {
+            double cprev = W.cs.empty() ? 0.0 : W.cs.back();
+            double hp = 1e-6 * std::max(1.0, fabs(tp));
+            double sl = (mv.beta * mv.eval(tp + sgn * hp) + 0.0 - cprev - 0.0) / hp;
+            if (sl > 0)
+                delta = std::min(2 * maxnats / sl, 1e3 * std::max(fabs(tp), 1e-3));
+            else
+                delta = delta == 0.0 ? std::max(fabs(tp), 1e-6) : 2 * delta;
+            t = tp + sgn * delta;
+            nx += 1;
+            if (nx > 80) return 0;
+        }
+        double cval = mv.beta * mv.eval(t);
+        vector<double> sec = mv.sec;
+        roots.clear();
+        groots.clear();
+        for (size_t j = 0; j < sec.size(); ++j) {
+            double a = secprev[j], b = sec[j];
+            if ((a < 0) != (b < 0) && a != b) {
+                double x = tp + (t - tp) * a / (a - b);
+                if (sgn * (x - tp) > 0 && sgn * (t - x) > 0) {
+                    if (stor && gmask[j])
+                        groots.push_back(x);
+                    else
+                        roots.push_back(x);
+                }
+            }
+        }
+        if (stor && !groots.empty()) {
+            secE = sec;
+            sort_walk(groots, sgn);
+            double a0 = tp;
+            for (double x : groots) {
+                double cx = mv.beta * mv.eval(x);
+                secB = mv.sec;
+                cmin = piece_roots(W, mv, cmin, secprev, secB, a0, x, gmask, sgn);
+                W.push(x, cx);
+                cmin = std::min(cmin, cx);
+                secprev = secB;
+                a0 = x;
+            }
+            cmin = piece_roots(W, mv, cmin, secprev, secE, a0, t, gmask, sgn);
+            secprev = secE;
+        } else {
+            secprev = sec;
+            if (!roots.empty()) {
+                sort_walk(roots, sgn);
+                for (double x : roots) {
+                    double cx = mv.beta * mv.eval(x);
+                    W.push(x, cx);
+                    cmin = std::min(cmin, cx);
+                }
+            }
+        }
+        W.push(t, cval);
+        cmin = std::min(cmin, cval);
+        if (cval + 0.0 - cmin > maxnats) return 1;
+        if (W.full) return 1;
+        tp = t;
+    }
+}
+
+// sample_line! (src/local.jl:1501) with the uniforms (u_cat, u_off) given; *guard set when the
+// walk exceeded the point cap (the move is then not taken)
+static double sample_line(Mover &mv, double maxnats, int cap, double u_cat, double u_off, bool *guard) {
+    vector<double> right, left;
+    for (const WS *w : {mv.wa, mv.ws})
+        for (double x : w->bps) {
+            if (!std::isfinite(x)) continue;
+            if (x > 0.0)
+                right.push_back(x);
+            else if (x < 0.0)
+                left.push_back(x);
+        }
+    mv.eval(0.0);
+    vector<double> sec0 = mv.sec;
+    Walk Wr, Wl;
+    Wr.cap = Wl.cap = cap;
+    *guard = false;
+    if (!walk(Wr, mv, right, 1.0, maxnats, sec0)) return 0.0;
+    if (Wr.full) {
+        *guard = true;
+        return 0.0;
+    }
+    if (!walk(Wl, mv, left, -1.0, maxnats, sec0)) return 0.0;
+    if (Wl.full) {
+        *guard = true;
+        return 0.0;
+    }
+    vector<double> pts, cs;
+    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) {
+        pts.push_back(Wl.pts[j]);
+        cs.push_back(Wl.cs[j]);
+    }
+    pts.push_back(0.0);
+    cs.push_back(0.0);
+    pts.insert(pts.end(), Wr.pts.begin(), Wr.pts.end());
+    cs.insert(cs.end(), Wr.cs.begin(), Wr.cs.end());
+    int nseg = (int)pts.size() - 1;
+    vector<double> lm(nseg);
+    double mx = -INFINITY;
+    for (int j = 0; j < nseg; ++j) {
+        double L = pts[j + 1] - pts[j];
+        lm[j] = L > 0 ? -std::min(cs[j], cs[j + 1]) + logseg(L, fabs(cs[j + 1] - cs[j])) : -INFINITY;
+        mx = std::max(mx, lm[j]);
+    }
+    double tot = 0.0;
+    for (int j = 0; j < nseg; ++j) tot += exp(lm[j] - mx);
+    double u = u_cat * tot, acc = 0.0;
+    int jj = nseg - 1;
+    for (int q = 0; q < nseg; ++q) {
+        acc += exp(lm[q] - mx);
+        if (u <= acc) {
+            jj = q;
+            break;
+        }
+    }
+    double L = pts[jj + 1] - pts[jj];
+    double g = (cs[jj + 1] - cs[jj]) / L;
+    return (g >= 0 || fabs(g * L) < 1e-10) ? pts[jj] + trexp_offset(u_off, g, L)
+                                          : pts[jj + 1] - trexp_offset(u_off, -g, L);
+}
+
+// commit_block! / apply_step! (src/local.jl:2495, :2507)
+static void commit(Ctx &c, Mover &mv, double t) {
+    if (t == 0.0) return;
+    mv.eval(t);
+    const Model &m = c.m;
+    for (WS *w : {mv.wa, mv.ws}) {
+        int tau = w->tau;
+        for (auto &en : w->ent) {
+            double d = t * en.a + (en.kid >= 0 ? en.ak * w->kinks[en.kid].phi : 0.0);
+            if (en.kind == EK_THETA)
+                c.theta[ix(c, en.idx, tau, mv.rep)] += d;
+            else if (en.kind == EK_GEN)
+                c.g[ix(c, en.idx, tau, mv.rep)] += d;
+            else
+                c.e[ix(c, en.idx, tau, mv.rep)] += d;
+        }
+        for (int e : w->lines) c.F[ix(c, e, tau, mv.rep)] += t * w->dfl[e];
+        for (int n : w->nodes) c.r[ix(c, n, tau, mv.rep)] += w->dr[n];
+    }
+    (void)m;
+}
+
+// ------------------------------------------------------------------------------------------
+// move selection (src/local.jl:1567-1900), with the tile stream of philox.h
+// ------------------------------------------------------------------------------------------
+struct TileStream {
+    uint64_t seed;
+    uint32_t tile, cls, sweep, j = 0;
+    double next() {
+        double u0, u1;
+        orc_uniform2(seed, ESM_TAG_LIST, j >> 1, tile, cls, sweep, &u0, &u1);
+        double u = (j & 1) ? u1 : u0;
+        ++j;
+        return u;
+    }
+    int pick(int n) {
+        int i = (int)floor(next() * n);
+        return i >= n ? n - 1 : i;
+    }
+};
+
+struct MoveRef {
+    int kind;  // -1 atom, else family
+    int field, atom;
+};
+
+static void move_list(const Ctx &c, TileStream &ts, vector<MoveRef> &out) {
+    const Model &m = c.m;
+    out.clear();
+    for (int f = 0; f < m.nfields; ++f)
+        for (int a = m.fap[f]; a < m.fap[f + 1]; ++a) out.push_back(MoveRef{-1, f, a});
+    int nextra = (int)nearbyint(c.o.extra * m.N);
+    double cum[ESM_NFAM], tot = 0.0;
+    for (int q = 0; q < ESM_NFAM; ++q) {
+        tot += c.o.rates[q];
+        cum[q] = tot;
+    }
+    for (int q = 0; q < ESM_NFAM; ++q) cum[q] /= tot;
+    for (int i = 0; i < nextra; ++i) {
+        double u = ts.next();
+        int kd = ESM_NFAM - 1;
+        for (int q = 0; q < ESM_NFAM; ++q)
+            if (cum[q] >= u) {
+                kd = q;
+                break;
+            }
+        out.push_back(MoveRef{kd, -1, -1});
+    }
+    for (int i = (int)out.size() - 1; i >= 1; --i) {  // Fisher-Yates
+        int j = ts.pick(i + 1);
+        std::swap(out[i], out[j]);
+    }
+}
+
+static inline double kappa_unit(const Ctx &c, int j) {  // kappa_unit (src/local.jl:1585), dispatchable j
+    int u = c.m.disp[j];
+    return c.m.uavail[u] * kcl(c, u);
+}
+
+// prorata! (src/local.jl:1782), plain model (no tracking kinks)
+static bool prorata(const Ctx &c, WS &w, int rep, int mnode, double g, vector<Kink> *jac) {
+    const Model &m = c.m;
+    if (g == 0.0) return false;
+    int tau = w.tau;
+    double Pm = 0.0, Qs = 0.0;
+    int nu = 0;
+    for (int q = m.up[mnode]; q < m.up[mnode + 1]; ++q) {
+        int j = m.ua[q];
+        double kap = kappa_unit(c, j);
+        if (!(fabs(kap) >= c.o.kmin)) continue;
+        double om = c.g[ix(c, j, tau, rep)];
+        Pm += kap * om;
+        Qs += kap * clampd(om, 0.0, 1.0);
+        nu += 1;
+    }
+    if (nu == 0) return false;
+    if (fabs(Pm) < 1e-6) return false;
+    double Q = c.r[ix(c, mnode, tau, rep)] + Qs + 0.0;
+    double e = Pm - std::max(Q, 0.0);
+    double nm = (double)(nu - 1);
+    w.kinks.push_back(Kink{Q, g, 0.0, Pm, e, nm});
+    int kid = (int)w.kinks.size() - 1;
+    for (int q = m.up[mnode]; q < m.up[mnode + 1]; ++q) {
+        int j = m.ua[q];
+        double kap = kappa_unit(c, j);
+        if (!(fabs(kap) >= c.o.kmin)) continue;
+        double sigma = kap * c.g[ix(c, j, tau, rep)] / Pm;
+        if (sigma == 0.0) continue;
+        w.add_kentry(j, sigma / kap, kid);
+    }
+    jac->push_back(w.kinks.back());
+    return true;
+}
+
+// prep_random!, prep_xloc!, prep_spair! (src/local.jl:1608, :1672, :1708)
+static bool prep_family(const Ctx &c, TileStream &ts, int fam, WS &ws, WS &wa, int rep, vector<Kink> *jac) {
+    const Model &m = c.m;
+    int N = m.N;
+    double kmin = c.o.kmin;
+    auto nunits = [&](int n) { return m.up[n + 1] - m.up[n]; };
+    switch (fam) {
+        case ESM_FAM_UNIT: {
+            int n = ts.pick(N);
+            if (nunits(n) == 0) return false;
+            int j = m.ua[m.up[n] + ts.pick(nunits(n))];
+            ws.add_entry(EK_GEN, j, 1.0);
+            return true;
+        }
+        case ESM_FAM_PAIR:
+        case ESM_FAM_XPAIR: {
+            int n = ts.pick(N);
+            int mm = fam == ESM_FAM_PAIR ? n : ts.pick(N);
+            if (fam == ESM_FAM_XPAIR && (mm == n || m.comp[mm] != m.comp[n])) return false;
+            if (nunits(n) == 0 || nunits(mm) == 0) return false;
+            int u1 = m.ua[m.up[n] + ts.pick(nunits(n))];
+            int u2 = m.ua[m.up[mm] + ts.pick(nunits(mm))];
+            if (u1 == u2) return false;
+            double k1 = kappa_unit(c, u1), k2 = kappa_unit(c, u2);
+            if (fabs(k1) < kmin || fabs(k2) < kmin) return false;
+            ws.add_entry(EK_GEN, u1, 1 / k1);
+            ws.add_entry(EK_GEN, u2, -1 / k2);
+            if (fam == ESM_FAM_XPAIR) {  // prep_reroute! (src/local.jl:1592)
+                for (int i = 0; i < N; ++i) {
+                    if (m.comp[i] != m.comp[n]) continue;
+                    double x = m.Z[(size_t)i * N + n] - m.Z[(size_t)i * N + mm];
+                    if (fabs(x) < 1e-15) continue;
+                    ws.add_entry(EK_THETA, i, x);
+                }
+            }
+            return true;
+        }
+        case ESM_FAM_XLOC:
+        case ESM_FAM_XLOCC: {
+            int n = ts.pick(N);
+            int np = m.xpp[n + 1] - m.xpp[n];
+            if (np == 0) return false;
+            int jp = ts.pick(np);
+            int pair = m.xpp[n] + jp;
+            int mm = m.xp[pair];
+            if (nunits(n) == 0 || nunits(mm) == 0) return false;
+            int u1 = m.ua[m.up[n] + ts.pick(nunits(n))];
+            int u2 = m.ua[m.up[mm] + ts.pick(nunits(mm))];
+            double k1 = kappa_unit(c, u1), k2 = kappa_unit(c, u2);
+            if (fabs(k1) < kmin || fabs(k2) < kmin) return false;
+            jac->clear();
+            ws.add_entry(EK_GEN, u1, 1 / k1);
+            ws.add_entry(EK_GEN, u2, -1 / k2);
+            for (int q = m.xnp[pair]; q < m.xnp[pair + 1]; ++q) ws.add_entry(EK_THETA, m.xn[q], m.xv[q]);
+            if (fam == ESM_FAM_XLOCC)
+                for (int q = m.xlp[pair]; q < m.xlp[pair + 1]; ++q) prorata(c, ws, rep, m.xln[q], m.xlg[q], jac);
+            return true;
+        }
+        case ESM_FAM_POTENTIAL: {
+            int n = ts.pick(N);
+            if (m.theta_nnz[n] == 0) return false;
+            ws.add_entry(EK_THETA, n, 1.0);
+            return true;
+        }
+        case ESM_FAM_CELLPAIR:
+        case ESM_FAM_CELL: {
+            double u = ts.next();
+            int q = m.nlev - 1;
+            for (int l = 0; l < m.nlev; ++l)
+                if (m.qcum[l] >= u) {
+                    q = l;
+                    break;
+                }
+            int ncell = m.clp[q + 1] - m.clp[q];
+            int cidx = m.clp[q] + ts.pick(ncell);
+            // injecting fields present in the cell, in field (group) order
+            vector<int> fl;
+            for (int p = m.cp[cidx]; p < m.cp[cidx + 1]; ++p) {
+                int gidx = m.ugroup[m.disp[m.cu[p]]];
+                if (std::find(fl.begin(), fl.end(), gidx) == fl.end()) fl.push_back(gidx);
+            }
+            std::sort(fl.begin(), fl.end());
+            if (fl.empty()) return false;
+            if (fam == ESM_FAM_CELL) {
+                int f = fl[ts.pick((int)fl.size())];
+                for (int p = m.cp[cidx]; p < m.cp[cidx + 1]; ++p)
+                    if (m.ugroup[m.disp[m.cu[p]]] == f) ws.add_entry(EK_GEN, m.cu[p], 1.0);
+                return true;
+            }
+            if (fl.size() < 2) return false;
+            int f1 = fl[ts.pick((int)fl.size())];
+            int f2 = fl[ts.pick((int)fl.size())];
+            if (f1 == f2) return false;
+            double K1 = 0.0, K2 = 0.0;
+            for (int p = m.cp[cidx]; p < m.cp[cidx + 1]; ++p) {
+                int j = m.cu[p];
+                if (m.ugroup[m.disp[j]] == f1) K1 += kappa_unit(c, j);
+                if (m.ugroup[m.disp[j]] == f2) K2 += kappa_unit(c, j);
+            }
+            if (fabs(K1) < kmin || fabs(K2) < kmin) return false;
+            for (int p = m.cp[cidx]; p < m.cp[cidx + 1]; ++p)
+                if (m.ugroup[m.disp[m.cu[p]]] == f1) ws.add_entry(EK_GEN, m.cu[p], 1 / K1);
+            for (int p = m.cp[cidx]; p < m.cp[cidx + 1]; ++p)
+                if (m.ugroup[m.disp[m.cu[p]]] == f2) ws.add_entry(EK_GEN, m.cu[p], -1 / K2);
+            return true;
+        }
+        case ESM_FAM_SPAIR: {
+            int n = ts.pick(N);
+            int ns = m.sp[n + 1] - m.sp[n];
+            if (ns == 0 || nunits(n) == 0) return false;
+            int sj = m.sa[m.sp[n] + ts.pick(ns)];
+            int su = m.stor[sj];
+            double ks = kcl(c, su) * m.uhours[su] / m.dt;
+            if (ks < kmin) return false;
+            int u1 = m.ua[m.up[n] + ts.pick(nunits(n))];
+            int u2 = m.ua[m.up[n] + ts.pick(nunits(n))];
+            double k1 = kappa_unit(c, u1), k2 = kappa_unit(c, u2);
+            if (fabs(k1) < kmin || fabs(k2) < kmin) return false;
+            wa.add_entry(EK_GEN, u1, ks / k1);
+            ws.add_entry(EK_SE, sj, 1.0);
+            ws.add_entry(EK_GEN, u2, -ks / k2);
+            return true;
+        }
+    }
+    return false;
+}
+
+// the moves of one (replica, step) task: the body of the threaded loop of local_sweep!
+// (src/local.jl:1954-2051)
+static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int tau, int rep, uint32_t sweep,
+                     int64_t *stats, WS &ws, WS &wa) {
+    const Model &m = c.m;
+    int T = m.T;
+    int taum = (tau - 1 + T) % T;
+    TileStream ts = ts0;  // the selection draws continue after the list draws
+    vector<Kink> jac;
+    Mover mv{&c, &ws, &wa, rep, m.beta_v, {}};
+    for (size_t mi = 0; mi < moves.size(); ++mi) {
+        ws.clear();
+        wa.clear();
+        ws.tau = tau;
+        wa.tau = taum;
+        jac.clear();
+        const MoveRef &mr = moves[mi];
+        int fi;
+        if (mr.kind < 0) {  // prep_atom! (src/local.jl:1567)
+            int role = m.frole[mr.field];
+            int kind = role == ESM_ROLE_THETA ? EK_THETA : (role == ESM_ROLE_GEN ? EK_GEN : EK_SE);
+            for (int q = m.ap[mr.atom]; q < m.ap[mr.atom + 1]; ++q) ws.add_entry(kind, m.ai[q], m.av[q]);
+            fi = ESM_NFAM;
+        } else {
+            if (!prep_family(c, ts, mr.kind, ws, wa, rep, &jac)) continue;
+            fi = mr.kind;
+        }
+        finalize_ws(c, ws, rep);
+        if (ws.ent.empty()) continue;
+        finalize_ws(c, wa, rep);
+        link_soc(m, wa, ws);
+        double uc, uo, uj, un;
+        orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)tau, (uint32_t)rep, sweep, &uc, &uo);
+        orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)tau, (uint32_t)rep, sweep, &uj, &un);
+        bool guard = false;
+        double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
+        if (guard) stats[2 * (ESM_NFAM + 1)] += 1;
+        if (mr.kind == ESM_FAM_XLOCC && t != 0.0 && !jac.empty()) {
+            double lj = 0.0;  // logjac (src/local.jl:1871)
+            for (auto &k : jac) lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
+            if (uj >= exp(std::min(0.0, lj))) t = 0.0;
+        }
+        commit(c, mv, t);
+        stats[2 * fi] += 1;
+        stats[2 * fi + 1] += t != 0.0;
+    }
+    ws.clear();
+    wa.clear();
+}
+
+static void class_steps(int T, int cls, vector<int> &out) {
+    out.clear();
+    if (T % 2 == 1) {
+        if (cls == 0)
+            for (int t = 0; t < T - 1; t += 2) out.push_back(t);
+        else if (cls == 1)
+            for (int t = 1; t < T - 1; t += 2) out.push_back(t);
+        else
+            out.push_back(T - 1);
+    } else {
+        for (int t = cls; t < T; t += 2) out.push_back(t);
+    }
+}
+
+static int span_of(const Ctx &c) { return c.o.span > 0 ? c.o.span : std::max(1, 32 / c.o.R); }
+
+static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthreads) {
+    vector<int> steps;
+    class_steps(c.m.T, cls, steps);
+    int span = span_of(c);
+    int ntile = ((int)steps.size() + span - 1) / span;
+    int R = c.o.R;
+    int nst = 2 * (ESM_NFAM + 1) + 1;
+#pragma omp parallel num_threads(nthreads)
+    {
+        vector<int64_t> loc(nst, 0);
+        WS ws, wa;
+        ws.init(c.m);
+        wa.init(c.m);
+        vector<MoveRef> moves;
+#pragma omp for schedule(dynamic, 1)
+        for (int tile = 0; tile < ntile; ++tile) {
+            TileStream ts{c.o.seed, (uint32_t)tile, (uint32_t)cls, sweep};
+            move_list(c, ts, moves);
+            for (int q = tile * span; q < std::min((int)steps.size(), (tile + 1) * span); ++q)
+                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts, steps[q], rep, sweep, loc.data(), ws, wa);
+        }
+#pragma omp critical
+        for (int i = 0; i < nst; ++i) stats[i] += loc[i];
+    }
+}
+
+static void class_order(const Ctx &c, uint32_t sweep, int order[3], int *ncls) {
+    double u0, u1;
+    orc_uniform2(c.o.seed, ESM_TAG_SWEEP, 0, 0, 0, sweep, &u0, &u1);
+    if (c.m.T % 2 == 0) {
+        *ncls = 2;
+        order[0] = u0 < 0.5 ? 0 : 1;
+        order[1] = 1 - order[0];
+    } else {
+        *ncls = 3;
+        order[0] = 0;
+        order[1] = 1;
+        order[2] = 2;
+        int j = std::min(2, (int)floor(u0 * 3));
+        std::swap(order[2], order[j]);
+        j = std::min(1, (int)floor(u1 * 2));
+        std::swap(order[1], order[j]);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// energy cost with the capacity gradient (src/energy.jl:551-757) and capacity_scores
+// (src/replicas.jl:329)
+// ------------------------------------------------------------------------------------------
+static void scores(Ctx &c, double *sk, double *fk, double *parts, int nthreads) {
+    const Model &m = c.m;
+    int T = m.T, R = c.o.R, K = m.K;
+    double dt = m.dt, cv = m.c_viol, k0 = m.kappa0;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int rep = 0; rep < R; ++rep) {
+        vector<double> dk(K, 0.0);
+        vector<double> rr(m.N);
+        vector<double> Gr((size_t)m.N * T);
+        double cgen = 0, cst = 0, pen = 0, shed = 0, dump = 0;
+        // residual and the balance gradient per step
+        for (int t = 0; t < T; ++t) {
+            for (int n = 0; n < m.N; ++n) rr[n] = load_map(wraw(c, n, t, rep));
+            for (int e = 0; e < m.L; ++e) {
+                int a = m.bus0[e], b = m.bus1[e];
+                double fe = m.lb[e] * (c.theta[ix(c, a, t, rep)] - c.theta[ix(c, b, t, rep)]);
+                rr[a] += fe + 0.5 * 0.0;
+                rr[b] += -fe + 0.5 * 0.0;
+                pen += cv * dt * (m.ls[e] * std::max(fabs(fe) / m.ls[e] - 1.0, 0.0));
+            }
+            for (int u = 0; u < K; ++u) {
+                if (m.ukind[u] == ESM_UNIT_STOR) continue;
+                double A, Y, Yc;
+                if (m.ukind[u] == ESM_UNIT_REN) {
+                    A = avail_map(wraw(c, m.useries[u], t, rep));
+                    Y = Yc = 1.0;
+                } else {
+                    A = m.uavail[u];
+                    Y = c.g[ix(c, m.disp_of_unit[u], t, rep)];
+                    Yc = clampd(Y, 0.0, 1.0);
+                }
+                double kv = kcl(c, u);
+                double p = A * kv * Yc;
+                cgen += dt * (m.umc[u] * p);
+                rr[m.ubus[u]] -= p;
+                if (m.ukind[u] == ESM_UNIT_DISP) {
+                    double ex = fabs(Y - Yc);
+                    if (ex > 0) pen += cv * dt * (kv + k0) * ex;
+                }
+            }
+            for (int j = 0; j < m.S; ++j) {
+                int u = m.stor[j];
+                double kv = kcl(c, u);
+                double ye = c.e[ix(c, j, t, rep)], ye1 = c.e[ix(c, j, (t + 1) % T, rep)];
+                double d, jj;
+                double cc = soc_cost(m, u, kv, kv + k0, dt, cv, ye, ye1, &d, &jj);
+                double pc, mcx;
+                soc_power(m, u, dt, clampd(ye, 0.0, 1.0), clampd(ye1, 0.0, 1.0), &pc, &mcx);
+                cst += dt * m.umc[u] * kv * (pc + mcx);
+                pen += cc - dt * m.umc[u] * kv * (pc + mcx);
+                rr[m.ubus[u]] += jj;
+            }
+            for (int n = 0; n < m.N; ++n) {
+                double x = rr[n];
+                if (x > 0)
+                    shed += dt * x;
+                else
+                    dump -= dt * x;
+                Gr[(size_t)n * T + t] = dt * (x > 0 ? m.c_shed : (x < 0 ? -m.c_dump : 0.0));
+            }
+        }
+        // generators (gen_grad, src/energy.jl:835)
+        for (int t = 0; t < T; ++t)
+            for (int u = 0; u < K; ++u) {
+                if (m.ukind[u] == ESM_UNIT_STOR) continue;
+                double A, Y, Yc;
+                bool compf;
+                if (m.ukind[u] == ESM_UNIT_REN) {
+                    A = avail_map(wraw(c, m.useries[u], t, rep));
+                    Y = Yc = 1.0;
+                    compf = true;
+                } else {
+                    A = m.uavail[u];
+                    Y = c.g[ix(c, m.disp_of_unit[u], t, rep)];
+                    Yc = clampd(Y, 0.0, 1.0);
+                    compf = false;
+                }
+                double kv = kcl(c, u);
+                double Gn = Gr[(size_t)m.ubus[u] * T + t];
+                if (!(compf || (0.0 < Y && Y < 1.0))) dk[u] += cv * dt * fabs(Y - Yc);
+                double dck = m.umc[u] * A * Yc;
+                dk[u] += dt * dck - A * Yc * Gn;
+                (void)kv;
+            }
+        // storage (soc_grad, src/energy.jl:466)
+        for (int t = 0; t < T; ++t)
+            for (int j = 0; j < m.S; ++j) {
+                int u = m.stor[j];
+                int t1 = (t + 1) % T;
+                double h = m.uhours[u];
+                double Ec = clampd(c.e[ix(c, j, t, rep)], 0.0, 1.0), Ec1 = clampd(c.e[ix(c, j, t1, rep)], 0.0, 1.0);
+                double d = h * (Ec1 - Ec) / dt - m.uqt[u];
+                double g = Gr[(size_t)m.ubus[u] * T + t];
+                if (d >= 0 && m.uetain[u] <= 0) {
+                    dk[u] += cv * dt * d;
+                } else if (d >= 0) {
+                    double pc = d / m.uetain[u];
+                    dk[u] += dt * m.umc[u] * pc + g * pc + (pc > 1 ? cv * dt * (pc - 1) : 0.0);
+                } else {
+                    double mcx = -d * m.uetaout[u];
+                    double mcc = std::min(mcx, 1.0);
+                    dk[u] += dt * m.umc[u] * mcc - g * mcc + ((mcx > 1 && m.uqt[u] <= 0) ? cv * dt * (mcx - 1) : 0.0);
+                }
+            }
+        for (int t = 0; t < T; ++t)
+            for (int j = 0; j < m.S; ++j) {
+                int u = m.stor[j];
+                double y = c.e[ix(c, j, t, rep)];
+                if (!(0.0 < y && y < 1.0)) dk[u] += cv * m.uhours[u] * fabs(y - clampd(y, 0.0, 1.0));
+            }
+        // score: -beta_v mask dk + log measure gradient (src/replicas.jl:334, src/energy.jl:811)
+        for (int u = 0; u < K; ++u) {
+            double y = c.k[u];
+            bool in = m.ulo[u] < y && y < m.uhi[u];
+            double s = -m.beta_v * ((in ? 1.0 : 0.0) * dk[u]);
+            double lm = 0.0;
+            if (m.physical && m.ukind[u] != ESM_UNIT_REN && in) lm = (double)T / (y + k0);
+            sk[(size_t)rep * K + u] = s + lm;
+        }
+        if (parts) {
+            double capex = 0.0;
+            for (int u = 0; u < K; ++u) {
+                double kc = kcl(c, u);
+                capex += m.ucapex[u] * c.k[u] + m.gamma_k * m.ucapex[u] * fabs(c.k[u] - kc);
+            }
+            double *P = parts + (size_t)rep * 8;
+            P[0] = capex;
+            P[1] = cgen + cst + (m.c_shed * shed + m.c_dump * dump) + pen;
+            P[2] = cgen;
+            P[3] = cst;
+            P[4] = shed;
+            P[5] = dump;
+            P[6] = pen;
+            P[7] = 0.0;
+        }
+    }
+    for (int u = 0; u < K; ++u) {
+        double ex = c.k[u] - kcl(c, u);
+        double sg = ex > 0 ? 1.0 : (ex < 0 ? -1.0 : 0.0);
+        fk[u] = m.beta_k * (m.ucapex[u] + m.gamma_k * m.ucapex[u] * sg);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Langevin step and dispatch following (src/replicas.jl:357-473, src/kop.jl)
+// ------------------------------------------------------------------------------------------
+static double langevin_one(double k, double g, double xi, double eta, double ks, double kmin, double clip, bool box,
+                           double hi, int *nclip) {
+    double w = log(k + ks);
+    double dw0 = eta * ((k + ks) * g + 1);
+    if (fabs(dw0) > clip) *nclip += 1;
+    double w1 = w + clampd(dw0, -clip, clip) + sqrt(2 * eta) * xi;
+    double wmin = log(kmin + ks);
+    w1 = w1 < wmin ? 2 * wmin - w1 : w1;
+    if (box) {
+        double wmax = log(std::max(hi, kmin + 1.0) + ks);
+        if (w1 > wmax && w <= wmax) w1 = std::max(2 * wmax - w1, wmin);
+    }
+    return exp(w1) - ks;
+}
+
+// set_dispatchable_capacity! (src/replicas.jl:412) for every replica
+static void follow_disp(Ctx &c, const vector<double> &kold, const vector<double> &knew) {
+    const Model &m = c.m;
+    for (int j = 0; j < m.D; ++j) {
+        int u = m.disp[j];
+        double kc0 = clampd(kold[u], m.ulo[u], m.uhi[u]), kc1 = clampd(knew[u], m.ulo[u], m.uhi[u]);
+        double sc = kc0 == kc1 ? 1.0 : kc0 / kc1;  // kc_ratio (src/local.jl:2119)
+        if (sc == 1.0) continue;
+        for (int t = 0; t < m.T; ++t)
+            for (int rep = 0; rep < c.o.R; ++rep) {
+                double &y = c.g[ix(c, j, t, rep)];
+                y = y + y * (sc - 1);
+            }
+    }
+}
+
+// kop_prepare / kop_term / kop_eval(commit) (src/kop.jl:79-160, :223) for one unit, one replica;
+// c.k[u] still holds the raw k0, the caller sets the new capacity afterwards
+static void kop_unit(Ctx &c, int u, double k1, int rep, bool follow) {
+    const Model &m = c.m;
+    int T = m.T, n = m.ubus[u];
+    double k0raw = c.k[u];
+    double kc0 = clampd(k0raw, m.ulo[u], m.uhi[u]);
+    double dt = m.dt;
+    for (int t = 0; t < T; ++t) {
+        double jinj;
+        if (m.ukind[u] == ESM_UNIT_REN) {
+            jinj = avail_map(wraw(c, m.useries[u], t, rep));
+        } else {
+            int sj = m.stor_of_unit[u];
+            double pc, mcx;
+            soc_power(m, u, dt, clampd(c.e[ix(c, sj, t, rep)], 0.0, 1.0), clampd(c.e[ix(c, sj, (t + 1) % T, rep)], 0.0, 1.0),
+                      &pc, &mcx);
+            jinj = mcx - pc;
+        }
+        double Pt = 0.0, Qs = 0.0;
+        int nu = 0;
+        for (int q = m.up[n]; q < m.up[n + 1]; ++q) {
+            int j = m.ua[q];
+            double kap = kappa_unit(c, j);
+            if (!(fabs(kap) >= c.o.kmin)) continue;
+            double om = c.g[ix(c, j, t, rep)];
+            Pt += kap * om;
+            Qs += kap * clampd(om, 0.0, 1.0);
+            nu += 1;
+        }
+        double kc1 = clampd(k1, m.ulo[u], m.uhi[u]);
+        double dkc = kc1 - kc0;
+        double dinj = jinj * dkc;
+        double dS = -dinj;
+        // below kmin the capacity moves alone (src/replicas.jl:461): the residual takes the change
+        if (follow && !(nu == 0 || fabs(Pt) < 1e-6)) {
+            double Q = c.r[ix(c, n, t, rep)] + Qs;
+            double e = Pt - std::max(Q, 0.0);
+            double P1 = std::max(Q - dinj, 0.0) + e;
+            for (int q = m.up[n]; q < m.up[n + 1]; ++q) {
+                int j = m.ua[q];
+                double kap = kappa_unit(c, j);
+                if (!(fabs(kap) >= c.o.kmin)) continue;
+                double y0 = c.g[ix(c, j, t, rep)];
+                double sigma = kap * y0 / Pt;
+                double y1 = sigma * P1 / kap;
+                dS -= kap * (clampd(y1, 0.0, 1.0) - clampd(y0, 0.0, 1.0));
+                c.g[ix(c, j, t, rep)] = y1;
+            }
+        }
+        c.r[ix(c, n, t, rep)] += dS;
+    }
+}
+
+static void langevin_step(Ctx &c, const double *w, const double *eta, const double *kappa_s, double kmin, double clip,
+                          int box, const double *xi, int64_t it, double *knew_out, int *nclip_out, int nthreads) {
+    const Model &m = c.m;
+    int K = m.K, R = c.o.R;
+    const vector<double> &sk = c.sk_last, &fk = c.fk_last;
+    double ratio = m.beta_k / m.beta_v;
+    vector<double> knew = c.k;
+    int nclip = 0;
+    int ngroups = 0;
+    for (int u = 0; u < K; ++u) ngroups = std::max(ngroups, m.ugroup[u] + 1);
+    for (int gidx = 0; gidx < ngroups; ++gidx) {
+        if (eta[gidx] == 0) continue;
+        int jj = 0;
+        for (int u = 0; u < K; ++u) {
+            if (m.ugroup[u] != gidx) continue;
+            double sbar = 0.0;
+            for (int rep = 0; rep < R; ++rep) sbar += w[rep] * sk[(size_t)rep * K + u];
+            double g = -fk[u] + ratio * sbar;
+            double x = xi ? xi[u] : orc_normal(c.o.seed, ESM_TAG_LGV, (uint32_t)jj, (uint32_t)gidx, (uint32_t)it, 0);
+            knew[u] = langevin_one(c.k[u], g, x, eta[gidx], kappa_s[gidx], kmin, clip, box != 0, m.uhi[u], &nclip);
+            ++jj;
+        }
+    }
+    // follow_capacities! (src/replicas.jl:448)
+    vector<double> kold = c.k;
+    follow_disp(c, kold, knew);
+    for (int u = 0; u < K; ++u)
+        if (m.ukind[u] == ESM_UNIT_DISP) c.k[u] = knew[u];
+    rebuild(c, nthreads);
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int rep = 0; rep < R; ++rep)
+        for (int u = 0; u < K; ++u) {
+            if (m.ukind[u] == ESM_UNIT_DISP) continue;
+            if (kold[u] >= kmin)
+                kop_unit(c, u, kold[u] * exp(log(knew[u] / kold[u])), rep, true);
+            else
+                kop_unit(c, u, knew[u], rep, false);
+        }
+    for (int u = 0; u < K; ++u) {
+        if (m.ukind[u] == ESM_UNIT_DISP) continue;
+        c.k[u] = kold[u] >= kmin ? kold[u] * exp(log(knew[u] / kold[u])) : knew[u];
+    }
+    rebuild(c, nthreads);
+    if (knew_out)
+        for (int u = 0; u < K; ++u) knew_out[u] = c.k[u];
+    if (nclip_out) *nclip_out = nclip;
+}
+
+}  // namespace
+
+// ============================================================================================
+// C entry points of the oracle (ctypes)
+// ============================================================================================
+extern "C" {
+
+double orc_logseg(double L, double x) { return logseg(L, x); }
+double orc_trexp_offset(double u, double g, double L) { return trexp_offset(u, g, L); }
+void orc_philox4(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t *out) {
+    orc_philox(k0, k1, c0, c1, c2, c3, out);
+}
+double orc_normal_at(uint64_t seed, uint32_t tag, uint32_t j, uint32_t c1, uint32_t c2, uint32_t c3) {
+    return orc_normal(seed, tag, j, c1, c2, c3);
+}
+
+// langevin_update (src/replicas.jl:368) on one field
+int orc_langevin_update(int n, const double *k, const double *g, const double *xi, double eta, double ks, double kmin,
+                        double clip, const double *hi, double *out) {
+    int nclip = 0;
+    for (int i = 0; i < n; ++i)
+        out[i] = langevin_one(k[i], g[i], xi[i], eta, ks, kmin, clip, hi != nullptr, hi ? hi[i] : 0.0, &nclip);
+    return nclip;
+}
+
+void *orc_create(const esm_model *em, const esm_opts *eo) {
+    Ctx *c = new Ctx();
+    Model &m = c->m;
+    m.N = em->N;
+    m.L = em->L;
+    m.T = em->T;
+    m.K = em->K;
+    m.D = em->D;
+    m.S = em->S;
+    m.n0 = em->n0;
+    m.nreg = em->nreg;
+    m.nfields = em->nfields;
+    m.nlev = em->nlev;
+    m.dt = em->dt;
+    m.c_shed = em->c_shed;
+    m.c_dump = em->c_dump;
+    m.c_viol = em->c_viol;
+    m.gamma_k = em->gamma_k;
+    m.kappa0 = em->kappa0;
+    m.beta_v = em->beta_v;
+    m.beta_k = em->beta_k;
+    m.physical = em->physical != 0;
+    int N = m.N, L = m.L, K = m.K;
+    m.bus0 = cp_(em->bus0, L);
+    m.bus1 = cp_(em->bus1, L);
+    m.lb = cp_(em->line_b, L);
+    m.ls = cp_(em->line_s, L);
+    m.ukind = cp_(em->unit_kind, K);
+    m.ugroup = cp_(em->unit_group, K);
+    m.ubus = cp_(em->unit_bus, K);
+    m.useries = cp_(em->unit_series, K);
+    m.umc = cp_(em->unit_mc, K);
+    m.ucapex = cp_(em->unit_capex, K);
+    m.ulo = cp_(em->unit_lo, K);
+    m.uhi = cp_(em->unit_hi, K);
+    m.uavail = cp_(em->unit_avail, K);
+    m.uhours = cp_(em->unit_hours, K);
+    m.uetain = cp_(em->unit_eta_in, K);
+    m.uetaout = cp_(em->unit_eta_out, K);
+    m.uqt = cp_(em->unit_qt, K);
+    m.disp = cp_(em->disp, m.D);
+    m.stor = cp_(em->stor, m.S);
+    m.sfield = cp_(em->series_field, m.n0);
+    m.snode = cp_(em->series_node, m.n0);
+    m.xbar = cp_(em->xbar, (size_t)m.n0 * m.T);
+    m.wscale = cp_(em->wscale, m.n0);
+    m.Ptr = cp_(em->Ptr, (size_t)m.nreg * m.nreg);
+    m.pi0 = cp_(em->pi0, m.nreg);
+    m.phi = cp_(em->phi, (size_t)m.nreg * m.n0);
+    m.mu = cp_(em->mu, (size_t)m.nreg * m.n0 * 3);
+    m.sig = cp_(em->sig, (size_t)m.nreg * m.n0);
+    m.sig0 = cp_(em->sig0, m.n0);
+    m.frole = cp_(em->field_role, m.nfields);
+    m.fap = cp_(em->field_atom_ptr, m.nfields + 1);
+    int natoms = m.fap[m.nfields];
+    m.ap = cp_(em->atom_ptr, natoms + 1);
+    m.ai = cp_(em->atom_idx, m.ap[natoms]);
+    m.av = cp_(em->atom_val, m.ap[natoms]);
+    m.nlp = cp_(em->nodelines_ptr, N + 1);
+    m.nl = cp_(em->nodelines, m.nlp[N]);
+    m.up = cp_(em->units_ptr, N + 1);
+    m.ua = cp_(em->units_at, m.up[N]);
+    m.sp = cp_(em->stor_ptr, N + 1);
+    m.sa = cp_(em->stor_at, m.sp[N]);
+    m.qcum = cp_(em->qcum, m.nlev);
+    m.clp = cp_(em->cell_level_ptr, m.nlev + 1);
+    int ncell = m.clp[m.nlev];
+    m.cp = cp_(em->cell_ptr, ncell + 1);
+    m.cu = cp_(em->cell_units, m.cp[ncell]);
+    m.xpp = cp_(em->xpart_ptr, N + 1);
+    int npair = m.xpp[N];
+    m.xp = cp_(em->xpart, npair);
+    m.xnp = cp_(em->xnod_ptr, npair + 1);
+    m.xn = cp_(em->xnod, m.xnp[npair]);
+    m.xv = cp_(em->xval, m.xnp[npair]);
+    m.xlp = cp_(em->xlk_ptr, npair + 1);
+    m.xln = cp_(em->xlkn, m.xlp[npair]);
+    m.xlg = cp_(em->xlkg, m.xlp[npair]);
+    m.Z = cp_(em->reroute, (size_t)N * N);
+    m.comp = cp_(em->comp, N);
+    m.theta_nnz.assign(N, 0);
+    for (int f = 0; f < m.nfields; ++f) {
+        if (m.frole[f] != ESM_ROLE_THETA) continue;
+        for (int a = m.fap[f]; a < m.fap[f + 1]; ++a)
+            for (int q = m.ap[a]; q < m.ap[a + 1]; ++q) m.theta_nnz[m.ai[q]] += 1;
+    }
+    m.disp_of_unit.assign(K, -1);
+    m.stor_of_unit.assign(K, -1);
+    for (int j = 0; j < m.D; ++j) m.disp_of_unit[m.disp[j]] = j;
+    for (int j = 0; j < m.S; ++j) m.stor_of_unit[m.stor[j]] = j;
+    Opts &o = c->o;
+    o.R = eo->R;
+    o.max_points = eo->max_points;
+    o.span = eo->span;
+    o.seed = eo->seed;
+    o.extra = eo->extra;
+    o.maxnats = eo->maxnats;
+    o.kmin = eo->kappa_min;
+    for (int q = 0; q < ESM_NFAM; ++q) o.rates[q] = eo->family_rates[q];
+    size_t TR = (size_t)m.T * o.R;
+    c->theta.assign(N * TR, 0.0);
+    c->g.assign(m.D * TR, 0.0);
+    c->e.assign(m.S * TR, 0.0);
+    c->z.assign(m.n0 * TR, 0.0);
+    c->reg.assign(TR, 0);
+    c->k.assign(K, 0.0);
+    c->r.assign(N * TR, 0.0);
+    c->F.assign(L * TR, 0.0);
+    return c;
+}
+
+void orc_destroy(void *p) { delete (Ctx *)p; }
+
+void orc_set_state(void *p, const double *theta, const double *g, const double *e, const double *z, const int32_t *reg,
+                   const double *k) {
+    Ctx *c = (Ctx *)p;
+    if (theta) std::copy(theta, theta + c->theta.size(), c->theta.begin());
+    if (g) std::copy(g, g + c->g.size(), c->g.begin());
+    if (e) std::copy(e, e + c->e.size(), c->e.begin());
+    if (z) std::copy(z, z + c->z.size(), c->z.begin());
+    if (reg) std::copy(reg, reg + c->reg.size(), c->reg.begin());
+    if (k) std::copy(k, k + c->k.size(), c->k.begin());
+}
+
+void orc_get_state(void *p, double *theta, double *g, double *e, double *z, int32_t *reg, double *k) {
+    Ctx *c = (Ctx *)p;
+    if (theta) std::copy(c->theta.begin(), c->theta.end(), theta);
+    if (g) std::copy(c->g.begin(), c->g.end(), g);
+    if (e) std::copy(c->e.begin(), c->e.end(), e);
+    if (z) std::copy(c->z.begin(), c->z.end(), z);
+    if (reg) std::copy(c->reg.begin(), c->reg.end(), reg);
+    if (k) std::copy(c->k.begin(), c->k.end(), k);
+}
+
+void orc_rebuild(void *p, int nthreads) { rebuild(*(Ctx *)p, nthreads); }
+
+void orc_get_caches(void *p, double *r, double *F) {
+    Ctx *c = (Ctx *)p;
+    if (r) std::copy(c->r.begin(), c->r.end(), r);
+    if (F) std::copy(c->F.begin(), c->F.end(), F);
+}
+
+void orc_set_caches(void *p, const double *r, const double *F) {
+    Ctx *c = (Ctx *)p;
+    if (r) std::copy(r, r + c->r.size(), c->r.begin());
+    if (F) std::copy(F, F + c->F.size(), c->F.begin());
+}
+
+// one class of one sweep (caches must be current)
+void orc_class_pass(void *p, int64_t sweep, int cls, int64_t *stats, int nthreads) {
+    class_pass(*(Ctx *)p, (uint32_t)sweep, cls, stats, nthreads);
+}
+
+// n sweeps: caches rebuilt at each sweep start (LocalCost, src/local.jl:1940), classes in the
+// sweep's order
+void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
+    Ctx *c = (Ctx *)p;
+    for (int s = 0; s < n; ++s) {
+        uint32_t sw = (uint32_t)(sweep0 + s);
+        rebuild(*c, nthreads);
+        int order[3], ncls;
+        class_order(*c, sw, order, &ncls);
+        for (int q = 0; q < ncls; ++q) class_pass(*c, sw, order[q], stats, nthreads);
+    }
+}
+
+void orc_class_order(void *p, int64_t sweep, int *order, int *ncls) {
+    class_order(*(Ctx *)p, (uint32_t)sweep, order, ncls);
+}
+
+void orc_scores(void *p, double *sk, double *fk, double *parts, int nthreads) {
+    Ctx *c = (Ctx *)p;
+    c->sk_last.assign((size_t)c->o.R * c->m.K, 0.0);
+    c->fk_last.assign(c->m.K, 0.0);
+    scores(*c, c->sk_last.data(), c->fk_last.data(), parts, nthreads);
+    c->has_scores = true;
+    if (sk) std::copy(c->sk_last.begin(), c->sk_last.end(), sk);
+    if (fk) std::copy(c->fk_last.begin(), c->fk_last.end(), fk);
+}
+
+int orc_langevin_step(void *p, const double *w, const double *eta, const double *kappa_s, double kmin, double clip,
+                      int box, const double *xi, int64_t it, double *knew_out, int *nclip_out, int nthreads) {
+    if (!((Ctx *)p)->has_scores) return -5;
+    langevin_step(*(Ctx *)p, w, eta, kappa_s, kmin, clip, box, xi, it, knew_out, nclip_out, nthreads);
+    ((Ctx *)p)->has_scores = false;
+    return 0;
+}
+
+}  // extern "C"

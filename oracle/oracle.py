@@ -1,0 +1,179 @@
+"""ctypes wrapper of the CPU oracle (``oracle/_build/liboracle_esm.so``) -- TEST INFRASTRUCTURE.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it, as the
+checker of the CUDA path; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle_esm.so")
+
+P_f64 = C.POINTER(C.c_double)
+P_i32 = C.POINTER(C.c_int32)
+P_i64 = C.POINTER(C.c_int64)
+NSTAT = 2 * (9 + 1) + 1
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc, no other dependency)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.orc_logseg.restype = C.c_double
+        L.orc_logseg.argtypes = [C.c_double, C.c_double]
+        L.orc_trexp_offset.restype = C.c_double
+        L.orc_trexp_offset.argtypes = [C.c_double, C.c_double, C.c_double]
+        L.orc_philox4.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
+        L.orc_normal_at.restype = C.c_double
+        L.orc_normal_at.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_langevin_update.restype = C.c_int
+        L.orc_langevin_update.argtypes = [C.c_int, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, P_f64, P_f64]
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_set_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
+        L.orc_get_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
+        L.orc_rebuild.argtypes = [C.c_void_p, C.c_int]
+        L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
+        L.orc_set_caches.argtypes = [C.c_void_p, P_f64, P_f64]
+        L.orc_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int, P_i64, C.c_int]
+        L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
+        L.orc_class_order.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32]
+        L.orc_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_int]
+        L.orc_langevin_step.restype = C.c_int
+        L.orc_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int, P_f64,
+                                        C.c_int64, P_f64, P_i32, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=P_f64):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def logseg(L, x):
+    return lib().orc_logseg(L, x)
+
+
+def trexp_offset(u, g, L):
+    return lib().orc_trexp_offset(u, g, L)
+
+
+def philox4(k0, k1, c0, c1, c2, c3):
+    out = (C.c_uint32 * 4)()
+    lib().orc_philox4(k0, k1, c0, c1, c2, c3, out)
+    return list(out)
+
+
+def langevin_update(k, g, xi, eta, ks, kmin=1.0, clip=np.inf, hi=None):
+    k, g, xi = (np.ascontiguousarray(x, dtype=np.float64) for x in (k, g, xi))
+    out = np.zeros_like(k)
+    hi = None if hi is None else np.ascontiguousarray(hi, dtype=np.float64)
+    nc = lib().orc_langevin_update(len(k), _p(k), _p(g), _p(xi), eta, ks, kmin, clip, _p(hi), _p(out))
+    return out, nc
+
+
+class Oracle:
+    """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
+
+    def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=96, span=0,
+                 threads=None):
+        import sys
+        sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
+        from esmgb.cabi import ModelBuffers, make_opts
+        self.m = model
+        self.R = R
+        self.buf = ModelBuffers(model)
+        self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span)
+        self.threads = threads or os.cpu_count() or 1
+        self.h = lib().orc_create(C.byref(self.buf.struct), C.byref(self.opts))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def shapes(self):
+        m, R = self.m, self.R
+        return {"theta": (m.N, m.T, R), "g": (m.D, m.T, R), "e": (m.S, m.T, R), "z": (m.n0, m.T, R),
+                "reg": (m.T, R), "k": (m.Kunits,)}
+
+    def set_state(self, st):
+        arr = {k: np.ascontiguousarray(getattr(st, k), dtype=np.int32 if k == "reg" else np.float64)
+               for k in ("theta", "g", "e", "z", "reg", "k")}
+        self._in = arr
+        lib().orc_set_state(self.h, _p(arr["theta"]), _p(arr["g"]), _p(arr["e"]), _p(arr["z"]),
+                            _p(arr["reg"], P_i32), _p(arr["k"]))
+
+    def get_state(self):
+        sh = self.shapes()
+        out = {k: np.zeros(s, dtype=np.int32 if k == "reg" else np.float64) for k, s in sh.items()}
+        lib().orc_get_state(self.h, _p(out["theta"]), _p(out["g"]), _p(out["e"]), _p(out["z"]),
+                            _p(out["reg"], P_i32), _p(out["k"]))
+        return out
+
+    def rebuild(self):
+        lib().orc_rebuild(self.h, self.threads)
+
+    def caches(self):
+        m, R = self.m, self.R
+        r = np.zeros((m.N, m.T, R))
+        F = np.zeros((m.L, m.T, R))
+        lib().orc_get_caches(self.h, _p(r), _p(F))
+        return r, F
+
+    def set_caches(self, r, F):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        lib().orc_set_caches(self.h, _p(r), _p(F))
+
+    def class_pass(self, sweep, cls):
+        st = np.zeros(NSTAT, np.int64)
+        lib().orc_class_pass(self.h, sweep, cls, _p(st, P_i64), self.threads)
+        return st
+
+    def sweeps(self, n, sweep0=0):
+        st = np.zeros(NSTAT, np.int64)
+        lib().orc_sweeps(self.h, n, sweep0, _p(st, P_i64), self.threads)
+        return st
+
+    def class_order(self, sweep):
+        o = np.zeros(3, np.int32)
+        n = np.zeros(1, np.int32)
+        lib().orc_class_order(self.h, sweep, _p(o, P_i32), _p(n, P_i32))
+        return list(o[: n[0]])
+
+    def scores(self):
+        m, R = self.m, self.R
+        sk = np.zeros((R, m.Kunits))
+        fk = np.zeros(m.Kunits)
+        parts = np.zeros((R, 8))
+        lib().orc_scores(self.h, _p(sk), _p(fk), _p(parts), self.threads)
+        return sk, fk, parts
+
+    def langevin_step(self, w, eta, kappa_s, kmin=1.0, clip=0.02, box=True, xi=None, it=0):
+        w, eta, kappa_s = (np.ascontiguousarray(x, dtype=np.float64) for x in (w, eta, kappa_s))
+        xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+        knew = np.zeros(self.m.Kunits)
+        nclip = np.zeros(1, np.int32)
+        rc = lib().orc_langevin_step(self.h, _p(w), _p(eta), _p(kappa_s), kmin, clip, int(box), _p(xi), it,
+                                     _p(knew), _p(nclip, P_i32), self.threads)
+        if rc != 0:
+            raise RuntimeError(f"oracle langevin_step: status {rc}")
+        return knew, int(nclip[0])

@@ -1,0 +1,158 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle on identical states and the same
+Philox streams (the reference's device verification protocol: same prepared moves, same random
+numbers, compared exactly or to round-off; docs/system/testing.md).
+
+Tolerances: FP64 kernels against the FP64 oracle 1e-9 relative per element, at most 1 % of
+(step, replica) tasks allowed to differ beyond it (discrete flips at a segment boundary from
+last-bit differences of the transcendental functions); FP32 kernels 2e-3 relative (4e-3 absolute on
+utilisations), at most 5 % of tasks flipped. Scores: FP64 1e-9 relative, FP32 5e-3 relative of the
+score scale."""
+import numpy as np
+import pytest
+
+from esmgb.device import DeviceChain
+from esmgb.model import make_model, initial_state
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b, scale):
+    return np.abs(a - b) / (scale + np.abs(b))
+
+
+def task_flips(sd, so, m, tol_rel, tol_abs):
+    """Fraction of (step, replica) entries whose state differs beyond tolerance, and the largest
+    difference among the others."""
+    bad = np.zeros((m.T, so["g"].shape[2]), bool)
+    th = _rel(sd["theta"], so["theta"], 1.0 + np.abs(so["theta"]).max()).max(0)
+    gg = np.abs(sd["g"] - so["g"]).max(0)
+    ee = np.abs(sd["e"] - so["e"]).max(0)
+    bad |= th > tol_rel
+    bad |= gg > tol_abs
+    bad |= ee > tol_abs
+    worst = max(th[~bad].max(initial=0), gg[~bad].max(initial=0), ee[~bad].max(initial=0))
+    return bad.mean(), worst
+
+
+def make(N=40, L=60, T=40, R=32, seed=11):
+    m = make_model(N, L, T, seed=seed)
+    st = initial_state(m, R, seed=3)
+    return m, st
+
+
+@pytest.fixture(scope="module")
+def base():
+    return make()
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_rebuild_caches(base, prec):
+    m, st = base
+    d = DeviceChain(m, 32, precision=prec, seed=5)
+    d.upload(st)
+    d.rebuild()
+    r, F = d.caches()
+    o = Oracle(m, 32, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    r0, F0 = o.caches()
+    tol = 1e-12 if prec == 64 else 2e-6
+    assert np.abs(r - r0).max() <= tol * (1 + np.abs(r0).max())
+    assert np.abs(F - F0).max() <= tol * (1 + np.abs(F0).max())
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_class_pass(base, prec):
+    m, st = base
+    d = DeviceChain(m, 32, precision=prec, seed=5)
+    d.upload(st)
+    d.rebuild()
+    o = Oracle(m, 32, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    sd = d.class_pass(3, 0)
+    so = o.class_pass(3, 0)
+    assert np.array_equal(sd[:20:2], so[:20:2])           # the same moves were tried
+    assert sd[-1] == so[-1] == 0                          # no guard events
+    a, b = d.download(), o.get_state()
+    frac, worst = task_flips(a, b, m, 1e-9 if prec == 64 else 2e-3, 1e-9 if prec == 64 else 4e-3)
+    print(f"precision {prec}: flipped tasks {frac:.4f}, worst other {worst:.2e}")
+    assert frac <= (0.01 if prec == 64 else 0.05)
+
+
+def test_sweeps_fp64_odd_T_small_R():
+    m, st = make(T=73, R=4)                               # three colour classes; 8 steps per warp
+    d = DeviceChain(m, 4, precision=64, seed=9)
+    d.upload(st)
+    o = Oracle(m, 4, seed=9)
+    o.set_state(st)
+    sd = d.sweeps(2, 10)
+    so = o.sweeps(2, 10)
+    assert np.array_equal(sd[:20:2], so[:20:2])
+    frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
+    print(f"odd T: flipped {frac:.4f}, worst {worst:.2e}")
+    assert frac <= 0.02
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_capacity_scores(base, prec):
+    m, st = base
+    d = DeviceChain(m, 32, precision=prec, seed=5)
+    d.upload(st)
+    d.sweeps(1, 0)
+    o = Oracle(m, 32, seed=5)
+    o.set_state(d.download())
+    sk, fk, parts = d.scores()
+    sk0, fk0, parts0 = o.scores()
+    scale = np.abs(sk0).max(axis=0) + 1e-3
+    tol = 1e-9 if prec == 64 else 5e-3
+    assert (np.abs(sk - sk0) / scale).max() < tol
+    np.testing.assert_allclose(fk, fk0, rtol=1e-14)
+    np.testing.assert_allclose(parts[:, :7], parts0[:, :7], rtol=1e-9 if prec == 64 else 1e-4, atol=1e-6)
+
+
+def test_langevin_step_fp64(base):
+    m, st = base
+    R = 32
+    d = DeviceChain(m, R, precision=64, seed=5)
+    d.upload(st)
+    d.sweeps(1, 0)
+    o = Oracle(m, R, seed=5)
+    o.set_state(d.download())
+    d.scores()
+    o.scores()
+    rng = np.random.Generator(np.random.PCG64(4))
+    xi = rng.standard_normal(m.Kunits)
+    w = np.full(R, 1.0 / R)
+    ng = len(m.carriers)
+    eta = np.full(ng, 5e-4)
+    ks = np.array([500.0, 200.0, 1000.0, 300.0, 100.0, 100.0])
+    kd, ncd = d.langevin_step(w, eta, ks, 1.0, 0.02, True, xi, 1)
+    ko, nco = o.langevin_step(w, eta, ks, 1.0, 0.02, True, xi, 1)
+    np.testing.assert_allclose(kd, ko, rtol=1e-12)
+    assert ncd == nco
+    a, b = d.download(), o.get_state()
+    assert np.abs(a["g"] - b["g"]).max() < 1e-9
+    r, _ = d.caches()
+    o.rebuild()
+    r0, _ = o.caches()
+    assert np.abs(r - r0).max() < 1e-6
+
+
+def test_langevin_stream_normals(base):
+    """Without injected normals the device draws them from its Philox stream; the oracle replays it."""
+    m, st = base
+    R = 32
+    d = DeviceChain(m, R, precision=64, seed=5)
+    d.upload(st)
+    o = Oracle(m, R, seed=5)
+    o.set_state(st)
+    d.scores()
+    o.scores()
+    w = np.full(R, 1.0 / R)
+    eta = np.full(len(m.carriers), 5e-4)
+    ks = np.full(len(m.carriers), 300.0)
+    kd, _ = d.langevin_step(w, eta, ks, it=7)
+    ko, _ = o.langevin_step(w, eta, ks, it=7)
+    np.testing.assert_allclose(kd, ko, rtol=1e-12)

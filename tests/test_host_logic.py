@@ -1,0 +1,71 @@
+"""Host logic of the replica sampler against the reference's known answers
+(test/test_replicas.jl:17-60) and the convergence diagnostics (test/test_convergence.jl)."""
+import math
+
+import numpy as np
+import pytest
+
+from esmgb import replicas as RP
+from esmgb import convergence as CV
+
+
+def test_schedule_gate_weights_adaptation():
+    ctl = RP.ReplicaCtl(M=4, burst_every=8, phi=0.3, gate_min=2, gate_max=5, gate_win=4, gate_tol=0.1,
+                        eta_w=[1e-3, 1e-3], kappa_s=[100.0, 100.0], probe_avg=2)
+    assert [[it for it in range(1, 17) if RP.weather_schedule(ctl, it, j)[1]] for j in range(1, 5)] == \
+        [[8, 16], [6, 14], [4, 12], [2, 10]]
+    assert RP.weather_schedule(ctl, 8, 1) == (0.3, True) and RP.weather_schedule(ctl, 7, 1) == (0.0, False)
+    ctl.theta = 0.1
+    assert math.isclose(RP.weather_schedule(ctl, 8, 1)[0], math.acos(math.cos(0.1) * math.cos(0.3)))
+    assert RP.weather_schedule(ctl, 7, 1)[0] == 0.1
+    ctl.theta = 0.0
+    p = [0.2, 0.0, 0.5, 0.3]
+    assert [RP.categorical(p, u) for u in (0.0, 0.1, 0.2, 0.2000001, 0.7, 0.70001, 1.0)] == [1, 1, 1, 3, 3, 4, 4]
+    assert RP.relaxation_indicator([[1.0, 2.0]], 4) == math.inf
+    assert math.isclose(RP.relaxation_indicator([[1.0, 2.0], [1.0, 2.0], [1.5, 2.0], [1.5, 2.2]], 4), 0.5)
+    R = RP.ReplicaSet(M=1, eta_w=ctl.eta_w, since=[0], window=[False], active=[False])
+    ctl.gate_max = 10
+    acts = []
+    for g in ([5.0, 1.0], [2.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0]):
+        acts.append(RP.update_gate(R, 0, g, ctl))
+        R.since[0] += 1
+    assert acts == [False, False, False, False, False, True, True]
+    ctl.gate_max = 5
+    R.since[0] = 0
+    R.active[0] = False
+    R.gbuf[0].clear()
+    acts = []
+    for it in range(1, 8):
+        acts.append(RP.update_gate(R, 0, [float(it), 0.0], ctl))
+        R.since[0] += 1
+    assert acts == [False, False, False, False, False, True, True]
+    Phis = [0.7, -1.3, 0.2, 2.1]
+    act = [True, False, True, True]
+    assert list(RP.tilt_weights(0.0, Phis, act)) == list(RP.uniform_weights(act)) == [1 / 3, 0.0, 1 / 3, 1 / 3]
+    w = RP.tilt_weights(2.0, Phis, act)
+    assert math.isclose(w.sum(), 1) and w[1] == 0 and math.isclose(w[3] / w[0], math.exp(2 * (2.1 - 0.7)))
+    assert list(RP.uniform_weights([False] * 4)) == [0.25] * 4
+    R.eta_w = [1e-3, 1e-3]
+    assert not RP.adapt_step(R, [0.5, 0.01], ctl)
+    assert RP.adapt_step(R, [-0.1, 0.03], ctl)
+    np.testing.assert_allclose(R.eta_w, [0.7e-3, 1.2e-3]) and not R.gaps
+
+
+def test_convergence_diagnostics():
+    rng = np.random.Generator(np.random.PCG64(1))
+
+    def ar(n, phi):
+        x = np.zeros(n)
+        x[0] = rng.standard_normal() / math.sqrt(1 - phi ** 2)
+        e = rng.standard_normal(n)
+        for t in range(1, n):
+            x[t] = phi * x[t - 1] + e[t]
+        return x
+    iid = [rng.standard_normal(1000) for _ in range(4)]
+    assert CV.rhat_rank(iid) < 1.01 and 3000 < CV.ess_bulk(iid) < 5000
+    a9 = [ar(2000, 0.9) for _ in range(4)]
+    assert 250 < CV.ess_bulk(a9) < 700
+    assert CV.rhat_rank([rng.standard_normal(1000) + (0.5 if k == 0 else 0.0) for k in range(4)]) > 1.01
+    assert CV.rhat_rank([rng.standard_normal(1000) * (2.0 if k == 0 else 1.0) for k in range(4)]) > 1.01
+    rw = [np.cumsum(rng.standard_normal(1000)) for _ in range(4)]
+    assert CV.rhat_rank(rw) > 1.01 or CV.ess_bulk(rw) < 400
