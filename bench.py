@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Replica-sampler step throughput on GB300 (the hot path of ESM-Sampling's `sampler = "replicas"`).
+
+A step is one replica step of one chain (replica_step!, src/replicas.jl:676): the scheduled weather
+bursts with their compensated re-initialisation, one operation sweep (local_sweep!, plain families)
+of every replica, the capacity scores, the replica-averaged Langevin step of the shared capacities
+and the dispatch following. Workload: 40 nodes, 60 lines, hourly T = 8760, 64 weather replicas
+(the "plain method on GPU" configuration), synthetic seeded data.
+
+  value  device throughput: sweeps of all replicas per second from CUDA-event spans on the
+         library's stream (inputs resident in HBM; every input is larger than L2)
+  e2e    the same metric through the public API with host buffers: the host-driven replica loop
+         (gate, weights, schedule) calling the C ABI, host<->device copies of every step included
+  --impl reference: the CPU restatement of the reference algorithm (the reference itself is Julia
+         and cannot run here) on all host cores, on a bounded sample of the same workload
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "esm-sampling_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(N=40, L=60, T=8760, R=64, seed=1234)
+METRIC = "local-move sweeps/s"
+UNIT = "sweeps/s"
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        rows = [r for r in self.rows if len(r) >= 9 and (r[0] == dev or len(set(x[0] for x in self.rows)) == 1)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def setup_chain(precision=32):
+    from esmgb.device import DeviceChain
+    from esmgb.model import initial_state, make_model
+    w = WORKLOAD
+    m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
+    st = initial_state(m, w["R"], seed=7)
+    d = DeviceChain(m, w["R"], precision=precision, seed=w["seed"])
+    d.upload(st)
+    return m, st, d
+
+
+def schedule(ctl, it, R, rng):
+    """Weather bursts of the step (weather_schedule / replica_weather!, src/replicas.jl:571-606)."""
+    from esmgb.replicas import weather_schedule, window_bounds
+    moved = np.zeros(R, np.int32)
+    theta = np.zeros(R)
+    window = np.zeros(R, np.int32)
+    wstart = np.ones(R, np.int32)
+    bursts = np.zeros(R, bool)
+    for j in range(R):
+        th, burst = weather_schedule(ctl, it, j + 1)
+        regime = (burst or ctl.burst_every == 0) and ctl.window > 0
+        win = regime and rng.random() < ctl.window_prob
+        theta[j] = th
+        bursts[j] = burst
+        if th > 0 or win:
+            moved[j] = 1
+        if win:
+            window[j] = ctl.window
+            wstart[j] = window_bounds(WORKLOAD["T"], ctl.window, rng.random())[0]
+    return moved, theta, window, wstart, bursts
+
+
+def carrier_params(m):
+    from esmgb.model import LANGEVIN_KAPPA
+    eta = np.full(len(m.carriers), 5e-4)             # langevin_eta (src/run.jl:105)
+    ks = np.array([LANGEVIN_KAPPA.get(c, 100.0) for c in m.carriers])
+    return eta, ks
+
+
+def device_loop(d, m, ctl, it0, n, rng, pre):
+    """The device-resident step: everything on the GPU, host arrays only for the schedule."""
+    eta, ks = carrier_params(m)
+    w = np.full(d.R, 1.0 / d.R)
+    for q in range(n):
+        it = it0 + q
+        moved, theta, window, wstart, _ = pre[q] if pre else schedule(ctl, it, d.R, rng)
+        if moved.any():
+            d.weather_step(moved, theta, window, wstart, it=it)
+        d.sweeps(1, sweep0=it, stats=False)
+        d.scores()
+        d.langevin_step(w, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
+
+
+def e2e_loop(d, m, ctl, R_set, it0, n, rng):
+    """The host-driven replica loop (replica_step!, src/replicas.jl:676-704) through the C ABI."""
+    from esmgb import replicas as RP
+    eta, ks = carrier_params(m)
+    ratio = m.beta_k / m.beta_v
+    h2d = d2h = 0
+    for q in range(n):
+        it = it0 + q
+        moved, theta, window, wstart, bursts = schedule(ctl, it, d.R, rng)
+        for j in range(d.R):
+            if bursts[j]:
+                R_set.since[j], R_set.window[j], R_set.active[j] = 0, bool(window[j] > 0), False
+                R_set.gbuf[j].clear()
+            else:
+                R_set.since[j] += 1
+        if moved.any():
+            d.weather_step(moved, theta, window, wstart, it=it)
+            h2d += moved.nbytes + theta.nbytes + window.nbytes + wstart.nbytes
+        d.sweeps(1, sweep0=it, stats=False)
+        sk, fk, parts = d.scores()
+        d2h += sk.nbytes + fk.nbytes + parts.nbytes
+        k = d.download_k() if hasattr(d, "download_k") else None
+        mask = RP.interior_nodes(k if k is not None else m.k0, m.unit_hi)
+        fkm = RP.masked_mean(fk, mask)
+        for j in range(d.R):
+            RP.update_gate(R_set, j, [RP.masked_mean(ratio * sk[j], mask) / fkm], ctl)
+        wts = RP.drift_weights(ctl, np.zeros(d.R), R_set.active)
+        knew, _ = d.langevin_step(wts, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
+        h2d += wts.nbytes + eta.nbytes + ks.nbytes
+        d2h += knew.nbytes
+    return h2d / n, d2h / n
+
+
+def cpu_sample(threads, sweeps=1, R=2):
+    """The oracle on the host cores: one operation sweep and the scores of R of the replicas."""
+    from esmgb.model import initial_state, make_model
+    from oracle.oracle import Oracle
+    w = WORKLOAD
+    m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
+    st = initial_state(m, R, seed=7)
+    o = Oracle(m, R, seed=w["seed"], threads=threads)
+    o.set_state(st)
+    t0 = time.perf_counter()
+    o.sweeps(sweeps, 0)
+    o.scores()
+    dt = time.perf_counter() - t0
+    return sweeps * (R / w["R"]) / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.build()
+    for _ in range(args.warmup):
+        cpu_sample(threads, 1, 1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, _ = cpu_sample(threads, 1, 1)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = args.steps / sum(1.0 / v for v in vals)
+    sample = (f"each step: one operation sweep and the capacity scores of 1 of the 64 replicas "
+              f"(T = 8760), scaled to 64 replicas")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": ("the reference is a Julia package (no Julia on this machine): its algorithm is timed through "
+                     "the FP64 C++ restatement in oracle/, OpenMP over the steps of a colour class"),
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict():
+    w = WORKLOAD
+    return {"workload": "plain replica sampler on GPU: 40 nodes, 60 lines, T=8760 hourly, 64 replicas",
+            "nodes": w["N"], "lines": w["L"], "T": w["T"], "replicas": w["R"], "chains_per_gpu": 1,
+            "l2": "inputs larger than L2 (state arrays 0.9 GB per chain)", "parallelism": "independent chains per GPU"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-replicas", type=int, default=2)
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        return run_reference(args)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    from esmgb import build as B
+    B.build()
+    from esmgb import replicas as RP
+    m, st, d = setup_chain(32)
+    R = d.R
+    ctl = RP.ReplicaCtl(M=R)
+    rng = np.random.Generator(np.random.PCG64(rank + 1))
+    # iterations placed so that the timed region contains a weather burst (every 40 steps)
+    it0 = 40 - args.warmup - args.steps // 2
+    it0 = it0 if it0 > 0 else 40 + it0 % 40
+    device_loop(d, m, ctl, it0, args.warmup, rng, None)
+    pre = [schedule(ctl, it0 + args.warmup + q, R, rng) for q in range(args.steps)]
+    d.sync(600.0)
+    if pg:
+        pg.barrier()
+    launches0 = d.launch_count()
+    d.set_timing(True)
+    clk = Clocks()
+    clk.start()
+    t0 = time.perf_counter()
+    device_loop(d, m, ctl, it0 + args.warmup, args.steps, rng, pre)
+    d.sync(600.0)
+    wall_dev = time.perf_counter() - t0
+    clocks = clk.stop()
+    kt = d.timing()
+    launches = d.launch_count() - launches0
+    dev_ms = sum(v[0] for v in kt.values())
+    if pg:
+        import torch
+        t = torch.tensor([dev_ms])
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t[0])
+        pg.barrier()
+    value = world * args.steps / (dev_ms / 1000.0)
+    # end to end through the public API, host driver included
+    Rset = RP.ReplicaSet(M=R, eta_w=[5e-4] * len(m.carriers))
+    d.sync(600.0)
+    t0 = time.perf_counter()
+    h2d, d2h = e2e_loop(d, m, ctl, Rset, it0 + args.warmup + args.steps, args.steps, rng)
+    d.sync(600.0)
+    e2e_wall = time.perf_counter() - t0
+    e2e = world * args.steps / e2e_wall
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (the line-move class pass): algorithmic bytes of one launch =
+    # the compulsory FP32 state traffic of one colour class, 4 (11 N + 2 L) (T/2) R bytes
+    N, L, T = m.N, m.L, m.T
+    cls_ms, cls_n = kt["class_pass"]
+    alg = 4 * (11 * N + 2 * L) * (T / 2) * R
+    per = cls_ms / max(cls_n, 1) / 1000.0
+    peak, kind = peaks()
+    achieved = alg / per / 1e9 if per > 0 else 0.0
+    moves = (sum(len(a.ptr) - 1 for a in m.atoms) + round(4.0 * N)) * T * R
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "linemove_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch_full")
+        except Exception:
+            traffic = None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator of the configuration)",
+            "config": config_dict(),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": kind,
+                         "kernel": "k_class_pass (line moves of one colour class)",
+                         "note": "the exact line sampler is FP32-issue-bound; the HBM bytes are the compulsory state"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "clocks": clocks,
+            "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+            "line_moves_per_s": moves * args.steps / (dev_ms / 1000.0) * world,
+            "wall_device_loop_s": wall_dev}
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import oracle as O
+            O.build()
+            threads = os.cpu_count() or 1
+            v, dt = cpu_sample(threads, 1, args.cpu_replicas)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": f"one operation sweep and the scores of {args.cpu_replicas} of the "
+                                              f"64 replicas at T = 8760 ({dt:.1f} s), scaled to 64 replicas"}
+        except Exception as e:  # the baseline is reported, never the target
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -62,14 +62,60 @@ struct esm_ctx {
     double *d_w = nullptr, *d_eta = nullptr, *d_kappa = nullptr, *d_xi = nullptr;
     int *d_nclip = nullptr;
     unsigned long long *d_stats = nullptr;
-    int32_t *d_reg = nullptr;
+    int32_t *d_reg = nullptr, *d_reg2 = nullptr;
     void *d_scratch = nullptr;
+    // weather
+    double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
+    double *d_wbeta = nullptr, *d_wtheta = nullptr, *d_wxi = nullptr;
+    int *d_moved = nullptr, *d_window = nullptr, *d_wstart = nullptr, *d_wflag = nullptr;
+    void *d_r0 = nullptr;
     // precision-dependent state pointers (aliases into Mf / Md)
     void *theta = nullptr, *g = nullptr, *e = nullptr, *r = nullptr, *F = nullptr, *z = nullptr;
     void *kc_d = nullptr, *kc_s = nullptr, *kc_r = nullptr;
+    // device timing
+    bool timing = false;
+    struct Mark {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    vector<Mark> marks;
+    vector<cudaEvent_t> pool;
+    double acc_ms[ESM_KT_N] = {0, 0, 0, 0, 0};
+    double acc_n[ESM_KT_N] = {0, 0, 0, 0, 0};
 };
 
 namespace {
+
+cudaEvent_t ev_get(esm_ctx *c) {
+    if (!c->pool.empty()) {
+        cudaEvent_t e = c->pool.back();
+        c->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// bracket the launches of one kernel family with events when timing is on
+struct Span {
+    esm_ctx *c;
+    int kind;
+    cudaEvent_t a = nullptr;
+    Span(esm_ctx *c_, int k) : c(c_), kind(k) {
+        if (c->timing) {
+            a = ev_get(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~Span() {
+        if (a) {
+            cudaEvent_t b = ev_get(c);
+            cudaEventRecord(b, c->stream);
+            c->marks.push_back({kind, a, b});
+        }
+    }
+};
 
 int fail(esm_ctx *c, int code, const char *fmt, ...) {
     char buf[512];
@@ -412,6 +458,7 @@ int down_state(esm_ctx *c, const void *src, double *h, size_t n) {
 }
 
 int rebuild_any(esm_ctx *c) {
+    Span sp(c, ESM_KT_REBUILD);
     CK(c->precision == 64 ? esm::launch_rebuild<double>(c->Md, c->stream) : esm::launch_rebuild<float>(c->Mf, c->stream));
     c->launches += 1;
     return ESM_OK;
@@ -420,6 +467,7 @@ int rebuild_any(esm_ctx *c) {
 int class_pass_any(esm_ctx *c, uint32_t sweep, int cls) {
     int ns = c->class_len[cls];
     if (ns == 0) return ESM_OK;
+    Span sp(c, ESM_KT_CLASS);
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, (double *)c->d_scratch, c->max_warps,
                                           c->d_stats, c->stream));
@@ -546,6 +594,27 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     if ((rc = dalloc(c, &c->d_nclip, 1))) return rc;
     if ((rc = dalloc(c, &c->d_stats, 2 * (ESM_NFAM + 1) + 1))) return rc;
     if ((rc = dalloc(c, &c->d_reg, (size_t)c->T * c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_reg2, (size_t)c->T * c->R))) return rc;
+    // weather prior (FP64)
+    size_t n0 = m->n0, nr = m->nreg;
+    if ((rc = upload(c, &c->d_phi, m->phi, nr * n0))) return rc;
+    if ((rc = upload(c, &c->d_mu, m->mu, nr * n0 * 3))) return rc;
+    if ((rc = upload(c, &c->d_sig, m->sig, nr * n0))) return rc;
+    if ((rc = upload(c, &c->d_sig0, m->sig0, n0))) return rc;
+    if ((rc = upload(c, &c->d_Ptr, m->Ptr, nr * nr))) return rc;
+    if ((rc = upload(c, &c->d_pi0, m->pi0, nr))) return rc;
+    if ((rc = dalloc(c, &c->d_wbeta, (size_t)c->R * nr * c->T))) return rc;
+    if ((rc = dalloc(c, &c->d_wtheta, c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_moved, c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_window, c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_wstart, c->R))) return rc;
+    if ((rc = dalloc(c, &c->d_wflag, c->R))) return rc;
+    {
+        size_t rbytes = (c->precision == 64 ? sizeof(double) : sizeof(float)) * (size_t)c->N * c->T * c->R;
+        char *q;
+        if ((rc = dalloc(c, &q, rbytes))) return rc;
+        c->d_r0 = q;
+    }
     CK(cudaStreamSynchronize(c->stream));
     return ESM_OK;
 }
@@ -553,6 +622,11 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
 int esm_destroy(esm_ctx *c) {
     if (!c) return ESM_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &mk : c->marks) {
+        cudaEventDestroy(mk.a);
+        cudaEventDestroy(mk.b);
+    }
+    for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     for (void *p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -654,6 +728,8 @@ int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
     if (rc) return rc;
     CK(cudaMemsetAsync(c->d_dk, 0, sizeof(double) * c->R * c->K, c->stream));
     CK(cudaMemsetAsync(c->d_parts, 0, sizeof(double) * c->R * 8, c->stream));
+    {
+    Span sp(c, ESM_KT_SCORE);
     if (c->precision == 64) {
         CK(esm::launch_scores<double>(c->Md, c->d_dk, c->d_parts, c->stream));
         CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
@@ -662,6 +738,7 @@ int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
         CK(esm::launch_scores<float>(c->Mf, c->d_dk, c->d_parts, c->stream));
         CK(esm::launch_score_finish<float>(c->Mf, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
                                            c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
+    }
     }
     c->launches += 2;
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * c->R * c->K, cudaMemcpyDeviceToHost, c->stream));
@@ -684,6 +761,8 @@ int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const doub
     if (xi) CK(cudaMemcpyAsync(c->d_xi, xi, sizeof(double) * K, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_nclip, 0, sizeof(int), c->stream));
     CK(cudaMemcpyAsync(c->d_kold, c->d_k, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
+    {
+    Span sp(c, ESM_KT_LANGEVIN);
     esm::k_langevin<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->R, c->d_ugroup, c->d_ugidx, c->d_kold, c->d_sk,
                                                             c->d_fk, c->d_w, c->d_eta, c->d_kappa,
                                                             c->beta_k / c->beta_v, kappa_min, clip, box,
@@ -697,8 +776,11 @@ int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const doub
         CK(esm::launch_follow_disp<float>(c->Mf, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
     k_mix<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, c->d_kmid);
     CK(cudaGetLastError());
+    }
     if ((rc = set_kc_any(c, c->d_kmid))) return rc;
     if ((rc = rebuild_any(c))) return rc;
+    {
+    Span sp(c, ESM_KT_LANGEVIN);
     esm::k_kop_capacity<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, kappa_min,
                                                                  c->d_k1);
     CK(cudaGetLastError());
@@ -706,6 +788,7 @@ int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const doub
         CK(esm::launch_kop<double>(c->Md, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
     else
         CK(esm::launch_kop<float>(c->Mf, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
+    }
     CK(cudaMemcpyAsync(c->d_k, c->d_k1, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
     if ((rc = set_kc_any(c, c->d_k))) return rc;
     if ((rc = rebuild_any(c))) return rc;
@@ -721,13 +804,74 @@ int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const doub
 
 int esm_weather_step(esm_ctx *c, const int32_t *moved, const double *theta, const int32_t *window,
                      const int32_t *wstart, const double *xi, int64_t it) {
-    (void)moved;
-    (void)theta;
-    (void)window;
-    (void)wstart;
-    (void)xi;
-    (void)it;
-    return fail(c, ESM_EINVAL, "esm_weather_step: not available in this build");
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    if (!moved || !theta || !window || !wstart) return fail(c, ESM_EINVAL, "moved, theta, window, wstart are required");
+    int R = c->R, rc;
+    bool any = false, anyw = false, anyt = false;
+    for (int r = 0; r < R; ++r) {
+        any |= moved[r] != 0;
+        anyw |= moved[r] && window[r] > 0;
+        anyt |= moved[r] && theta[r] > 0;
+    }
+    if (!any) return ESM_OK;
+    CK(cudaMemcpyAsync(c->d_moved, moved, sizeof(int) * R, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_wtheta, theta, sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_window, window, sizeof(int) * R, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_wstart, wstart, sizeof(int) * R, cudaMemcpyHostToDevice, c->stream));
+    vector<int> wflag(R);
+    for (int r = 0; r < R; ++r) wflag[r] = moved[r] && window[r] > 0;
+    CK(cudaMemcpyAsync(c->d_wflag, wflag.data(), sizeof(int) * R, cudaMemcpyHostToDevice, c->stream));
+    const double *dxi = nullptr;
+    if (xi) {
+        size_t n = (size_t)R * c->n0 * c->T;
+        if (!c->d_wxi && (rc = dalloc(c, &c->d_wxi, n))) return rc;
+        CK(cudaMemcpyAsync(c->d_wxi, xi, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        dxi = c->d_wxi;
+    }
+    // residual before the change (compensate_weather!, src/replicas.jl:207 r0)
+    if ((rc = rebuild_any(c))) return rc;
+    size_t rbytes = (c->precision == 64 ? sizeof(double) : sizeof(float)) * (size_t)c->N * c->T * R;
+    CK(cudaMemcpyAsync(c->d_r0, c->r, rbytes, cudaMemcpyDeviceToDevice, c->stream));
+    {
+    Span sp(c, ESM_KT_WEATHER);
+    if (anyt) {  // pCN in the innovations at the current regimes
+        if (c->precision == 64)
+            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
+                                             c->d_reg, c->d_reg, dxi, c->seed, (uint32_t)it, 1, c->stream));
+        else
+            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
+                                            c->d_reg, c->d_reg, dxi, c->seed, (uint32_t)it, 1, c->stream));
+        c->launches += 1;
+    }
+    if (anyw) {  // regime window, then z rebuilt from its innovations at the new regimes
+        esm::k_regime_window<<<(R + 63) / 64, 64, 0, c->stream>>>(c->T, R, c->nreg, c->d_Ptr, c->d_pi0, c->d_moved,
+                                                                  c->d_window, c->d_wstart, c->d_reg, c->d_reg2,
+                                                                  c->d_wbeta, c->seed, (uint32_t)it);
+        CK(cudaGetLastError());
+        if (c->precision == 64)
+            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
+                                             c->d_reg, c->d_reg2, nullptr, c->seed, (uint32_t)it, 0, c->stream));
+        else
+            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
+                                            c->d_reg, c->d_reg2, nullptr, c->seed, (uint32_t)it, 0, c->stream));
+        CK(cudaMemcpyAsync(c->d_reg, c->d_reg2, sizeof(int32_t) * c->T * R, cudaMemcpyDeviceToDevice, c->stream));
+        c->launches += 2;
+    }
+    }
+    if ((rc = rebuild_any(c))) return rc;
+    {
+    Span sp(c, ESM_KT_WEATHER);
+    if (c->precision == 64)
+        CK(esm::launch_compensate<double>(c->Md, c->d_moved, (const double *)c->d_r0, c->stream));
+    else
+        CK(esm::launch_compensate<float>(c->Mf, c->d_moved, (const float *)c->d_r0, c->stream));
+    }
+    c->launches += 1;
+    if ((rc = rebuild_any(c))) return rc;
+    c->has_scores = false;
+    CK(cudaStreamSynchronize(c->stream));
+    return ESM_OK;
 }
 
 int esm_sync(esm_ctx *c, double timeout_s) {
@@ -744,5 +888,40 @@ int esm_sync(esm_ctx *c, double timeout_s) {
 }
 
 int64_t esm_launch_count(const esm_ctx *c) { return c ? c->launches : 0; }
+
+int esm_set_timing(esm_ctx *c, int32_t on) {
+    if (!c) return ESM_EINVAL;
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto &mk : c->marks) {
+        c->pool.push_back(mk.a);
+        c->pool.push_back(mk.b);
+    }
+    c->marks.clear();
+    for (int i = 0; i < ESM_KT_N; ++i) c->acc_ms[i] = c->acc_n[i] = 0;
+    c->timing = on != 0;
+    return ESM_OK;
+}
+
+int esm_timing(esm_ctx *c, double *out) {
+    if (!c || !out) return ESM_EINVAL;
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto &mk : c->marks) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, mk.a, mk.b));
+        c->acc_ms[mk.kind] += ms;
+        c->acc_n[mk.kind] += 1;
+        c->pool.push_back(mk.a);
+        c->pool.push_back(mk.b);
+    }
+    c->marks.clear();
+    for (int i = 0; i < ESM_KT_N; ++i) {
+        out[2 * i] = c->acc_ms[i];
+        out[2 * i + 1] = c->acc_n[i];
+        c->acc_ms[i] = c->acc_n[i] = 0;
+    }
+    return ESM_OK;
+}
+
+void *esm_stream(esm_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 }  // extern "C"

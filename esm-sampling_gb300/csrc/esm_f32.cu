@@ -19,4 +19,8 @@ template cudaError_t launch_kop<float>(const DevModel<float> &, const double *, 
                                        const double *, double, cudaStream_t);
 template cudaError_t launch_set_kc<float>(int, const double *, const double *, const double *, const int *,
                                           const int *, float *, float *, float *, cudaStream_t);
+template cudaError_t launch_weather_z<float>(const DevModel<float> &, const double *, const double *, const double *,
+                                             const double *, const int *, const double *, const int *, const int *,
+                                             const double *, uint64_t, uint32_t, int, cudaStream_t);
+template cudaError_t launch_compensate<float>(const DevModel<float> &, const int *, const float *, cudaStream_t);
 }  // namespace esm

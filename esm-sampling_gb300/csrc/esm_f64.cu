@@ -19,4 +19,8 @@ template cudaError_t launch_kop<double>(const DevModel<double> &, const double *
                                        const double *, double, cudaStream_t);
 template cudaError_t launch_set_kc<double>(int, const double *, const double *, const double *, const int *,
                                           const int *, double *, double *, double *, cudaStream_t);
+template cudaError_t launch_weather_z<double>(const DevModel<double> &, const double *, const double *, const double *,
+                                             const double *, const int *, const double *, const int *, const int *,
+                                             const double *, uint64_t, uint32_t, int, cudaStream_t);
+template cudaError_t launch_compensate<double>(const DevModel<double> &, const int *, const double *, cudaStream_t);
 }  // namespace esm

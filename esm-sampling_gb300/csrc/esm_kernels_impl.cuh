@@ -319,6 +319,55 @@ __global__ void k_set_kc(int K, const double *k_raw, const double *u_lo, const d
 }
 
 #ifdef ESM_COMMON_KERNELS
+
+// regime_window (src/replicas.jl:131-163), one thread per replica; a is 1-based; beta scratch [R*K*T]
+__global__ void k_regime_window(int T, int R, int K, const double *Ptr, const double *pi0, const int *moved,
+                                const int *window, const int *wstart, const int *reg, int *reg2, double *beta,
+                                uint64_t seed, uint32_t it) {
+    int rep = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rep >= R) return;
+    for (int t = 0; t < T; ++t) reg2[(size_t)t * R + rep] = reg[(size_t)t * R + rep];
+    if (!moved[rep] || window[rep] <= 0) return;
+    int a = min(T, max(1, wstart[rep]));
+    int b = min(T, a + window[rep] - 1);
+    int B = b - a + 1;
+    double *bt = beta + (size_t)rep * K * T;
+    for (int q = 0; q < K * B; ++q) bt[q] = 1.0;
+    if (b < T) {
+        int mb = reg[(size_t)b * R + rep];
+        for (int q = 0; q < K; ++q) bt[(size_t)q * B + (B - 1)] = Ptr[(size_t)q * K + mb];
+        for (int tau = b - 1; tau >= a; --tau) {
+            int col = tau - a, nxt = col + 1;
+            for (int q = 0; q < K; ++q) {
+                double s = 0.0;
+                for (int p = 0; p < K; ++p) s += Ptr[(size_t)q * K + p] * bt[(size_t)p * B + nxt];
+                bt[(size_t)q * B + col] = s;
+            }
+        }
+    }
+    for (int tau = a; tau <= b; ++tau) {
+        int j = tau - a;
+        double u, u2;
+        uniform2(seed, ESM_TAG_WTH, (uint32_t)(j >> 1), 1, (uint32_t)rep, it, &u, &u2);
+        if (j & 1) u = u2;
+        double tot = 0.0;
+        for (int q = 0; q < K; ++q) {
+            double pr = tau == 1 ? pi0[q] : Ptr[(size_t)reg2[(size_t)(tau - 2) * R + rep] * K + q];
+            tot += pr * bt[(size_t)q * B + j];
+        }
+        double tt = u * tot, cc = 0.0;
+        int kk = K - 1;
+        for (int q = 0; q < K; ++q) {
+            double pr = tau == 1 ? pi0[q] : Ptr[(size_t)reg2[(size_t)(tau - 2) * R + rep] * K + q];
+            cc += pr * bt[(size_t)q * B + j];
+            if (tt <= cc) {
+                kk = q;
+                break;
+            }
+        }
+        reg2[(size_t)(tau - 1) * R + rep] = kk;
+    }
+}
 // ---------------------------------------------------------------------------------------------
 // Langevin step of the shared capacities (langevin_capacities / langevin_update,
 // src/replicas.jl:368-403), FP64, one thread per unit; replica average in replica order (:697)
@@ -418,6 +467,113 @@ template <class real>
 cudaError_t launch_set_kc(int K, const double *k_raw, const double *lo, const double *hi, const int *u_kind,
                           const int *u_loc, real *kc_d, real *kc_s, real *kc_r, cudaStream_t s) {
     k_set_kc<real><<<(K + 127) / 128, 128, 0, s>>>(K, k_raw, lo, hi, u_kind, u_loc, kc_d, kc_s, kc_r);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// weather process (src/replicas.jl:49-112 pCN in the VAR innovations; :131-163 regime window;
+// :207 compensate_weather!) for the diagonal single-level VAR; the recursion runs in FP64
+// ---------------------------------------------------------------------------------------------
+template <class real>
+__device__ inline double var_mean(const DevModel<real> &M, const double *phi, const double *mu, int k, int i,
+                                  double zprev, int t) {
+    double tau = t + 1;
+    double cs = cos(2 * 3.141592653589793 * tau / M.T), sn = sin(2 * 3.141592653589793 * tau / M.T);
+    const double *m3 = mu + ((size_t)k * M.n0 + i) * 3;
+    return phi[(size_t)k * M.n0 + i] * zprev + 1.0 * m3[0] + cs * m3[1] + sn * m3[2];
+}
+
+template <class real>
+__device__ inline double weather_normal(uint64_t seed, uint32_t j, uint32_t rep, uint32_t it) {
+    double u0, u1;
+    uniform2(seed, ESM_TAG_WTH, j >> 1, 0, rep, it, &u0, &u1);
+    real rr = sqrt(real(-2) * log(real(1) - (real)u0));
+    real a = real(6.283185307179586) * (real)u1;
+    return (double)((j & 1) ? rr * sin(a) : rr * cos(a));
+}
+
+// one pass over series i of replica rep: innovations at regA, rotation by theta (> 0), rebuilt at regB
+template <class real>
+__global__ void k_weather_z(DevModel<real> M, const double *phi, const double *mu, const double *sig,
+                            const double *sig0, const int *moved, const double *theta, const int *regA,
+                            const int *regB, const double *xi, uint64_t seed, uint32_t it, int use_theta) {
+    int rep = blockIdx.y * blockDim.x + threadIdx.x;
+    int i = blockIdx.x;
+    if (rep >= M.R || i >= M.n0) return;
+    if (!moved[rep]) return;
+    double th = use_theta ? theta[rep] : 0.0;
+    if (use_theta && !(th > 0)) return;
+    double ct = cos(th), st = sin(th);
+    double zpo = 0, zpn = 0;
+    int T = M.T, R = M.R;
+    for (int t = 0; t < T; ++t) {
+        size_t zi = sidx(i, t, rep, T, R);
+        double zo = (double)M.z[zi];
+        int ka = regA[(size_t)t * R + rep], kb = regB[(size_t)t * R + rep];
+        double e = t == 0 ? zo / sig0[i] : (zo - var_mean(M, phi, mu, ka, i, zpo, t)) / sig[(size_t)ka * M.n0 + i];
+        if (use_theta) {
+            double x = xi ? xi[(size_t)rep * M.n0 * T + (size_t)t * M.n0 + i]
+                          : weather_normal<real>(seed, (uint32_t)((size_t)t * M.n0 + i), (uint32_t)rep, it);
+            e = ct * e + st * x;
+        }
+        double zn = t == 0 ? sig0[i] * e : var_mean(M, phi, mu, kb, i, zpn, t) + sig[(size_t)kb * M.n0 + i] * e;
+        M.z[zi] = (real)zn;
+        zpo = zo;
+        zpn = zn;
+    }
+}
+
+// compensate_weather! (src/replicas.jl:207) per (node, step, replica) of the moved replicas
+template <class real>
+__global__ void k_compensate(DevModel<real> M, const int *moved, const real *r0) {
+    size_t TR = (size_t)M.T * M.R;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)M.N * TR) return;
+    int n = (int)(i / TR);
+    size_t tr = i % TR;
+    int t = (int)(tr / M.R), rep = (int)(tr % M.R);
+    if (!moved[rep]) return;
+    real need = M.r[i] - r0[i];
+    if (fabs(need) < real(1e-6)) return;
+    int nu = M.up[n + 1] - M.up[n];
+    if (nu == 0) return;
+    real tot = 0;
+    for (int q = 0; q < nu; ++q) {
+        int j = M.ua[M.up[n] + q];
+        real ks = M.d_avail[j] * M.kc_d[j];
+        real ps = ks * clampr<real>(M.g[sidx(j, t, rep, M.T, M.R)], 0, 1);
+        tot += need > 0 ? fmax(ks - ps, real(0)) : ps;
+    }
+    if (!(tot > real(1e-9))) return;
+    real a = need > 0 ? fmin(need, tot) / tot : fmax(need, -tot) / tot;
+    for (int q = 0; q < nu; ++q) {
+        int j = M.ua[M.up[n] + q];
+        real ks = M.d_avail[j] * M.kc_d[j];
+        if (fabs(ks) < real(1e-9)) continue;
+        size_t gi = sidx(j, t, rep, M.T, M.R);
+        real ps = ks * clampr<real>(M.g[gi], 0, 1);
+        real w = need > 0 ? fmax(ks - ps, real(0)) : ps;
+        real dy = a * w / ks;
+        if (dy == 0) continue;
+        M.g[gi] += dy;
+    }
+}
+
+template <class real>
+cudaError_t launch_weather_z(const DevModel<real> &M, const double *phi, const double *mu, const double *sig,
+                             const double *sig0, const int *moved, const double *theta, const int *regA,
+                             const int *regB, const double *xi, uint64_t seed, uint32_t it, int use_theta,
+                             cudaStream_t s) {
+    int bx = M.R < 64 ? M.R : 64;
+    dim3 grid(M.n0, (M.R + bx - 1) / bx);
+    k_weather_z<real><<<grid, bx, 0, s>>>(M, phi, mu, sig, sig0, moved, theta, regA, regB, xi, seed, it, use_theta);
+    return cudaGetLastError();
+}
+
+template <class real>
+cudaError_t launch_compensate(const DevModel<real> &M, const int *moved, const real *r0, cudaStream_t s) {
+    size_t n = (size_t)M.N * M.T * M.R;
+    k_compensate<real><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M, moved, r0);
     return cudaGetLastError();
 }
 

@@ -24,4 +24,11 @@ cudaError_t launch_kop(const DevModel<real> &M, const double *kold, const double
 template <class real>
 cudaError_t launch_set_kc(int K, const double *k_raw, const double *lo, const double *hi, const int *u_kind,
                           const int *u_loc, real *kc_d, real *kc_s, real *kc_r, cudaStream_t s);
+template <class real>
+cudaError_t launch_weather_z(const DevModel<real> &M, const double *phi, const double *mu, const double *sig,
+                             const double *sig0, const int *moved, const double *theta, const int *regA,
+                             const int *regB, const double *xi, uint64_t seed, uint32_t it, int use_theta,
+                             cudaStream_t s);
+template <class real>
+cudaError_t launch_compensate(const DevModel<real> &M, const int *moved, const real *r0, cudaStream_t s);
 }  // namespace esm

@@ -20,7 +20,9 @@ NSTAT = 2 * (9 + 1) + 1
 # the symbols declared in include/esmcuda.h
 EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
            "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
-           "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count")
+           "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
+           "esm_set_timing", "esm_timing", "esm_stream")
+KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather")
 
 _lib = None
 
@@ -64,6 +66,10 @@ def load(build_if_missing=True):
     L.esm_sync.argtypes = [C.c_void_p, C.c_double]
     L.esm_launch_count.restype = C.c_int64
     L.esm_launch_count.argtypes = [C.c_void_p]
+    L.esm_set_timing.argtypes = [C.c_void_p, C.c_int32]
+    L.esm_timing.argtypes = [C.c_void_p, P_f64]
+    L.esm_stream.restype = C.c_void_p
+    L.esm_stream.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -121,6 +127,11 @@ class DeviceChain:
                                               _p(out["reg"], P_i32), _p(out["k"])), "esm_download_state")
         return out
 
+    def download_k(self):
+        k = np.zeros(self.m.Kunits)
+        self._check(self.L.esm_download_state(self.h, None, None, None, None, None, _p(k)), "esm_download_state")
+        return k
+
     def rebuild(self):
         self._check(self.L.esm_rebuild_caches(self.h), "esm_rebuild_caches")
 
@@ -159,8 +170,31 @@ class DeviceChain:
                                              _p(knew), _p(nclip, P_i32)), "esm_langevin_step")
         return knew, int(nclip[0])
 
+    def weather_step(self, moved, theta, window, wstart, xi=None, it=0):
+        """Weather process of the flagged replicas and the compensated re-initialisation of their
+        dispatch (replica_weather!, src/replicas.jl:586); wstart is the 1-based window start."""
+        moved = np.ascontiguousarray(moved, dtype=np.int32)
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        window = np.ascontiguousarray(window, dtype=np.int32)
+        wstart = np.ascontiguousarray(wstart, dtype=np.int32)
+        xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+        self._check(self.L.esm_weather_step(self.h, _p(moved, P_i32), _p(theta), _p(window, P_i32),
+                                            _p(wstart, P_i32), _p(xi), it), "esm_weather_step")
+
     def sync(self, timeout_s=60.0):
         self._check(self.L.esm_sync(self.h, timeout_s), "esm_sync")
+
+    def set_timing(self, on=True):
+        self._check(self.L.esm_set_timing(self.h, int(on)), "esm_set_timing")
+
+    def timing(self):
+        """Per kernel family: (milliseconds, launches) since the last call (CUDA events on the stream)."""
+        out = np.zeros(2 * len(KERNEL_FAMILIES))
+        self._check(self.L.esm_timing(self.h, _p(out)), "esm_timing")
+        return {k: (out[2 * i], int(out[2 * i + 1])) for i, k in enumerate(KERNEL_FAMILIES)}
+
+    def stream(self):
+        return self.L.esm_stream(self.h)
 
     def launch_count(self):
         return int(self.L.esm_launch_count(self.h))

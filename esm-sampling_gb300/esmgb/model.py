@@ -610,16 +610,37 @@ class ReplicaState:
     k: np.ndarray       # [Kunits]
 
 
+def sample_weather_batch(m: SynthModel, R: int, rng):
+    """Exact prior draws of R replicas at once (the recursion of ``src/weather.jl:461``
+    ``sample_weather``, vectorised over replicas): regimes [T, R] and anomalies [n0, T, R]."""
+    T, n0 = m.T, m.n0
+    reg = np.zeros((T, R), np.int32)
+    cum0 = np.cumsum(m.pi0)
+    cumP = np.cumsum(m.Ptr, axis=1)
+    reg[0] = np.minimum(np.searchsorted(cum0, rng.random(R), side="left"), m.K - 1)
+    u = rng.random((T, R))
+    for t in range(1, T):
+        reg[t] = np.minimum((u[t][:, None] > cumP[reg[t - 1]]).sum(1), m.K - 1)
+    z = np.zeros((n0, T, R))
+    z[:, 0, :] = m.sig0[:, None] * rng.standard_normal((n0, R))
+    cols = np.arange(n0)
+    for t in range(1, T):
+        e = rng.standard_normal((n0, R))
+        cs, sn = math.cos(2 * math.pi * (t + 1) / T), math.sin(2 * math.pi * (t + 1) / T)
+        k = reg[t]
+        mean = (m.phi[k].T * z[:, t - 1, :] + m.mu[k, :, 0].T + cs * m.mu[k, :, 1].T + sn * m.mu[k, :, 2].T)
+        z[:, t, :] = mean + m.sig[k].T * e
+    del cols
+    return reg, z
+
+
 def initial_state(m: SynthModel, R: int, seed: int = 7) -> ReplicaState:
     """Start state: independent prior weather draws per replica, zero angles, OCGT covering the
     residual load after renewables, storage half full (a heuristic interior start in the spirit of
     ``src/run.jl:470`` ``heuristic_start``)."""
     T = m.T
-    z = np.zeros((m.n0, T, R))
-    reg = np.zeros((T, R), np.int32)
-    for r in range(R):
-        rng = np.random.Generator(np.random.PCG64([seed, r]))
-        reg[:, r], z[:, :, r] = sample_weather(m, rng)
+    rng = np.random.Generator(np.random.PCG64([seed, R]))
+    reg, z = sample_weather_batch(m, R, rng)
     X = m.xbar[:, :, None] + m.wscale[:, None, None] * z
     W = np.empty_like(X)
     ld = m.series_field == 0

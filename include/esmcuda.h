@@ -178,6 +178,18 @@ int esm_langevin_step(esm_ctx *ctx, const double *w, const double *eta, const do
 int esm_weather_step(esm_ctx *ctx, const int32_t *moved, const double *theta,
                      const int32_t *window, const int32_t *wstart, const double *xi, int64_t it);
 
+/* Kernel families of the device timing (esm_timing). */
+enum { ESM_KT_CLASS = 0, ESM_KT_REBUILD, ESM_KT_SCORE, ESM_KT_LANGEVIN, ESM_KT_WEATHER, ESM_KT_N };
+
+/* Device timing: while on, every launch of the library is bracketed by CUDA events on the
+   context's stream. esm_timing writes out[2*i] = accumulated milliseconds and out[2*i+1] = launches
+   of family i (ESM_KT_*) since timing was switched on, then resets the counters. */
+int esm_set_timing(esm_ctx *ctx, int32_t on);
+int esm_timing(esm_ctx *ctx, double *out);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work after it. */
+void *esm_stream(esm_ctx *ctx);
+
 /* Synchronise the context's stream with a bounded wait (ESM_ETIMEOUT after timeout_s). */
 int esm_sync(esm_ctx *ctx, double timeout_s);
 

@@ -1263,6 +1263,142 @@ static void langevin_step(Ctx &c, const double *w, const double *eta, const doub
     if (nclip_out) *nclip_out = nclip;
 }
 
+// ------------------------------------------------------------------------------------------
+// weather process of one replica (src/replicas.jl:49-112 pCN in the VAR innovations, :131-167
+// regime window, :207 compensate_weather!), for the diagonal single-level VAR of the model
+// ------------------------------------------------------------------------------------------
+static inline double var_mean(const Model &m, int k, int i, double zprev, int t) {
+    double tau = t + 1;  // harmonics(tau, T0) with the reference's 1-based step (src/weather.jl:47)
+    double cs = cos(2 * M_PI * tau / m.T), sn = sin(2 * M_PI * tau / m.T);
+    const double *mu = &m.mu[((size_t)k * m.n0 + i) * 3];
+    return m.phi[(size_t)k * m.n0 + i] * zprev + 1.0 * mu[0] + cs * mu[1] + sn * mu[2];
+}
+
+// innovations of series i at regimes regA, rotated by theta (if > 0), rebuilt at regimes regB
+static void series_pass(Ctx &c, int i, int rep, const int *regA, const int *regB, double theta, const double *xi,
+                        int64_t it) {
+    const Model &m = c.m;
+    double zpo = 0, zpn = 0;
+    double ct = cos(theta), st = sin(theta);
+    for (int t = 0; t < m.T; ++t) {
+        double zo = c.z[ix(c, i, t, rep)];
+        int ka = regA[t], kb = regB[t];
+        double e = t == 0 ? zo / m.sig0[i] : (zo - var_mean(m, ka, i, zpo, t)) / m.sig[(size_t)ka * m.n0 + i];
+        if (theta > 0) {
+            double x = xi ? xi[(size_t)t * m.n0 + i]
+                          : orc_normal(c.o.seed, ESM_TAG_WTH, (uint32_t)((size_t)t * m.n0 + i), 0, (uint32_t)rep,
+                                       (uint32_t)it);
+            e = ct * e + st * x;
+        }
+        double zn = t == 0 ? m.sig0[i] * e : var_mean(m, kb, i, zpn, t) + m.sig[(size_t)kb * m.n0 + i] * e;
+        c.z[ix(c, i, t, rep)] = zn;
+        zpo = zo;
+        zpn = zn;
+    }
+}
+
+// regime_window (src/replicas.jl:131-163) with the uniforms of the stream; a is 1-based
+static void regime_window(const Ctx &c, const vector<int> &reg, int a, int b, int rep, int64_t it, vector<int> &out) {
+    const Model &m = c.m;
+    int K = m.nreg, T0 = m.T, B = b - a + 1;
+    out = reg;
+    vector<double> beta((size_t)K * B, 1.0);
+    if (b < T0) {
+        for (int q = 0; q < K; ++q) beta[(size_t)q * B + (B - 1)] = m.Ptr[(size_t)q * K + reg[b]];
+        for (int tau = b - 1; tau >= a; --tau) {
+            int col = tau - a, nxt = tau - a + 1;
+            for (int q = 0; q < K; ++q) {
+                double s = 0.0;
+                for (int p = 0; p < K; ++p) s += m.Ptr[(size_t)q * K + p] * beta[(size_t)p * B + nxt];
+                beta[(size_t)q * B + col] = s;
+            }
+        }
+    }
+    for (int tau = a; tau <= b; ++tau) {
+        double u, u2;
+        int j = tau - a;
+        orc_uniform2(c.o.seed, ESM_TAG_WTH, (uint32_t)(j >> 1), 1, (uint32_t)rep, (uint32_t)it, &u, &u2);
+        if (j & 1) u = u2;
+        vector<double> p(K);
+        double tot = 0.0;
+        for (int q = 0; q < K; ++q) {
+            double pr = tau == 1 ? m.pi0[q] : m.Ptr[(size_t)out[tau - 2] * K + q];
+            p[q] = pr * beta[(size_t)q * B + (tau - a)];
+            tot += p[q];
+        }
+        double tt = u * tot, cc = 0.0;
+        int kk = K - 1;
+        for (int q = 0; q < K; ++q) {
+            cc += p[q];
+            if (tt <= cc) {
+                kk = q;
+                break;
+            }
+        }
+        out[tau - 1] = kk;
+    }
+}
+
+// compensate_weather! (src/replicas.jl:207) of one replica from the residual r0 before the change
+static void compensate(Ctx &c, int rep, const vector<double> &r0) {
+    const Model &m = c.m;
+    for (int n = 0; n < m.N; ++n)
+        for (int t = 0; t < m.T; ++t) {
+            double need = c.r[ix(c, n, t, rep)] - r0[(size_t)n * m.T + t];
+            if (fabs(need) < 1e-6) continue;
+            int nu = m.up[n + 1] - m.up[n];
+            if (nu == 0) continue;
+            vector<double> ks(nu), wq(nu);
+            double tot = 0.0;
+            for (int q = 0; q < nu; ++q) {
+                int j = m.ua[m.up[n] + q];
+                ks[q] = kappa_unit(c, j);
+                double ps = ks[q] * clampd(c.g[ix(c, j, t, rep)], 0.0, 1.0);
+                wq[q] = need > 0 ? std::max(ks[q] - ps, 0.0) : ps;
+                tot += wq[q];
+            }
+            if (!(tot > 1e-9)) continue;
+            double a = need > 0 ? std::min(need, tot) / tot : std::max(need, -tot) / tot;
+            for (int q = 0; q < nu; ++q) {
+                if (fabs(ks[q]) < 1e-9) continue;
+                double dy = a * wq[q] / ks[q];
+                if (dy == 0.0) continue;
+                c.g[ix(c, m.ua[m.up[n] + q], t, rep)] += dy;
+            }
+        }
+}
+
+// weather_process_step + compensation for the flagged replicas; wstart is the 1-based window start
+static void weather_step(Ctx &c, const int *moved, const double *theta, const int *window, const int *wstart,
+                         const double *xi, int64_t it, int nthreads) {
+    const Model &m = c.m;
+    int R = c.o.R, T = m.T;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int rep = 0; rep < R; ++rep) {
+        if (!moved[rep]) continue;
+        for (int t = 0; t < T; ++t) rebuild_step(c, t, rep);
+        vector<double> r0((size_t)m.N * T);
+        for (int n = 0; n < m.N; ++n)
+            for (int t = 0; t < T; ++t) r0[(size_t)n * T + t] = c.r[ix(c, n, t, rep)];
+        vector<int> reg(T);
+        for (int t = 0; t < T; ++t) reg[t] = c.reg[(size_t)t * R + rep];
+        const double *xr = xi ? xi + (size_t)rep * m.n0 * T : nullptr;
+        if (theta[rep] > 0)
+            for (int i = 0; i < m.n0; ++i) series_pass(c, i, rep, reg.data(), reg.data(), theta[rep], xr, it);
+        if (window[rep] > 0) {
+            int a = std::max(1, std::min(T, wstart[rep]));
+            int b = std::min(T, a + window[rep] - 1);
+            vector<int> reg2;
+            regime_window(c, reg, a, b, rep, it, reg2);
+            for (int i = 0; i < m.n0; ++i) series_pass(c, i, rep, reg.data(), reg2.data(), 0.0, nullptr, it);
+            for (int t = 0; t < T; ++t) c.reg[(size_t)t * R + rep] = reg2[t];
+        }
+        for (int t = 0; t < T; ++t) rebuild_step(c, t, rep);
+        compensate(c, rep, r0);
+        for (int t = 0; t < T; ++t) rebuild_step(c, t, rep);
+    }
+}
+
 }  // namespace
 
 // ============================================================================================
@@ -1474,6 +1610,11 @@ int orc_langevin_step(void *p, const double *w, const double *eta, const double 
     langevin_step(*(Ctx *)p, w, eta, kappa_s, kmin, clip, box, xi, it, knew_out, nclip_out, nthreads);
     ((Ctx *)p)->has_scores = false;
     return 0;
+}
+
+void orc_weather_step(void *p, const int32_t *moved, const double *theta, const int32_t *window,
+                      const int32_t *wstart, const double *xi, int64_t it, int nthreads) {
+    weather_step(*(Ctx *)p, moved, theta, window, wstart, xi, it, nthreads);
 }
 
 }  // extern "C"

@@ -59,6 +59,7 @@ def lib():
         L.orc_langevin_step.restype = C.c_int
         L.orc_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int, P_f64,
                                         C.c_int64, P_f64, P_i32, C.c_int]
+        L.orc_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64, C.c_int]
         _lib = L
     return _lib
 
@@ -92,7 +93,7 @@ def langevin_update(k, g, xi, eta, ks, kmin=1.0, clip=np.inf, hi=None):
 class Oracle:
     """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
 
-    def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=96, span=0,
+    def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=192, span=0,
                  threads=None):
         import sys
         sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
@@ -177,3 +178,12 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle langevin_step: status {rc}")
         return knew, int(nclip[0])
+
+    def weather_step(self, moved, theta, window, wstart, xi=None, it=0):
+        moved = np.ascontiguousarray(moved, dtype=np.int32)
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        window = np.ascontiguousarray(window, dtype=np.int32)
+        wstart = np.ascontiguousarray(wstart, dtype=np.int32)
+        xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+        lib().orc_weather_step(self.h, _p(moved, P_i32), _p(theta), _p(window, P_i32), _p(wstart, P_i32), _p(xi),
+                               it, self.threads)

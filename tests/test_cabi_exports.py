@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "esmcuda.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*)\s*(esm_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*|void \*)\s*(esm_\w+)\s*\(", src, re.M)))
 
 
 def test_header_and_binding_agree():

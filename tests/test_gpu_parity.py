@@ -36,8 +36,14 @@ def task_flips(sd, so, m, tol_rel, tol_abs):
 
 
 def make(N=40, L=60, T=40, R=32, seed=11):
+    """A non-degenerate state: the heuristic start (whose residuals cancel to round-off, so that
+    their signs are set by last-bit differences) perturbed at random."""
     m = make_model(N, L, T, seed=seed)
     st = initial_state(m, R, seed=3)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    st.e = rng.uniform(0.05, 0.95, st.e.shape)
+    st.theta = 30.0 * rng.standard_normal(st.theta.shape)
     return m, st
 
 
@@ -156,3 +162,25 @@ def test_langevin_stream_normals(base):
     kd, _ = d.langevin_step(w, eta, ks, it=7)
     ko, _ = o.langevin_step(w, eta, ks, it=7)
     np.testing.assert_allclose(kd, ko, rtol=1e-12)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_weather_step(base, prec):
+    m, st = base
+    R = 32
+    d = DeviceChain(m, R, precision=prec, seed=5)
+    d.upload(st)
+    o = Oracle(m, R, seed=5)
+    o.set_state(st)
+    moved = (np.arange(R) % 3 != 0).astype(np.int32)
+    theta = np.where(np.arange(R) % 2 == 0, 0.3, 0.1)
+    window = np.where(np.arange(R) % 4 == 1, 12, 0)
+    wstart = 1 + (np.arange(R) * 7) % m.T
+    d.weather_step(moved, theta, window, wstart, it=4)
+    o.weather_step(moved, theta, window, wstart, it=4)
+    a, b = d.download(), o.get_state()
+    assert np.array_equal(a["reg"], b["reg"])
+    tz = 1e-9 if prec == 64 else 2e-5
+    assert np.abs(a["z"] - b["z"]).max() < tz * (1 + np.abs(b["z"]).max())
+    tg = 1e-8 if prec == 64 else 2e-3
+    assert np.abs(a["g"] - b["g"]).max() < tg
