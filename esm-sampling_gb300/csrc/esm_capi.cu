@@ -464,16 +464,16 @@ int rebuild_any(esm_ctx *c) {
     return ESM_OK;
 }
 
-int class_pass_any(esm_ctx *c, uint32_t sweep, int cls) {
+int class_pass_any(esm_ctx *c, uint32_t sweep, int cls, int limit = 0) {
     int ns = c->class_len[cls];
     if (ns == 0) return ESM_OK;
     Span sp(c, ESM_KT_CLASS);
     if (c->precision == 64)
-        CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, (double *)c->d_scratch, c->max_warps,
-                                          c->d_stats, c->stream));
+        CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, limit, (double *)c->d_scratch,
+                                          c->max_warps, c->d_stats, c->stream));
     else
-        CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, (float *)c->d_scratch, c->max_warps,
-                                         c->d_stats, c->stream));
+        CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, limit, (float *)c->d_scratch,
+                                         c->max_warps, c->d_stats, c->stream));
     c->launches += 1;
     return ESM_OK;
 }
@@ -693,12 +693,12 @@ int esm_download_caches(esm_ctx *c, double *r, double *F) {
     return f64 ? down_state<double>(c, c->F, F, c->L * TR) : down_state<float>(c, c->F, F, c->L * TR);
 }
 
-int esm_class_pass(esm_ctx *c, int64_t sweep, int32_t cls, int64_t *stats) {
+int esm_class_pass(esm_ctx *c, int64_t sweep, int32_t cls, int32_t move_limit, int64_t *stats) {
     if (!c) return ESM_EINVAL;
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
     if (cls < 0 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
     CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * (2 * (ESM_NFAM + 1) + 1), c->stream));
-    int rc = class_pass_any(c, (uint32_t)sweep, cls);
+    int rc = class_pass_any(c, (uint32_t)sweep, cls, move_limit);
     if (rc) return rc;
     c->has_scores = false;
     return stats_out(c, stats);

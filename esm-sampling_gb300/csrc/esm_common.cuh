@@ -152,4 +152,125 @@ __device__ inline real phibal(real x, real cs, real cd) {
     return x > 0 ? cs * x : -cd * x;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Difference forms of the cost pieces. A line move changes each term by a small amount on top of
+// a large value (a generator cost of 1e8 EUR changes by 1e2); the reference evaluates c(t) - c(0),
+// which in FP32 leaves ~10 EUR of rounding, i.e. 1e-3 nats of noise on the line potential. These
+// forms compute the change itself from the move's increments, exactly where the term stays on one
+// linear piece and by the plain difference only across a kink (where both values are small).
+// ---------------------------------------------------------------------------------------------
+
+// change of cl(y) = clamp(y, 0, 1) and of the box excess |y - cl(y)| when y0 moves by dy
+template <class real>
+__device__ inline void clamp_diff(real y0, real dy, real *dyc, real *dex) {
+    real y1 = y0 + dy;
+    if (y0 > 0 && y0 < 1 && y1 > 0 && y1 < 1) {
+        *dyc = dy;
+        *dex = 0;
+    } else if (y0 >= 1 && y1 >= 1) {
+        *dyc = 0;
+        *dex = dy;
+    } else if (y0 <= 0 && y1 <= 0) {
+        *dyc = 0;
+        *dex = -dy;
+    } else {
+        real c0 = clampr<real>(y0, 0, 1), c1 = clampr<real>(y1, 0, 1);
+        *dyc = c1 - c0;
+        *dex = fabs(y1 - c1) - fabs(y0 - c0);
+    }
+}
+
+// change of max(|f| - s, 0) when f0 moves by df
+template <class real>
+__device__ inline real hinge_diff(real f0, real df, real s) {
+    real f1 = f0 + df;
+    if (fabs(f0) <= s && fabs(f1) <= s) return 0;
+    if (f0 > s && f1 > s) return df;
+    if (f0 < -s && f1 < -s) return -df;
+    return fmax(fabs(f1) - s, real(0)) - fmax(fabs(f0) - s, real(0));
+}
+
+// change of phibal(S) when S0 moves by dS
+template <class real>
+__device__ inline real phibal_diff(real S0, real dS, real cs, real cd) {
+    real S1 = S0 + dS;
+    if (S0 > 0 && S1 > 0) return cs * dS;
+    if (S0 < 0 && S1 < 0) return -cd * dS;
+    return phibal<real>(S1, cs, cd) - phibal<real>(S0, cs, cd);
+}
+
+// state-of-charge storage term (src/energy.jl:448 soc_cost) as functions of d: the injection per
+// unit capacity pc - mc, the running part pc + mc and the penalty part (charging beyond the
+// rating, discharging beyond it without inflow, charging a unit that cannot charge)
+template <class real>
+__device__ inline void soc_parts(real d, real etain, real etaout, real qt, real *inj, real *run, real *pen) {
+    if (d >= 0) {
+        real pc = etain > 0 ? d / etain : real(0);
+        *inj = pc;
+        *run = pc;
+        *pen = (pc > 1 ? pc - 1 : real(0)) + (etain <= 0 ? d : real(0));
+    } else {
+        real x = -d * etaout;
+        real mc = fmin(x, real(1));
+        *inj = -mc;
+        *run = mc;
+        *pen = (qt <= 0 && x - 1 > 0) ? x - 1 : real(0);
+    }
+}
+
+template <class real>
+__device__ inline int soc_piece(real d, real etain, real etaout) {
+    if (d >= 0) return (etain > 0 && d / etain > 1) ? 1 : 0;
+    return (-d * etaout >= 1) ? 3 : 2;
+}
+
+// change of the storage term when the start value ye moves by a and the end value ye1 by b.
+// Returns the cost change; *dj the injection change, *d1 the new d.
+template <class real>
+__device__ inline real soc_diff(real h, real qt, real etain, real etaout, real mc, real k, real w, real dt, real cv,
+                                real ye, real ye1, real a, real b, real *dj, real *d1) {
+    real dc0, dex0, dc1, dex1;
+    clamp_diff<real>(ye, a, &dc0, &dex0);
+    clamp_diff<real>(ye1, b, &dc1, &dex1);
+    real ec = clampr<real>(ye, 0, 1), ec1 = clampr<real>(ye1, 0, 1);
+    real d0 = h * (ec1 - ec) / dt - qt;
+    real dd = h * (dc1 - dc0) / dt;
+    real dn = d0 + dd;
+    real dinj, drun, dpen;
+    int p0 = soc_piece<real>(d0, etain, etaout), p1 = soc_piece<real>(dn, etain, etaout);
+    if (p0 == p1) {
+        real si, sr, sp;
+        if (p0 == 0) {
+            si = etain > 0 ? real(1) / etain : real(0);
+            sr = si;
+            sp = etain <= 0 ? real(1) : real(0);
+        } else if (p0 == 1) {
+            si = real(1) / etain;
+            sr = si;
+            sp = si;
+        } else if (p0 == 2) {
+            si = etaout;
+            sr = -etaout;
+            sp = 0;
+        } else {
+            si = 0;
+            sr = 0;
+            sp = qt <= 0 ? -etaout : real(0);
+        }
+        dinj = si * dd;
+        drun = sr * dd;
+        dpen = sp * dd;
+    } else {
+        real i0, r0, q0, i1, r1, q1;
+        soc_parts<real>(d0, etain, etaout, qt, &i0, &r0, &q0);
+        soc_parts<real>(dn, etain, etaout, qt, &i1, &r1, &q1);
+        dinj = i1 - i0;
+        drun = r1 - r0;
+        dpen = q1 - q0;
+    }
+    *dj = k * dinj;
+    *d1 = dn;
+    return dt * mc * k * drun + cv * dt * w * dpen + cv * w * h * dex0;
+}
+
 }  // namespace esm

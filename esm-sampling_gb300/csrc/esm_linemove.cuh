@@ -12,5 +12,5 @@ template <class real>
 size_t linemove_smem_per_warp(const DevModel<real> &M);
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
-                              real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s);
+                              int limit, real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s);
 }  // namespace esm

@@ -203,89 +203,68 @@ struct Lane {
             real Q = S(LL.kq, q);
             S(LL.kph, q) = fmax(Q + d.kg[q] * t, real(0)) - fmax(Q, real(0));
         }
-        // ---- step tau
+        // ---- step tau (every term in difference form, see clamp_diff)
         for (int q = 0; q < nns; ++q) S(LL.drs, q) = 0;
         for (int q = 0; q < ng; ++q) {
             int j = d.gi[q];
-            real y0 = M.g[ix(j, tau)];
             real k = M.kc_d[j], A = M.d_avail[j];
-            real y1 = y0 + t * d.ga[q];
-            real p0, p1;
-            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
-            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
-            D += c1 - c0;
-            S(LL.drs, d.gpos[q]) -= p1 - p0;
+            real dyc, dex;
+            clamp_diff<real>(M.g[ix(j, tau)], t * d.ga[q], &dyc, &dex);
+            real dp = A * k * dyc;
+            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            S(LL.drs, d.gpos[q]) -= dp;
         }
         for (int q = 0; q < nku; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
             real ak = S(LL.kua, q);
             if (ak == 0) continue;
             int j = d.ku[q];
-            real y0 = M.g[ix(j, tau)];
             real k = M.kc_d[j], A = M.d_avail[j];
-            real y1 = y0 + (t * real(0) + ak * S(LL.kph, d.kk[q]));
-            real p0, p1;
-            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
-            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
-            D += c1 - c0;
-            S(LL.drs, d.kupos[q]) -= p1 - p0;
+            real dyc, dex;
+            clamp_diff<real>(M.g[ix(j, tau)], ak * S(LL.kph, d.kk[q]), &dyc, &dex);
+            real dp = A * k * dyc;
+            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            S(LL.drs, d.kupos[q]) -= dp;
         }
         for (int q = 0; q < nl; ++q) {
             int e = d.li[q];
-            real f0 = M.F[ix(e, tau)], f1 = f0 + t * d.ldf[q];
-            real se = M.ls[e];
-            D += cv * dt * (fmax(fabs(f1) - se, real(0)) - fmax(fabs(f0) - se, real(0)));
-            S(LL.drs, d.lpa[q]) += f1 - f0;
-            S(LL.drs, d.lpb[q]) -= f1 - f0;
+            real df = t * d.ldf[q];
+            D += cv * dt * hinge_diff<real>(M.F[ix(e, tau)], df, M.ls[e]);
+            S(LL.drs, d.lpa[q]) += df;
+            S(LL.drs, d.lpb[q]) -= df;
         }
         for (int q = 0; q < nse; ++q) {
             int j = d.si[q];
-            real k = M.kc_s[j], w = k + k0;
-            real ye = M.e[ix(j, tau)], ye1 = M.e[ix(j, tau1)];
-            real d0, j0, d1, j1;
-            real c0 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv, ye,
-                                     ye1, &d0, &j0);
-            real c1 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
-                                     ye + t * d.sa[q], ye1 + t * real(0), &d1, &j1);
-            D += c1 - c0;
-            S(LL.drs, d.spos[q]) += j1 - j0;
+            real k = M.kc_s[j];
+            real dj, d1;
+            D += soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
+                                M.e[ix(j, tau)], M.e[ix(j, tau1)], t * d.sa[q], real(0), &dj, &d1);
+            S(LL.drs, d.spos[q]) += dj;
             S(LL.dcs, q) = d1;
         }
-        for (int q = 0; q < nns; ++q) {
-            real S0 = M.r[ix(d.nds[q], tau)];
-            real S1 = S0 + S(LL.drs, q);
-            D += dt * (phibal<real>(S1, M.c_shed, M.c_dump) - phibal<real>(S0, M.c_shed, M.c_dump));
-        }
+        for (int q = 0; q < nns; ++q)
+            D += dt * phibal_diff<real>(M.r[ix(d.nds[q], tau)], S(LL.drs, q), M.c_shed, M.c_dump);
         // ---- step tau - 1 (linked storage terms: the end value moves with step tau)
         for (int q = 0; q < nna; ++q) S(LL.dra, q) = 0;
         for (int q = 0; q < nga; ++q) {
             int j = d.gia[q];
-            real y0 = M.g[ix(j, taum)];
             real k = M.kc_d[j], A = M.d_avail[j];
-            real y1 = y0 + t * d.gaa[q];
-            real p0, p1;
-            real c0 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y0, &p0);
-            real c1 = gen_cost<real>(M.d_mc[j], A, k, k + k0, dt, cv, y1, &p1);
-            D += c1 - c0;
-            S(LL.dra, d.gposa[q]) -= p1 - p0;
+            real dyc, dex;
+            clamp_diff<real>(M.g[ix(j, taum)], t * d.gaa[q], &dyc, &dex);
+            real dp = A * k * dyc;
+            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            S(LL.dra, d.gposa[q]) -= dp;
         }
         for (int q = 0; q < nse; ++q) {
             int j = d.si[q];
-            real k = M.kc_s[j], w = k + k0;
-            real ye = M.e[ix(j, taum)], ye1 = M.e[ix(j, tau)];
-            real d0, j0, d1, j1;
-            real c0 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv, ye,
-                                     ye1, &d0, &j0);
-            real c1 = soc_cost<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
-                                     ye + t * real(0), ye1 + t * d.sa[q], &d1, &j1);
-            D += c1 - c0;
-            S(LL.dra, d.sposa[q]) += j1 - j0;
+            real k = M.kc_s[j];
+            real dj, d1;
+            D += soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
+                                M.e[ix(j, taum)], M.e[ix(j, tau)], real(0), t * d.sa[q], &dj, &d1);
+            S(LL.dra, d.sposa[q]) += dj;
             S(LL.dca, q) = d1;
         }
-        for (int q = 0; q < nna; ++q) {
-            real S0 = M.r[ix(d.nda[q], taum)];
-            real S1 = S0 + S(LL.dra, q);
-            D += dt * (phibal<real>(S1, M.c_shed, M.c_dump) - phibal<real>(S0, M.c_shed, M.c_dump));
-        }
+        for (int q = 0; q < nna; ++q)
+            D += dt * phibal_diff<real>(M.r[ix(d.nda[q], taum)], S(LL.dra, q), M.c_shed, M.c_dump);
         return M.beta_v * D;
     }
 
@@ -1095,7 +1074,7 @@ __device__ void lane_kinks(const Lane<real> &Ln) {
 // ---------------------------------------------------------------------------------------------
 template <class real>
 __global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int *steps, int nsteps, int ntile,
-                                                   int wpt, uint32_t sweep, int cls, real *scratch,
+                                                   int wpt, uint32_t sweep, int cls, int limit, real *scratch,
                                                    unsigned long long *stats, size_t smem_per_warp) {
     extern __shared__ __align__(16) char smem[];
     int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1129,7 +1108,8 @@ __global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int 
         Ln.tau1 = (Ln.tau + 1) % T;
         Stream st{M.seed, (uint32_t)tile, (uint32_t)cls, sweep, 0u};
         build_list(M, d, st, lane);
-        for (int mi = 0; mi < nmoves; ++mi) {
+        int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
+        for (int mi = 0; mi < nrun; ++mi) {
             int fi = prep_move(M, d, st, d.moves[mi], lane);
             if (fi < 0) continue;
             if (!Ln.active) continue;
@@ -1185,7 +1165,7 @@ size_t linemove_smem_per_warp(const DevModel<real> &M) {
 
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
-                              real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s) {
+                              int limit, real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s) {
     int ntile = (nsteps + M.span - 1) / M.span;
     int wpt = (M.span * M.R + 31) / 32;
     int items = ntile * wpt;
@@ -1199,7 +1179,8 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
         cudaFuncSetAttribute(k_class_pass<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_class_pass<real><<<blocks, wpb * 32, smem, s>>>(M, steps, nsteps, ntile, wpt, sweep, cls, scratch, stats, spw);
+    k_class_pass<real><<<blocks, wpb * 32, smem, s>>>(M, steps, nsteps, ntile, wpt, sweep, cls, limit, scratch, stats,
+                                                      spw);
     return cudaGetLastError();
 }
 

@@ -58,7 +58,7 @@ def load(build_if_missing=True):
     L.esm_rebuild_caches.argtypes = [C.c_void_p]
     L.esm_download_caches.argtypes = [C.c_void_p, P_f64, P_f64]
     L.esm_operation_sweeps.argtypes = [C.c_void_p, C.c_int32, C.c_int64, P_i64]
-    L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, P_i64]
+    L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
     L.esm_capacity_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
     L.esm_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int32, P_f64,
                                     C.c_int64, P_f64, P_i32]
@@ -142,9 +142,9 @@ class DeviceChain:
         self._check(self.L.esm_download_caches(self.h, _p(r), _p(F)), "esm_download_caches")
         return r, F
 
-    def class_pass(self, sweep, cls):
+    def class_pass(self, sweep, cls, limit=0):
         st = np.zeros(NSTAT, np.int64)
-        self._check(self.L.esm_class_pass(self.h, sweep, cls, _p(st, P_i64)), "esm_class_pass")
+        self._check(self.L.esm_class_pass(self.h, sweep, cls, limit, _p(st, P_i64)), "esm_class_pass")
         return st
 
     def sweeps(self, n, sweep0=0, stats=True):

@@ -150,8 +150,9 @@ int esm_download_caches(esm_ctx *ctx, double *r, double *F);
    2*(ESM_NFAM+1), the number of guard events (walk beyond max_points). */
 int esm_operation_sweeps(esm_ctx *ctx, int32_t n, int64_t sweep0, int64_t *stats);
 
-/* One colour class of one sweep (parity tests): class index in the sweep's class order. */
-int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int64_t *stats);
+/* One colour class of one sweep (parity tests): class cls (0: even 0-based steps, 1: odd, 2: the
+   last step of an odd year); only the first move_limit entries of every move list when > 0. */
+int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int32_t move_limit, int64_t *stats);
 
 /* Capacity scores per replica: sk [R*K] (s_k = -beta_v dC/dk + dlogJ/dk, node space) and the
    capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with

@@ -872,14 +872,15 @@ static bool prep_family(const Ctx &c, TileStream &ts, int fam, WS &ws, WS &wa, i
 // the moves of one (replica, step) task: the body of the threaded loop of local_sweep!
 // (src/local.jl:1954-2051)
 static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int tau, int rep, uint32_t sweep,
-                     int64_t *stats, WS &ws, WS &wa) {
+                     int64_t *stats, WS &ws, WS &wa, int limit) {
     const Model &m = c.m;
     int T = m.T;
     int taum = (tau - 1 + T) % T;
     TileStream ts = ts0;  // the selection draws continue after the list draws
     vector<Kink> jac;
     Mover mv{&c, &ws, &wa, rep, m.beta_v, {}};
-    for (size_t mi = 0; mi < moves.size(); ++mi) {
+    size_t nrun = limit > 0 && (size_t)limit < moves.size() ? (size_t)limit : moves.size();
+    for (size_t mi = 0; mi < nrun; ++mi) {
         ws.clear();
         wa.clear();
         ws.tau = tau;
@@ -935,7 +936,7 @@ static void class_steps(int T, int cls, vector<int> &out) {
 
 static int span_of(const Ctx &c) { return c.o.span > 0 ? c.o.span : std::max(1, 32 / c.o.R); }
 
-static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthreads) {
+static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthreads, int limit = 0) {
     vector<int> steps;
     class_steps(c.m.T, cls, steps);
     int span = span_of(c);
@@ -954,7 +955,7 @@ static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthr
             TileStream ts{c.o.seed, (uint32_t)tile, (uint32_t)cls, sweep};
             move_list(c, ts, moves);
             for (int q = tile * span; q < std::min((int)steps.size(), (tile + 1) * span); ++q)
-                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts, steps[q], rep, sweep, loc.data(), ws, wa);
+                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts, steps[q], rep, sweep, loc.data(), ws, wa, limit);
         }
 #pragma omp critical
         for (int i = 0; i < nst; ++i) stats[i] += loc[i];
@@ -1573,8 +1574,8 @@ void orc_set_caches(void *p, const double *r, const double *F) {
 }
 
 // one class of one sweep (caches must be current)
-void orc_class_pass(void *p, int64_t sweep, int cls, int64_t *stats, int nthreads) {
-    class_pass(*(Ctx *)p, (uint32_t)sweep, cls, stats, nthreads);
+void orc_class_pass(void *p, int64_t sweep, int cls, int limit, int64_t *stats, int nthreads) {
+    class_pass(*(Ctx *)p, (uint32_t)sweep, cls, stats, nthreads, limit);
 }
 
 // n sweeps: caches rebuilt at each sweep start (LocalCost, src/local.jl:1940), classes in the

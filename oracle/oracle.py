@@ -52,7 +52,7 @@ def lib():
         L.orc_rebuild.argtypes = [C.c_void_p, C.c_int]
         L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
         L.orc_set_caches.argtypes = [C.c_void_p, P_f64, P_f64]
-        L.orc_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int, P_i64, C.c_int]
+        L.orc_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i64, C.c_int]
         L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
         L.orc_class_order.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32]
         L.orc_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_int]
@@ -116,7 +116,8 @@ class Oracle:
                 "reg": (m.T, R), "k": (m.Kunits,)}
 
     def set_state(self, st):
-        arr = {k: np.ascontiguousarray(getattr(st, k), dtype=np.int32 if k == "reg" else np.float64)
+        get = (lambda k: st[k]) if isinstance(st, dict) else (lambda k: getattr(st, k))
+        arr = {k: np.ascontiguousarray(get(k), dtype=np.int32 if k == "reg" else np.float64)
                for k in ("theta", "g", "e", "z", "reg", "k")}
         self._in = arr
         lib().orc_set_state(self.h, _p(arr["theta"]), _p(arr["g"]), _p(arr["e"]), _p(arr["z"]),
@@ -144,9 +145,9 @@ class Oracle:
         F = np.ascontiguousarray(F, dtype=np.float64)
         lib().orc_set_caches(self.h, _p(r), _p(F))
 
-    def class_pass(self, sweep, cls):
+    def class_pass(self, sweep, cls, limit=0):
         st = np.zeros(NSTAT, np.int64)
-        lib().orc_class_pass(self.h, sweep, cls, _p(st, P_i64), self.threads)
+        lib().orc_class_pass(self.h, sweep, cls, limit, _p(st, P_i64), self.threads)
         return st
 
     def sweeps(self, n, sweep0=0):
