@@ -176,14 +176,14 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
 template <class real>
 struct Lane {
     const DevModel<real> &M;
-    Desc<real> &d;
-    real *slab;  // this warp's scratch slab
+    Desc<real> &d;            // the warp's move descriptor (shared memory)
+    real *slab;               // this warp's scratch slab
     int lane;
-    LaneLayout LL;
+    const LaneLayout &LL;     // per-lane scratch layout (shared memory)
     int tau, taum, tau1, rep;
     bool active;
 
-    __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int lane_, LaneLayout LL_)
+    __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int lane_, const LaneLayout &LL_)
         : M(M_), d(d_), slab(slab_), lane(lane_), LL(LL_) {}
 
     __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * 32 + lane]; }
@@ -1073,14 +1073,21 @@ __device__ void lane_kinks(const Lane<real> &Ln) {
 // the kernel: one colour class of one sweep
 // ---------------------------------------------------------------------------------------------
 template <class real>
-__global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int *steps, int nsteps, int ntile,
+__global__ void __launch_bounds__(128) k_class_pass(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps, int ntile,
                                                    int wpt, uint32_t sweep, int cls, int limit, real *scratch,
                                                    unsigned long long *stats, size_t smem_per_warp) {
     extern __shared__ __align__(16) char smem[];
+    __shared__ Desc<real> sdesc[4];
+    __shared__ LaneLayout sLL;
+    __shared__ unsigned long long scnt[4][2 * (ESM_NFAM + 1) + 1];
     int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int nmoves = M.natoms + M.nextra;
-    Desc<real> d = carve_desc<real>(smem + wib * smem_per_warp, M, nmoves);
-    LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    if (lane == 0) sdesc[wib] = carve_desc<real>(smem + wib * smem_per_warp, M, nmoves);
+    if (threadIdx.x == 0) sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    for (int i = lane; i < 2 * (ESM_NFAM + 1) + 1; i += 32) scnt[wib][i] = 0;
+    __syncthreads();
+    Desc<real> &d = sdesc[wib];
+    const LaneLayout &LL = sLL;
     int gw = blockIdx.x * (blockDim.x >> 5) + wib;
     int nw = gridDim.x * (blockDim.x >> 5);
     real *slab = scratch + (size_t)gw * LL.total * 32;
@@ -1092,8 +1099,6 @@ __global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int 
     }
     for (int i = lane; i < M.L; i += 32) d.lmark[i] = 0;
     __syncwarp();
-    unsigned long long loc_tried[ESM_NFAM + 1], loc_moved[ESM_NFAM + 1], loc_guard = 0;
-    for (int i = 0; i <= ESM_NFAM; ++i) loc_tried[i] = loc_moved[i] = 0;
     Lane<real> Ln(M, d, slab, lane, LL);
     for (int item = gw; item < ntile * wpt; item += nw) {
         int tile = item / wpt, grp = item % wpt;
@@ -1118,7 +1123,7 @@ __global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int 
             uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
             bool guard;
             real t = Ln.sample_line((real)uc, (real)uo, &guard);
-            if (guard) ++loc_guard;
+            if (guard) atomicAdd(&scnt[wib][2 * (ESM_NFAM + 1)], 1ull);
             if (fi == ESM_FAM_XLOCC && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
                 int nk = d.hdr[3];
                 bool any = false;
@@ -1137,16 +1142,14 @@ __global__ void __launch_bounds__(128) k_class_pass(DevModel<real> M, const int 
                 }
             }
             if (t != 0) Ln.commit(t);
-            loc_tried[fi] += 1;
-            loc_moved[fi] += t != 0;
+            atomicAdd(&scnt[wib][2 * fi], 1ull);
+            if (t != 0) atomicAdd(&scnt[wib][2 * fi + 1], 1ull);
         }
         __syncwarp();
     }
-    for (int i = 0; i <= ESM_NFAM; ++i) {
-        if (loc_tried[i]) atomicAdd(&stats[2 * i], loc_tried[i]);
-        if (loc_moved[i]) atomicAdd(&stats[2 * i + 1], loc_moved[i]);
-    }
-    if (loc_guard) atomicAdd(&stats[2 * (ESM_NFAM + 1)], loc_guard);
+    __syncwarp();
+    for (int i = lane; i < 2 * (ESM_NFAM + 1) + 1; i += 32)
+        if (scnt[wib][i]) atomicAdd(&stats[i], scnt[wib][i]);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -14,7 +14,7 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libesmcuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-UNITS = [("esm_capi.cu", []), ("esm_f32.cu", []), ("esm_f64.cu", ["-fmad=false"])]
+UNITS = [("esm_capi.cu", []), ("esm_f32.cu", []), ("esm_f64.cu", ["-fmad=false"]), ("esm_mlp.cu", [])]
 
 
 def nvcc():

@@ -197,6 +197,27 @@ int esm_sync(esm_ctx *ctx, double timeout_s);
 /* Device launches recorded since creation (kernels of this library). */
 int64_t esm_launch_count(const esm_ctx *ctx);
 
+/* ------------------------------------------------------------------------------------------
+ * Surrogate of the replica-averaged capacity score (no counterpart in the reference: the
+ * learned proposal is an addition of this library). An MLP with nlayers linear layers of widths
+ * dims[0] -> dims[1] -> ... -> dims[nlayers], SiLU between them, BF16 weights and activations
+ * with FP32 accumulation on the tensor cores, trained by Adam on the mean-squared error.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct esm_mlp esm_mlp;
+int esm_mlp_create(int32_t nlayers, const int32_t *dims, int32_t batch_max, uint64_t seed, esm_mlp **out);
+int esm_mlp_destroy(esm_mlp *mlp);
+const char *esm_mlp_last_error(const esm_mlp *mlp);
+/* layer l: W [dims[l+1], dims[l]] row-major and b [dims[l+1]], FP32 (either may be NULL) */
+int esm_mlp_set_layer(esm_mlp *mlp, int32_t l, const float *w, const float *b);
+int esm_mlp_get_layer(esm_mlp *mlp, int32_t l, float *w, float *b);
+/* y [B, dims[nlayers]] = MLP(x [B, dims[0]]) */
+int esm_mlp_forward(esm_mlp *mlp, int32_t B, const float *x, float *y);
+/* one Adam step (lr) on the minibatch; loss_out: (1/2B) sum (y - t)^2 before the step;
+   grads_out (may be NULL): the gradients, layer by layer, W then b */
+int esm_mlp_train_step(esm_mlp *mlp, int32_t B, const float *x, const float *target, float lr,
+                       double *loss_out, float *grads_out);
+int64_t esm_mlp_launch_count(const esm_mlp *mlp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1591,6 +1591,21 @@ void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
     }
 }
 
+// the move list of a tile (diagnostics): kind (-1 atom, else family), field, atom
+int orc_move_list(void *p, int64_t sweep, int cls, int tile, int *kinds, int *fields, int *atoms, int maxn) {
+    Ctx *c = (Ctx *)p;
+    TileStream ts{c->o.seed, (uint32_t)tile, (uint32_t)cls, (uint32_t)sweep};
+    vector<MoveRef> moves;
+    move_list(*c, ts, moves);
+    int n = (int)moves.size() < maxn ? (int)moves.size() : maxn;
+    for (int i = 0; i < n; ++i) {
+        kinds[i] = moves[i].kind;
+        fields[i] = moves[i].field;
+        atoms[i] = moves[i].atom;
+    }
+    return (int)moves.size();
+}
+
 void orc_class_order(void *p, int64_t sweep, int *order, int *ncls) {
     class_order(*(Ctx *)p, (uint32_t)sweep, order, ncls);
 }

@@ -59,6 +59,8 @@ def lib():
         L.orc_langevin_step.restype = C.c_int
         L.orc_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int, P_f64,
                                         C.c_int64, P_f64, P_i32, C.c_int]
+        L.orc_move_list.restype = C.c_int
+        L.orc_move_list.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i32, P_i32, P_i32, C.c_int]
         L.orc_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64, C.c_int]
         _lib = L
     return _lib
@@ -154,6 +156,11 @@ class Oracle:
         st = np.zeros(NSTAT, np.int64)
         lib().orc_sweeps(self.h, n, sweep0, _p(st, P_i64), self.threads)
         return st
+
+    def move_list(self, sweep, cls, tile, maxn=4096):
+        k, f, a = (np.zeros(maxn, np.int32) for _ in range(3))
+        n = lib().orc_move_list(self.h, sweep, cls, tile, _p(k, P_i32), _p(f, P_i32), _p(a, P_i32), maxn)
+        return k[:n], f[:n], a[:n]
 
     def class_order(self, sweep):
         o = np.zeros(3, np.int32)
