@@ -32,6 +32,8 @@ for _p in (ROOT, os.path.join(ROOT, "esm-sampling_gb300")):
 import numpy as np  # noqa: E402
 
 WORKLOAD = dict(N=40, L=60, T=8760, R=64, seed=1234)
+# a reduced case of the same model (T = 584, 15-hour steps) for profiler captures
+SMALL = dict(N=40, L=60, T=584, R=64, seed=1234)
 METRIC = "local-move sweeps/s"
 UNIT = "sweeps/s"
 
@@ -226,6 +228,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args):
+    """Operation sweeps of the reduced case, for ncu captures of the line-move kernel."""
+    from esmgb import build as B
+    B.build()
+    from esmgb.device import DeviceChain
+    from esmgb.model import initial_state, make_model
+    w = SMALL
+    m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
+    d = DeviceChain(m, w["R"], precision=32, seed=w["seed"])
+    d.upload(initial_state(m, w["R"], seed=7))
+    d.sweeps(args.warmup, 0, stats=False)
+    d.set_timing(True)
+    st = d.sweeps(args.steps, args.warmup)
+    kt = d.timing()
+    print(json.dumps({"case": "small", "T": w["T"], "R": w["R"], "sweeps": args.steps,
+                      "kernel_ms": {k: v[0] for k, v in kt.items()}, "launches": {k: v[1] for k, v in kt.items()},
+                      "moves_tried": int(st[:20:2].sum()), "guards": int(st[-1])}), flush=True)
+
+
 def config_dict():
     w = WORKLOAD
     return {"workload": "plain replica sampler on GPU: 40 nodes, 60 lines, T=8760 hourly, 64 replicas",
@@ -241,7 +262,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-replicas", type=int, default=2)
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
+    if args.case == "small":
+        return profile_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)

@@ -49,3 +49,25 @@ def grads(layers, x, t):
             s = 1.0 / (1.0 + np.exp(-z))
             d = da * (s * (1.0 + z * (1.0 - s)))
     return loss, out
+
+
+def grads_exact(layers, x, t):
+    """The same gradients without BF16 rounding (FP64 throughout), for finite-difference checks."""
+    B = x.shape[0]
+    a = [np.asarray(x, np.float64)]
+    zs = []
+    for l, (W, b) in enumerate(layers):
+        z = a[-1] @ np.asarray(W, np.float64).T + np.asarray(b, np.float64)
+        zs.append(z)
+        if l + 1 < len(layers):
+            a.append(silu(z))
+    loss = 0.5 * np.sum((zs[-1] - t) ** 2) / B
+    d = (zs[-1] - t) / B
+    out = [None] * len(layers)
+    for l in range(len(layers) - 1, -1, -1):
+        out[l] = (d.T @ a[l], d.sum(0))
+        if l > 0:
+            z = zs[l - 1]
+            s = 1.0 / (1.0 + np.exp(-z))
+            d = (d @ np.asarray(layers[l][0], np.float64)) * (s * (1.0 + z * (1.0 - s)))
+    return loss, out
