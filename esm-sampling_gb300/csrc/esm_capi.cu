@@ -427,6 +427,59 @@ int alloc_state(esm_ctx *c) {
     return ESM_OK;
 }
 
+// FP32 build: an FP64 copy of the state (fields and weather) and its caches. The capacity scores
+// weigh every node balance by the shed or the dump price according to its sign, and near equilibrium
+// many balances sit within FP32 round-off of zero: the scores are therefore computed in FP64 on the
+// widened FP32 state, with the FP64 parameters, as the FP64 build computes them.
+int alloc_shadow(esm_ctx *c) {
+    esm::DevModel<double> &M = c->Md;
+    size_t TR = (size_t)M.T * M.R;
+    double *p;
+    int rc;
+#define AL(field, n)                       \
+    if ((rc = dalloc(c, &p, (size_t)(n)))) \
+        return rc;                         \
+    M.field = p;
+    AL(theta, M.N * TR);
+    AL(g, M.D * TR);
+    AL(e, M.S * TR);
+    AL(r, M.N * TR);
+    AL(F, M.L * TR);
+    AL(z, M.n0 * TR);
+    AL(kc_d, M.D);
+    AL(kc_s, M.S);
+    AL(kc_r, std::max(M.Nren, 1));
+#undef AL
+    return ESM_OK;
+}
+
+__global__ void k_widen(size_t n, const float *a, double *b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
+int widen_state(esm_ctx *c) {
+    const esm::DevModel<float> &A = c->Mf;
+    esm::DevModel<double> &B = c->Md;
+    size_t TR = (size_t)A.T * A.R;
+    struct {
+        const float *a;
+        double *b;
+        size_t n;
+    } v[4] = {{A.theta, B.theta, A.N * TR}, {A.g, B.g, A.D * TR}, {A.e, B.e, A.S * TR}, {A.z, B.z, A.n0 * TR}};
+    for (auto &x : v) {
+        if (x.n == 0) continue;
+        k_widen<<<(unsigned)std::min<size_t>((x.n + 255) / 256, 152 * 16), 256, 0, c->stream>>>(x.n, x.a, x.b);
+        CK(cudaGetLastError());
+        c->launches += 1;
+    }
+    CK(esm::launch_set_kc<double>(c->K, c->d_k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (double *)B.kc_d,
+                                  (double *)B.kc_s, (double *)B.kc_r, c->stream));
+    CK(esm::launch_rebuild<double>(B, c->stream));
+    c->launches += 2;
+    return ESM_OK;
+}
+
 template <class real>
 int set_kc(esm_ctx *c, const double *k) {
     CK(esm::launch_set_kc<real>(c->K, k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (real *)c->kc_d, (real *)c->kc_s,
@@ -542,6 +595,10 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     if (rc) return rc;
     rc = c->precision == 64 ? alloc_state<double>(c) : alloc_state<float>(c);
     if (rc) return rc;
+    if (c->precision == 32) {  // the FP64 model and state the capacity scores are computed on
+        if ((rc = build_model<double>(c, m, o))) return rc;
+        if ((rc = alloc_shadow(c))) return rc;
+    }
     // classes
     c->ncls = c->T % 2 ? 3 : 2;
     c->class_len.assign(3, 0);
@@ -735,9 +792,10 @@ int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
         CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
                                             c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
     } else {
-        CK(esm::launch_scores<float>(c->Mf, c->d_dk, c->d_parts, c->stream));
-        CK(esm::launch_score_finish<float>(c->Mf, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
-                                           c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
+        if ((rc = widen_state(c))) return rc;
+        CK(esm::launch_scores<double>(c->Md, c->d_dk, c->d_parts, c->stream));
+        CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
+                                            c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
     }
     }
     c->launches += 2;

@@ -137,7 +137,8 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
 
 // per-lane scratch layout (reals), interleaved by lane within a warp slab
 struct LaneLayout {
-    int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua, total;
+    int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua;
+    int ut, uk, usl, ue, un, uh, ui, ucl, zr, zl, total;
 };
 __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxstu, int maxroots, int maxk, int maxku) {
     LaneLayout L;
@@ -164,6 +165,16 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
     L.kph = o; o += maxk;
     L.kv = o; o += maxk;
     L.kua = o; o += maxku;
+    L.ut = o; o += maxstu;
+    L.uk = o; o += maxstu;
+    L.usl = o; o += maxstu;
+    L.ue = o; o += 3 * maxstu;
+    L.un = o; o += maxstu;
+    L.uh = o; o += maxstu;
+    L.ui = o; o += maxstu;
+    L.ucl = o; o += maxstu;
+    L.zr = o; o += maxpts;
+    L.zl = o; o += maxpts;
     L.total = o;
     return L;
 }
@@ -182,12 +193,27 @@ struct Lane {
     const LaneLayout &LL;     // per-lane scratch layout (shared memory)
     int tau, taum, tau1, rep;
     bool active;
+    // FP32 build: the round-off scale (nats) of the last eval, 4 eps times the sum of the magnitudes of
+    // its terms (the node-balance terms of a move cancel to far less than their size)
+    mutable real nzs = 0;
 
     __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int lane_, const LaneLayout &LL_)
         : M(M_), d(d_), slab(slab_), lane(lane_), LL(LL_) {}
 
     __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * 32 + lane]; }
     __device__ inline size_t ix(int x, int t) const { return sidx(x, t, rep, M.T, M.R); }
+
+    __device__ static inline real nzacc(real v, real &A) {
+        A += fabs(v);
+        return v;
+    }
+    // append a walk point (its potential and, in FP32, the round-off scale of that potential)
+    __device__ inline void push(int pofs, int cofs, int *np, real x, real c, real z) const {
+        S(pofs, *np) = x;
+        S(cofs, *np) = c;
+        if constexpr (sizeof(real) == 4) S(pofs == LL.pr ? LL.zr : LL.zl, *np) = z;
+        ++*np;
+    }
 
     // ------------------------------------------------------------------ evaluation of the move
     // eval_move! (src/local.jl:789) of both steps (the later step first, as mv_eval! of a block
@@ -197,7 +223,7 @@ struct Lane {
         int ng = hdr[0], nse = hdr[1], nl = hdr[2], nk = hdr[3], nku = hdr[4], nns = hdr[5], nga = hdr[6],
             nna = hdr[7];
         real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
-        real D = 0;
+        real D = 0, A = 0;
         // kinks (src/local.jl:605 update_kinks!)
         for (int q = 0; q < nk; ++q) {
             real Q = S(LL.kq, q);
@@ -211,7 +237,7 @@ struct Lane {
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, tau)], t * d.ga[q], &dyc, &dex);
             real dp = A * k * dyc;
-            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.drs, d.gpos[q]) -= dp;
         }
         for (int q = 0; q < nku; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
@@ -222,13 +248,13 @@ struct Lane {
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, tau)], ak * S(LL.kph, d.kk[q]), &dyc, &dex);
             real dp = A * k * dyc;
-            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.drs, d.kupos[q]) -= dp;
         }
         for (int q = 0; q < nl; ++q) {
             int e = d.li[q];
             real df = t * d.ldf[q];
-            D += cv * dt * hinge_diff<real>(M.F[ix(e, tau)], df, M.ls[e]);
+            D += nzacc(cv * dt * hinge_diff<real>(M.F[ix(e, tau)], df, M.ls[e]), A);
             S(LL.drs, d.lpa[q]) += df;
             S(LL.drs, d.lpb[q]) -= df;
         }
@@ -236,13 +262,13 @@ struct Lane {
             int j = d.si[q];
             real k = M.kc_s[j];
             real dj, d1;
-            D += soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
-                                M.e[ix(j, tau)], M.e[ix(j, tau1)], t * d.sa[q], real(0), &dj, &d1);
+            D += nzacc(soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
+                                M.e[ix(j, tau)], M.e[ix(j, tau1)], t * d.sa[q], real(0), &dj, &d1), A);
             S(LL.drs, d.spos[q]) += dj;
             S(LL.dcs, q) = d1;
         }
         for (int q = 0; q < nns; ++q)
-            D += dt * phibal_diff<real>(M.r[ix(d.nds[q], tau)], S(LL.drs, q), M.c_shed, M.c_dump);
+            D += nzacc(dt * phibal_diff<real>(M.r[ix(d.nds[q], tau)], S(LL.drs, q), M.c_shed, M.c_dump), A);
         // ---- step tau - 1 (linked storage terms: the end value moves with step tau)
         for (int q = 0; q < nna; ++q) S(LL.dra, q) = 0;
         for (int q = 0; q < nga; ++q) {
@@ -251,20 +277,21 @@ struct Lane {
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, taum)], t * d.gaa[q], &dyc, &dex);
             real dp = A * k * dyc;
-            D += dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex;
+            D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.dra, d.gposa[q]) -= dp;
         }
         for (int q = 0; q < nse; ++q) {
             int j = d.si[q];
             real k = M.kc_s[j];
             real dj, d1;
-            D += soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
-                                M.e[ix(j, taum)], M.e[ix(j, tau)], real(0), t * d.sa[q], &dj, &d1);
+            D += nzacc(soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + k0, dt, cv,
+                                M.e[ix(j, taum)], M.e[ix(j, tau)], real(0), t * d.sa[q], &dj, &d1), A);
             S(LL.dra, d.sposa[q]) += dj;
             S(LL.dca, q) = d1;
         }
         for (int q = 0; q < nna; ++q)
-            D += dt * phibal_diff<real>(M.r[ix(d.nda[q], taum)], S(LL.dra, q), M.c_shed, M.c_dump);
+            D += nzacc(dt * phibal_diff<real>(M.r[ix(d.nda[q], taum)], S(LL.dra, q), M.c_shed, M.c_dump), A);
+        if constexpr (sizeof(real) == 4) nzs = M.beta_v * A * real(4.8e-7);
         return M.beta_v * D;
     }
 
@@ -424,9 +451,7 @@ struct Lane {
             real x = S(LL.ro, i);
             real cx = eval(x);
             if (*np >= M.maxpts) return false;
-            S(pofs, *np) = x;
-            S(cofs, *np) = cx;
-            ++*np;
+            push(pofs, cofs, np, x, cx, nzs);
             *cmin = fmin(*cmin, cx);
         }
         return true;
@@ -444,7 +469,12 @@ struct Lane {
             real t;
             if (!next_bp(tp, sgn, &t)) {
                 real cprev = *np == 0 ? real(0) : S(cofs, *np - 1);
-                real hp = real(1e-6) * fmax(real(1), fabs(tp));
+                // the probe step of walk! (1e-6 relative). In FP32 the state values y0 + t a carry
+                // an absolute round-off of ~1e-7, as large as a 1e-6 step's increment: the FP32
+                // build probes 1e-3 ahead instead. The ray points only place the discretisation
+                // (the roots inside a ray step are inserted all the same), so this changes which
+                // points are walked, not the conditional that is sampled.
+                real hp = real(sizeof(real) == 4 ? 1e-3 : 1e-6) * fmax(real(1), fabs(tp));
                 real sl = (eval(tp + sgn * hp) + real(0) - cprev - real(0)) / hp;
                 if (sl > 0)
                     delta = fmin(real(2) * M.maxnats / sl, real(1e3) * fmax(fabs(tp), real(1e-3)));
@@ -454,7 +484,7 @@ struct Lane {
                 nx += 1;
                 if (nx > 80) return 0;
             }
-            real c = eval(t);
+            real c = eval(t), zc = nzs;
             int nro = 0, ngro = 0;
             if (!collect(tp, t, sgn, stor, true, !stor, &nro, &ngro)) return -1;
             // when storage splitting applies, the other roots are found per piece below
@@ -463,13 +493,11 @@ struct Lane {
                 real a0 = tp;
                 for (int i = 0; i < ngro; ++i) {
                     real x = S(LL.gro, i);
-                    real cx = eval(x);
+                    real cx = eval(x), zx = nzs;
                     if (!piece_roots(pofs, cofs, np, a0, x, sgn, &cmin)) return -1;
                     eval(x);  // restore the secondaries at x
                     if (*np >= M.maxpts) return -1;
-                    S(pofs, *np) = x;
-                    S(cofs, *np) = cx;
-                    ++*np;
+                    push(pofs, cofs, np, x, cx, zx);
                     cmin = fmin(cmin, cx);
                     save_prev();
                     a0 = x;
@@ -489,17 +517,13 @@ struct Lane {
                         real x = S(LL.ro, i);
                         real cx = eval(x);
                         if (*np >= M.maxpts) return -1;
-                        S(pofs, *np) = x;
-                        S(cofs, *np) = cx;
-                        ++*np;
+                        push(pofs, cofs, np, x, cx, nzs);
                         cmin = fmin(cmin, cx);
                     }
                 }
             }
             if (*np >= M.maxpts) return -1;
-            S(pofs, *np) = t;
-            S(cofs, *np) = c;
-            ++*np;
+            push(pofs, cofs, np, t, c, zc);
             cmin = fmin(cmin, c);
             if (c + real(0) - cmin > M.maxnats) return 1;
             tp = t;
@@ -512,9 +536,16 @@ struct Lane {
         if (x > 0) return log(L) + log(-expm1(-x)) - log(x);
         return log(L) - x + log(-expm1(x)) - log(-x);
     }
-    __device__ static real trexp_offset(real u, real g, real L) {
+    // A segment whose potential changes by less than this many nats is drawn uniformly from its
+    // left end (trexp_offset's 1e-10). In the FP32 build the potential of a flat segment comes out
+    // as round-off -- up to ~1e-3 nats next to a node-balance kink on the steep side -- and the
+    // sign of that round-off would pick between the left and the mirrored u -> t map: it takes
+    // 1e-4, or the round-off scale of the segment's two end points if larger (the density then
+    // varies by no more than that across the segment).
+    static constexpr real flat_nats = sizeof(real) == 4 ? real(1e-4) : real(1e-10);
+    __device__ static real trexp_offset(real u, real g, real L, real flat) {
         real x = g * L;
-        if (fabs(x) < real(1e-10)) return u * L;
+        if (fabs(x) < flat) return u * L;
         if (g > 0) return -log1p(-u * (-expm1(-x))) / g;
         return L + log1p(-u * (-expm1(x))) / (-g);
     }
@@ -524,23 +555,240 @@ struct Lane {
         if (i == nl) return 0;
         return S(LL.pr, i - nl - 1);
     }
+    __device__ inline real Zz(int i, int nl) const {  // FP32 round-off scale of the merged points
+        if (i < nl) return S(LL.zl, nl - 1 - i);
+        if (i == nl) return 0;
+        return S(LL.zr, i - nl - 1);
+    }
     __device__ inline real Cc(int i, int nl) const {
         if (i < nl) return S(LL.cl, nl - 1 - i);
         if (i == nl) return 0;
         return S(LL.cr, i - nl - 1);
     }
 
+
+    // ------------------------------------------------------------ separable storage moves
+    // A move whose terms are storage units at distinct nodes and nothing else (the atoms of a
+    // state-of-charge field, 97 % of the walk work of a sweep): the line potential is a sum of
+    // one-dimensional piecewise-linear functions, one per unit, with at most ten kinks each. The
+    // walk visits the points walk! visits -- the units' clamp points (the primary breakpoints),
+    // their storage thresholds and the zero crossings of their node balances (the secondary
+    // roots) -- event by event, re-evaluating only the unit whose piece changes, and advancing the
+    // potential along the summed slopes in between.
+    __device__ bool separable() const {
+        const int *h = d.hdr;
+        return h[1] > 0 && h[0] == 0 && h[2] == 0 && h[3] == 0 && h[4] == 0 && h[6] == 0 && h[8] == 0 &&
+               h[5] == h[1] && h[7] == h[1];
+    }
+
+    // beta * (cost change) of unit q at t, with its two node balances (tau and tau - 1)
+    __device__ real unit_val(int q, real t, real *Sw, real *Sa) const {
+        int j = d.si[q];
+        real x = t * d.sa[q];
+        real k = M.kc_s[j], w = k + M.kappa0, dt = M.dt, cv = M.c_viol;
+        real djw, dw, dja, da;
+        real cw = soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
+                                 M.e[ix(j, tau)], M.e[ix(j, tau1)], x, real(0), &djw, &dw);
+        real ca = soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, w, dt, cv,
+                                 M.e[ix(j, taum)], M.e[ix(j, tau)], real(0), x, &dja, &da);
+        real S0w = M.r[ix(d.nds[d.spos[q]], tau)], S0a = M.r[ix(d.nda[d.sposa[q]], taum)];
+        *Sw = S0w + djw;
+        *Sa = S0a + dja;
+        real bw = dt * phibal_diff<real>(S0w, djw, M.c_shed, M.c_dump);
+        real ba = dt * phibal_diff<real>(S0a, dja, M.c_shed, M.c_dump);
+        return M.beta_v * (cw + bw + ca + ba);
+    }
+
+    // The piece of unit q that starts at t0: its end (the next clamp of the state of charge -- a
+    // primary breakpoint -- or the next storage threshold, both exact) and the zero crossings of
+    // its node balances inside it (linear there, so found by interpolation as piece_roots! does).
+    // Stored as an event list in walking order: times in ue[0..un), the end kind in uh (1 clamp,
+    // 2 threshold, 0 none: the piece runs to infinity).
+    __device__ void unit_piece(int q, real t0, real sgn) const {
+        int j = d.si[q];
+        real a = d.sa[q];
+        real e0 = M.e[ix(j, tau)];
+        real e1c = clampr<real>(M.e[ix(j, tau1)], 0, 1), emc = clampr<real>(M.e[ix(j, taum)], 0, 1);
+        real h = M.s_hours[j], qt = M.s_qt[j], ein = M.s_etain[j], eout = M.s_etaout[j], dt = M.dt;
+        bool have = false, prim = false;
+        real ts = 0;
+        auto cand = [&](real x, bool p) {
+            real tc = x / a;
+            if (!isfinite(tc) || !(sgn * (tc - t0) > 0)) return;
+            if (!have || sgn * (tc - ts) < 0) {
+                ts = tc;
+                prim = p;
+                have = true;
+            }
+        };
+        cand(real(0) - e0, true);
+        cand(real(1) - e0, true);
+        S(LL.ucl, q) = (have && prim) ? ts : real(INFINITY) * sgn;  // the next clamp of this unit
+        real th[3];
+        int nth = 0;
+        th[nth++] = 0;  // the sign changes of the three storage secondaries (src/local.jl:885)
+        if (ein > 0) th[nth++] = ein;
+        if (eout > 0) th[nth++] = real(-1) / eout;
+        for (int i = 0; i < nth; ++i) {
+            real xw = e1c - e0 - (th[i] + qt) * dt / h;  // d at tau crosses th
+            if (e0 + xw >= 0 && e0 + xw <= 1) cand(xw, false);
+            real xa = emc - e0 + (th[i] + qt) * dt / h;  // d of step tau - 1 crosses th
+            if (e0 + xa >= 0 && e0 + xa <= 1) cand(xa, false);
+        }
+        real tpb = have ? ts : t0 + sgn * fmax(real(1), fabs(t0));
+        real Sw0, Sa0, Sw1, Sa1;
+        unit_val(q, t0, &Sw0, &Sa0);
+        unit_val(q, tpb, &Sw1, &Sa1);
+        real r[2];
+        int nr = 0;
+        real pa[2] = {Sw0, Sa0}, pb[2] = {Sw1, Sa1};
+        for (int i = 0; i < 2; ++i) {
+            real x;
+            if (have) {
+                if (root_of(pa[i], pb[i], t0, tpb, sgn, &x)) r[nr++] = x;
+            } else if (pa[i] != pb[i]) {  // linear to infinity: the crossing anywhere ahead
+                x = t0 + (tpb - t0) * pa[i] / (pa[i] - pb[i]);
+                if (isfinite(x) && sgn * (x - t0) > 0) r[nr++] = x;
+            }
+        }
+        if (nr == 2 && sgn * (r[1] - r[0]) < 0) {
+            real x = r[0];
+            r[0] = r[1];
+            r[1] = x;
+        }
+        int n = 0;
+        for (int i = 0; i < nr; ++i) S(LL.ue + 3 * q, n++) = r[i];
+        if (have) S(LL.ue + 3 * q, n++) = ts;
+        S(LL.un, q) = real(n);
+        S(LL.uh, q) = have ? (prim ? real(1) : real(2)) : real(0);
+        S(LL.ui, q) = real(0);
+    }
+
+    // set the next event of unit q (at or after position t) and the slope of its potential to there
+    __device__ void unit_next(int q, real t, real sgn) const {
+        int i = (int)S(LL.ui, q), n = (int)S(LL.un, q), hk = (int)S(LL.uh, q);
+        real Sw, Sa;
+        real f0 = unit_val(q, t, &Sw, &Sa);
+        real tn, tprobe;
+        real kind;
+        if (i < n) {
+            tn = S(LL.ue + 3 * q, i);
+            tprobe = tn;
+            kind = (i == n - 1 && hk != 0) ? (hk == 1 ? real(1) : real(0)) : real(0);
+        } else {
+            tn = real(INFINITY) * sgn;
+            tprobe = t + sgn * fmax(real(1), fabs(t));
+            kind = real(-1);
+        }
+        real f1 = unit_val(q, tprobe, &Sw, &Sa);
+        S(LL.ut, q) = tn;
+        S(LL.uk, q) = kind;
+        S(LL.usl, q) = (f1 - f0) / (tprobe - t);
+    }
+
+    // move unit q past its current event at t: to the next event of its piece, or into the next piece
+    __device__ void unit_pass(int q, real t, real sgn) const {
+        int i = (int)S(LL.ui, q), n = (int)S(LL.un, q), hk = (int)S(LL.uh, q);
+        if (i == n - 1 && hk != 0)
+            unit_piece(q, t, sgn);
+        else
+            S(LL.ui, q) = real(i + 1);
+        unit_next(q, t, sgn);
+    }
+
+    // walk! for a separable move; same returns as walk()
+    __device__ int walk_sep(int pofs, int cofs, int *np, real sgn) const {
+        int nu = d.hdr[1];
+        double B = 0;     // summed slope of the potential at the current position
+        double absB = 0;  // the sum of the magnitudes of the units' slopes (round-off scale)
+        for (int q = 0; q < nu; ++q) {
+            unit_piece(q, real(0), sgn);
+            unit_next(q, real(0), sgn);
+            B += (double)S(LL.usl, q);
+            absB += fabs((double)S(LL.usl, q));
+        }
+        *np = 0;
+        double c = 0, cmin = 0;
+        real tcur = 0, delta = 0;
+        int nx = 0;
+        while (true) {
+            // the next primary breakpoint among the units, or a ray step beyond the last one
+            real tP = 0;
+            bool haveP = false;
+            for (int q = 0; q < nu; ++q) {
+                real tq = S(LL.ucl, q);
+                if (!isfinite(tq)) continue;
+                if (!haveP || sgn * (tq - tP) < 0) {
+                    tP = tq;
+                    haveP = true;
+                }
+            }
+            real target;
+            if (!haveP) {
+                double sl = (double)sgn * B;  // the outgoing slope at the last point (walk!'s probe)
+                if (sl > 0)
+                    delta = fmin(real(2) * M.maxnats / (real)sl, real(1e3) * fmax(fabs(tcur), real(1e-3)));
+                else
+                    delta = delta == 0 ? fmax(fabs(tcur), real(1e-6)) : real(2) * delta;
+                target = tcur + sgn * delta;
+                nx += 1;
+                if (nx > 80) return 0;
+            } else {
+                target = tP;
+            }
+            // the secondary points before the target
+            while (true) {
+                real tS = 0;
+                int qS = -1;
+                for (int q = 0; q < nu; ++q) {
+                    if (S(LL.uk, q) < 0) continue;
+                    real tq = S(LL.ut, q);
+                    if (qS < 0 || sgn * (tq - tS) < 0) {
+                        tS = tq;
+                        qS = q;
+                    }
+                }
+                if (qS < 0 || !(sgn * (target - tS) > 0)) break;
+                c += B * (double)(tS - tcur);
+                tcur = tS;
+                if (*np >= M.maxpts) return -1;
+                push(pofs, cofs, np, tS, (real)c, real(4.8e-7) * (real)(fabs(c) + absB * fabs((double)tS)));
+                cmin = fmin(cmin, c);
+                real old = S(LL.usl, qS);
+                unit_pass(qS, tS, sgn);
+                B += (double)S(LL.usl, qS) - (double)old;
+                absB = fmax(absB, absB + fabs((double)S(LL.usl, qS)) - fabs((double)old));
+            }
+            c += B * (double)(target - tcur);
+            tcur = target;
+            if (*np >= M.maxpts) return -1;
+            push(pofs, cofs, np, target, (real)c, real(4.8e-7) * (real)(fabs(c) + absB * fabs((double)target)));
+            cmin = fmin(cmin, c);
+            // every unit with an event here (its clamp, or a secondary that fell on it) moves on; a
+            // new piece starts strictly after its start, so this ends
+            for (int q = 0; q < nu; ++q)
+                while (S(LL.uk, q) >= 0 && S(LL.ut, q) == target) {
+                    real old = S(LL.usl, q);
+                    unit_pass(q, target, sgn);
+                    B += (double)S(LL.usl, q) - (double)old;
+                    absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
+                }
+            if (c - cmin > (double)M.maxnats) return 1;
+        }
+    }
+
     // sample_line! (src/local.jl:1501); *guard on buffer overflow (t = 0)
     __device__ real sample_line(real ucat, real uoff, bool *guard) const {
         *guard = false;
         int nr = 0, nl = 0;
-        int w = walk(LL.pr, LL.cr, &nr, real(1));
+        bool sep = separable();
+        int w = sep ? walk_sep(LL.pr, LL.cr, &nr, real(1)) : walk(LL.pr, LL.cr, &nr, real(1));
         if (w < 0) {
             *guard = true;
             return 0;
         }
         if (w == 0) return 0;
-        w = walk(LL.pl, LL.cl, &nl, real(-1));
+        w = sep ? walk_sep(LL.pl, LL.cl, &nl, real(-1)) : walk(LL.pl, LL.cl, &nl, real(-1));
         if (w < 0) {
             *guard = true;
             return 0;
@@ -570,7 +818,23 @@ struct Lane {
         real p0 = P(jj, nl), p1 = P(jj + 1, nl);
         real L = p1 - p0;
         real g = (Cc(jj + 1, nl) - Cc(jj, nl)) / L;
-        return (g >= 0 || fabs(g * L) < real(1e-10)) ? p0 + trexp_offset(uoff, g, L) : p1 - trexp_offset(uoff, -g, L);
+        real flat = flat_nats;
+        if constexpr (sizeof(real) == 4) {
+            // each end's round-off: that of its terms, and that of placing the point itself (a
+            // kink at x lands within ulp(x) of where it is, on either side, where the potential
+            // turns by the difference of the neighbouring slopes)
+            auto slope = [&](int j) -> real {
+                if (j < 0 || j >= nseg) return 0;
+                real Lj = P(j + 1, nl) - P(j, nl);
+                return Lj > 0 ? fabs((Cc(j + 1, nl) - Cc(j, nl)) / Lj) : real(0);
+            };
+            real gl = slope(jj - 1), gm = slope(jj), gr = slope(jj + 1);
+            real z0 = Zz(jj, nl) + real(2.4e-7) * fabs(p0) * fmax(gl, gm);
+            real z1 = Zz(jj + 1, nl) + real(2.4e-7) * fabs(p1) * fmax(gm, gr);
+            flat = fmax(flat, z0 + z1);
+        }
+        return (g >= 0 || fabs(g * L) < flat) ? p0 + trexp_offset(uoff, g, L, flat)
+                                              : p1 - trexp_offset(uoff, -g, L, flat);
     }
 
     // commit_block! / apply_step! (src/local.jl:2495, :2507)

@@ -13,6 +13,9 @@ import numpy as np
 
 from .device import EsmError, load
 
+EXPORTS = ("esm_mlp_create", "esm_mlp_destroy", "esm_mlp_last_error", "esm_mlp_set_layer", "esm_mlp_get_layer",
+           "esm_mlp_forward", "esm_mlp_train_step", "esm_mlp_launch_count")
+
 P_f32 = C.POINTER(C.c_float)
 P_f64 = C.POINTER(C.c_double)
 P_i32 = C.POINTER(C.c_int32)

@@ -8,6 +8,7 @@ import pytest
 
 from esmgb import build as B
 from esmgb import device as DV
+from esmgb import surrogate as SG
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -18,7 +19,7 @@ def declared_symbols():
 
 
 def test_header_and_binding_agree():
-    assert sorted(DV.EXPORTS) == declared_symbols()
+    assert sorted(DV.EXPORTS + SG.EXPORTS) == declared_symbols()
 
 
 def test_library_exports_all_symbols():
