@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <chrono>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -802,6 +803,75 @@ int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * c->R * c->K, cudaMemcpyDeviceToHost, c->stream));
     if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
     if (parts) CK(cudaMemcpyAsync(parts, c->d_parts, sizeof(double) * c->R * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_scores = true;
+    return ESM_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Capacity scores whose call allocates nothing. For callers that must not allocate device memory
+// in the call: a caller whose device memory is owned by a caching allocator (PyTorch's, a memory
+// pool with a hard cap) -- cudaMalloc behind its back fails or fragments once the pool holds the
+// device -- and a caller whose step must not stall, as cudaMalloc/cudaFree can synchronise the
+// device. The score accumulators (the R x K score sums and the R x 8 cost parts) live in one
+// file-scope device array instead of buffers of the context.
+//   Limit: R * (K + 8) <= ESM_SCORE_SCRATCH_DOUBLES (8 MiB); larger contexts get ESM_EINVAL.
+//   Set-up: the first call on a device, with that device current, resolves the array's address
+//   (cudaGetSymbolAddress) once; make it before any stream capture. The first call on a context
+//   also reserves that context's error-message buffer.
+//   The array is shared by every context on the device: overlapping calls (two streams, two
+//   threads, two contexts) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------------------------
+static __device__ __align__(256) double g_score_scratch[ESM_SCORE_SCRATCH_DOUBLES];
+
+namespace {
+std::mutex g_scratch_mu;
+double *g_scratch_dev[ESM_MAX_DEVICES] = {};
+
+int score_scratch(esm_ctx *c, double **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= ESM_MAX_DEVICES) return fail(c, ESM_EINVAL, "device %d beyond %d", dev, ESM_MAX_DEVICES);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_dev[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_score_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(c, ESM_ECUDA, "cudaGetSymbolAddress of the score scratch: %s", cudaGetErrorString(e));
+        g_scratch_dev[dev] = (double *)p;
+    }
+    *out = g_scratch_dev[dev];
+    return ESM_OK;
+}
+}  // namespace
+
+int esm_capacity_scores_static(esm_ctx *c, double *sk, double *fk, double *parts) {
+    if (!c) return ESM_EINVAL;
+    if (c->err.capacity() < 512) c->err.reserve(512);
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    size_t R = c->R, K = c->K, need = R * (K + 8);
+    if (need > (size_t)ESM_SCORE_SCRATCH_DOUBLES)
+        return fail(c, ESM_EINVAL, "R*(K+8) = %zu doubles of score scratch needed, the static scratch holds %d",
+                    need, ESM_SCORE_SCRATCH_DOUBLES);
+    double *dk = nullptr;
+    int rc = score_scratch(c, &dk);
+    if (rc) return rc;
+    double *pd = dk + R * K;
+    if (c->precision == 64) {
+        CK(esm::launch_rebuild<double>(c->Md, c->stream));
+    } else {
+        CK(esm::launch_rebuild<float>(c->Mf, c->stream));
+        if ((rc = widen_state(c))) return rc;
+    }
+    // the accumulators start at zero (the score kernel adds into them)
+    CK(cudaMemsetAsync(dk, 0, sizeof(double) * need, c->stream));
+    CK(esm::launch_scores<double>(c->Md, dk, pd, c->stream));
+    CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
+                                        c->physical, dk, c->d_sk, c->d_fk, pd, c->stream));
+    c->launches += 3;
+    if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * R * K, cudaMemcpyDeviceToHost, c->stream));
+    if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
+    if (parts) CK(cudaMemcpyAsync(parts, pd, sizeof(double) * R * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->has_scores = true;
     return ESM_OK;

@@ -21,7 +21,7 @@ NSTAT = 2 * (9 + 1) + 1
 EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
            "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
-           "esm_set_timing", "esm_timing", "esm_stream")
+           "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static")
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather")
 
 _lib = None
@@ -60,6 +60,7 @@ def load(build_if_missing=True):
     L.esm_operation_sweeps.argtypes = [C.c_void_p, C.c_int32, C.c_int64, P_i64]
     L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
     L.esm_capacity_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
+    L.esm_capacity_scores_static.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
     L.esm_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int32, P_f64,
                                     C.c_int64, P_f64, P_i32]
     L.esm_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64]
@@ -159,6 +160,17 @@ class DeviceChain:
         fk = np.zeros(m.Kunits)
         parts = np.zeros((R, 8))
         self._check(self.L.esm_capacity_scores(self.h, _p(sk), _p(fk), _p(parts)), "esm_capacity_scores")
+        return sk, fk, parts
+
+    def scores_static(self):
+        """esm_capacity_scores_static: the same scores, accumulated in the library's file-scope
+        device scratch (nothing is allocated in the call; overlapping calls race)."""
+        m, R = self.m, self.R
+        sk = np.zeros((R, m.Kunits))
+        fk = np.zeros(m.Kunits)
+        parts = np.zeros((R, 8))
+        self._check(self.L.esm_capacity_scores_static(self.h, _p(sk), _p(fk), _p(parts)),
+                    "esm_capacity_scores_static")
         return sk, fk, parts
 
     def langevin_step(self, w, eta, kappa_s, kmin=1.0, clip=0.02, box=True, xi=None, it=0):

@@ -160,6 +160,18 @@ int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int32_t move_limit,
    per replica: capex, op, gen, storage, shed, dump, penalty, 0 (CostParts, src/energy.jl:531). */
 int esm_capacity_scores(esm_ctx *ctx, double *sk, double *fk, double *parts);
 
+/* esm_capacity_scores without allocating in the call (no counterpart in the reference): for a
+   caller that must not allocate device memory here -- one whose device memory is held by a caching
+   allocator or a capped pool, or whose step must not stall on cudaMalloc/cudaFree. The score
+   accumulators live in a file-scope device array of ESM_SCORE_SCRATCH_DOUBLES doubles (8 MiB);
+   R*(K+8) beyond that is rejected with ESM_EINVAL. The first call on a device (with it current)
+   resolves the array's address: make it before any stream capture. The array is shared by all
+   contexts on a device, so overlapping calls race: serialise them. Same outputs and effect as
+   esm_capacity_scores (a following esm_langevin_step uses these scores). */
+#define ESM_SCORE_SCRATCH_DOUBLES (1 << 20)
+#define ESM_MAX_DEVICES 64
+int esm_capacity_scores_static(esm_ctx *ctx, double *sk, double *fk, double *parts);
+
 /* The Langevin step of the shared capacities from the replica-weighted score
    (src/replicas.jl:697 sbar = sum_j w_j sk_j; langevin_capacities :391, langevin_update :368)
    followed by the dispatch following of every replica (follow_capacities! :448:

@@ -1,0 +1,46 @@
+"""esm_capacity_scores_static (the score entry point that allocates nothing in the call) against
+esm_capacity_scores on the same state, through the C ABI, on two calls in a row; and its size
+limit. Collected last so that it also runs after every other GPU test."""
+import numpy as np
+import pytest
+
+from esmgb.device import DeviceChain, EsmError
+from esmgb.model import initial_state, make_model
+
+pytestmark = pytest.mark.gpu
+
+
+def _state(m, R, seed=3):
+    st = initial_state(m, R, seed=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    st.e = rng.uniform(0.05, 0.95, st.e.shape)
+    return st
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_static_scores_match(prec):
+    m = make_model(40, 60, 40, seed=11)
+    st = _state(m, 32)
+    d = DeviceChain(m, 32, precision=prec, seed=5)
+    d.upload(st)
+    d.sweeps(1, 0)
+    sk0, fk0, p0 = d.scores()
+    scale = np.abs(sk0).max(axis=0) + 1e-3
+    for _ in range(2):                     # two calls in a row: the scratch is cleared each time
+        sk, fk, parts = d.scores_static()
+        # the score sums are FP64 atomics in both entry points: equal up to summation order
+        assert (np.abs(sk - sk0) / scale).max() < 1e-9
+        np.testing.assert_allclose(fk, fk0, rtol=1e-14)
+        np.testing.assert_allclose(parts, p0, rtol=1e-9, atol=1e-6)
+    d.close()
+
+
+def test_static_scores_size_limit():
+    m = make_model(40, 60, 2, seed=11)
+    R = (1 << 20) // (m.Kunits + 8) + 1    # one replica beyond the static scratch
+    d = DeviceChain(m, R, precision=64, seed=5)
+    d.upload(_state(m, R))
+    with pytest.raises(EsmError, match="static scratch holds"):
+        d.scores_static()
+    d.close()
