@@ -65,6 +65,7 @@ struct esm_ctx {
     unsigned long long *d_stats = nullptr;
     int32_t *d_reg = nullptr, *d_reg2 = nullptr;
     void *d_scratch = nullptr;
+    char *d_descs = nullptr;  // the move descriptors of the current class pass
     // weather
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
     double *d_wbeta = nullptr, *d_wtheta = nullptr, *d_wxi = nullptr;
@@ -425,6 +426,10 @@ int alloc_state(esm_ctx *c) {
     size_t per = esm::linemove_scratch_reals<real>(M);
     if ((rc = dalloc(c, &q, per * (size_t)c->max_warps))) return rc;
     c->d_scratch = q;
+    // the move descriptors of a class pass
+    char *dp;
+    if ((rc = dalloc(c, &dp, esm::linemove_smem_per_warp<real>(M) * (size_t)(M.natoms + M.nextra)))) return rc;
+    c->d_descs = dp;
     return ESM_OK;
 }
 
@@ -524,11 +529,13 @@ int class_pass_any(esm_ctx *c, uint32_t sweep, int cls, int limit = 0) {
     Span sp(c, ESM_KT_CLASS);
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, limit, (double *)c->d_scratch,
-                                          c->max_warps, c->d_stats, c->stream));
+                                          c->max_warps, c->d_stats, c->d_descs, c->stream));
     else
         CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, limit, (float *)c->d_scratch,
-                                         c->max_warps, c->d_stats, c->stream));
-    c->launches += 1;
+                                         c->max_warps, c->d_stats, c->d_descs, c->stream));
+    int nmoves = c->Mf.natoms + c->Mf.nextra;
+    if (c->precision == 64) nmoves = c->Md.natoms + c->Md.nextra;
+    c->launches += 1 + (limit > 0 && limit < nmoves ? limit : nmoves);
     return ESM_OK;
 }
 

@@ -1,4 +1,4 @@
-// Host entry points of the line-move class kernel (esm_linemove.cu).
+// Host entry points of the line-move kernels (esm_linemove_impl.cuh).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -9,8 +9,11 @@ namespace esm {
 template <class real>
 size_t linemove_scratch_reals(const DevModel<real> &M);  // per warp
 template <class real>
-size_t linemove_smem_per_warp(const DevModel<real> &M);
+size_t linemove_smem_per_warp(const DevModel<real> &M);  // bytes of one move descriptor
+// one colour class: the descriptors of its moves into descs ((natoms + nextra) descriptors), then
+// one launch per move
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
-                              int limit, real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s);
+                              int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
+                              cudaStream_t s);
 }  // namespace esm

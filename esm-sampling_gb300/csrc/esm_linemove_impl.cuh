@@ -138,7 +138,7 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
 // per-lane scratch layout (reals), interleaved by lane within a warp slab
 struct LaneLayout {
     int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua;
-    int ut, uk, usl, ue, un, uh, ui, ucl, zr, zl, total;
+    int ut, uk, usl, ue, un, uh, ui, ucl, ufe, ufn, usw, usa, zr, zl, total;
 };
 __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxstu, int maxroots, int maxk, int maxku) {
     LaneLayout L;
@@ -173,6 +173,10 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
     L.uh = o; o += maxstu;
     L.ui = o; o += maxstu;
     L.ucl = o; o += maxstu;
+    L.ufe = o; o += maxstu;
+    L.ufn = o; o += maxstu;
+    L.usw = o; o += maxstu;
+    L.usa = o; o += maxstu;
     L.zr = o; o += maxpts;
     L.zl = o; o += maxpts;
     L.total = o;
@@ -218,7 +222,7 @@ struct Lane {
     // ------------------------------------------------------------------ evaluation of the move
     // eval_move! (src/local.jl:789) of both steps (the later step first, as mv_eval! of a block
     // move, :1219). Returns beta * DeltaC(t); fills d (storage) and dr (nodes) at t.
-    __device__ real eval(real t) const {
+    __device__ __noinline__ real eval(real t) const {
         const int *hdr = d.hdr;
         int ng = hdr[0], nse = hdr[1], nl = hdr[2], nk = hdr[3], nku = hdr[4], nns = hdr[5], nga = hdr[6],
             nna = hdr[7];
@@ -327,7 +331,7 @@ struct Lane {
 
     // collect sign changes between prev (at lo) and cur (at hi): storage ones into gro (if
     // storage splitting applies), the others into ro. Returns false on root-buffer overflow.
-    __device__ bool collect(real lo, real hi, real sgn, bool stor, bool want_stor, bool want_other, int *nro,
+    __device__ __noinline__ bool collect(real lo, real hi, real sgn, bool stor, bool want_stor, bool want_other, int *nro,
                             int *ngro) const {
         int nse = d.hdr[1], nns = d.hdr[5], nna = d.hdr[7];
         real x;
@@ -383,7 +387,7 @@ struct Lane {
 
     // next primary breakpoint beyond tp in walking direction (finalize!, src/local.jl:656, scanned
     // instead of sorted: the same sequence); returns false if none
-    __device__ bool next_bp(real tp, real sgn, real *out) const {
+    __device__ __noinline__ bool next_bp(real tp, real sgn, real *out) const {
         int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nk = d.hdr[3], nku = d.hdr[4], nga = d.hdr[6];
         bool have = false;
         real best = 0;
@@ -442,7 +446,7 @@ struct Lane {
     }
 
     // piece_roots! (src/local.jl:1267) between prev (at a) and cur (at b); evaluates the roots
-    __device__ bool piece_roots(int pofs, int cofs, int *np, real a, real b, real sgn, real *cmin) const {
+    __device__ __noinline__ bool piece_roots(int pofs, int cofs, int *np, real a, real b, real sgn, real *cmin) const {
         int nro = 0, ngro = 0;
         if (!collect(a, b, sgn, true, false, true, &nro, &ngro)) return false;
         if (nro == 0) return true;
@@ -458,7 +462,7 @@ struct Lane {
     }
 
     // walk! (src/local.jl:1294), plain model. Returns 1 proper, 0 improper, -1 buffer overflow.
-    __device__ int walk(int pofs, int cofs, int *np, real sgn) const {
+    __device__ __noinline__ int walk(int pofs, int cofs, int *np, real sgn) const {
         bool stor = d.hdr[1] > 0;
         real tp = 0, cmin = 0, delta = 0;
         int nx = 0;
@@ -582,7 +586,7 @@ struct Lane {
     }
 
     // beta * (cost change) of unit q at t, with its two node balances (tau and tau - 1)
-    __device__ real unit_val(int q, real t, real *Sw, real *Sa) const {
+    __device__ __noinline__ real unit_val(int q, real t, real *Sw, real *Sa) const {
         int j = d.si[q];
         real x = t * d.sa[q];
         real k = M.kc_s[j], w = k + M.kappa0, dt = M.dt, cv = M.c_viol;
@@ -599,12 +603,13 @@ struct Lane {
         return M.beta_v * (cw + bw + ca + ba);
     }
 
-    // The piece of unit q that starts at t0: its end (the next clamp of the state of charge -- a
-    // primary breakpoint -- or the next storage threshold, both exact) and the zero crossings of
-    // its node balances inside it (linear there, so found by interpolation as piece_roots! does).
-    // Stored as an event list in walking order: times in ue[0..un), the end kind in uh (1 clamp,
-    // 2 threshold, 0 none: the piece runs to infinity).
-    __device__ void unit_piece(int q, real t0, real sgn) const {
+    // The piece of unit q that starts at t0 (where its node balances are Sw0, Sa0): its end (the
+    // next clamp of the state of charge -- a primary breakpoint -- or the next storage threshold,
+    // both exact) and the zero crossings of its node balances inside it (linear there, so found
+    // by interpolation as piece_roots! does). Stored as an event list in walking order: times in
+    // ue[0..un), the end kind in uh (1 clamp, 2 threshold, 0 none: the piece runs to infinity);
+    // the unit's potential and node balances at the end (or at a probe beyond t0) in ufe, usw, usa.
+    __device__ __noinline__ void unit_piece(int q, real t0, real sgn, real Sw0, real Sa0) const {
         int j = d.si[q];
         real a = d.sa[q];
         real e0 = M.e[ix(j, tau)];
@@ -636,9 +641,10 @@ struct Lane {
             if (e0 + xa >= 0 && e0 + xa <= 1) cand(xa, false);
         }
         real tpb = have ? ts : t0 + sgn * fmax(real(1), fabs(t0));
-        real Sw0, Sa0, Sw1, Sa1;
-        unit_val(q, t0, &Sw0, &Sa0);
-        unit_val(q, tpb, &Sw1, &Sa1);
+        real Sw1, Sa1;
+        S(LL.ufe, q) = unit_val(q, tpb, &Sw1, &Sa1);
+        S(LL.usw, q) = Sw1;
+        S(LL.usa, q) = Sa1;
         real r[2];
         int nr = 0;
         real pa[2] = {Sw0, Sa0}, pb[2] = {Sw1, Sa1};
@@ -664,65 +670,72 @@ struct Lane {
         S(LL.ui, q) = real(0);
     }
 
-    // set the next event of unit q (at or after position t) and the slope of its potential to there
-    __device__ void unit_next(int q, real t, real sgn) const {
+    // the next event of unit q after its current position t (where its potential is f): time (ut,
+    // +-inf if none), kind (uk: 1 clamp, 0 secondary, -1 none), the potential there (ufn) and the
+    // slope to there (usl)
+    __device__ __noinline__ void unit_next(int q, real t, real f, real sgn) const {
         int i = (int)S(LL.ui, q), n = (int)S(LL.un, q), hk = (int)S(LL.uh, q);
-        real Sw, Sa;
-        real f0 = unit_val(q, t, &Sw, &Sa);
-        real tn, tprobe;
-        real kind;
+        real Sw, Sa, tn, fn;
         if (i < n) {
             tn = S(LL.ue + 3 * q, i);
-            tprobe = tn;
-            kind = (i == n - 1 && hk != 0) ? (hk == 1 ? real(1) : real(0)) : real(0);
-        } else {
-            tn = real(INFINITY) * sgn;
-            tprobe = t + sgn * fmax(real(1), fabs(t));
-            kind = real(-1);
+            bool end = i == n - 1 && hk != 0;
+            fn = end ? S(LL.ufe, q) : unit_val(q, tn, &Sw, &Sa);
+            S(LL.ut, q) = tn;
+            S(LL.uk, q) = end ? (hk == 1 ? real(1) : real(0)) : real(0);
+            S(LL.ufn, q) = fn;
+            S(LL.usl, q) = (fn - f) / (tn - t);
+        } else {  // linear to infinity
+            real tp = t + sgn * fmax(real(1), fabs(t));
+            fn = unit_val(q, tp, &Sw, &Sa);
+            S(LL.ut, q) = real(INFINITY) * sgn;
+            S(LL.uk, q) = real(-1);
+            S(LL.usl, q) = (fn - f) / (tp - t);
         }
-        real f1 = unit_val(q, tprobe, &Sw, &Sa);
-        S(LL.ut, q) = tn;
-        S(LL.uk, q) = kind;
-        S(LL.usl, q) = (f1 - f0) / (tprobe - t);
     }
 
     // move unit q past its current event at t: to the next event of its piece, or into the next piece
     __device__ void unit_pass(int q, real t, real sgn) const {
         int i = (int)S(LL.ui, q), n = (int)S(LL.un, q), hk = (int)S(LL.uh, q);
+        real f = S(LL.ufn, q);
         if (i == n - 1 && hk != 0)
-            unit_piece(q, t, sgn);
+            unit_piece(q, t, sgn, S(LL.usw, q), S(LL.usa, q));
         else
             S(LL.ui, q) = real(i + 1);
-        unit_next(q, t, sgn);
+        unit_next(q, t, f, sgn);
+    }
+
+    // the next clamp among the units (primary breakpoint); false if none is left
+    __device__ bool next_clamp(int nu, real sgn, real *tP) const {
+        bool have = false;
+        for (int q = 0; q < nu; ++q) {
+            real tq = S(LL.ucl, q);
+            if (!isfinite(tq)) continue;
+            if (!have || sgn * (tq - *tP) < 0) {
+                *tP = tq;
+                have = true;
+            }
+        }
+        return have;
     }
 
     // walk! for a separable move; same returns as walk()
-    __device__ int walk_sep(int pofs, int cofs, int *np, real sgn) const {
+    __device__ __noinline__ int walk_sep(int pofs, int cofs, int *np, real sgn) const {
         int nu = d.hdr[1];
         double B = 0;     // summed slope of the potential at the current position
         double absB = 0;  // the sum of the magnitudes of the units' slopes (round-off scale)
         for (int q = 0; q < nu; ++q) {
-            unit_piece(q, real(0), sgn);
-            unit_next(q, real(0), sgn);
+            unit_piece(q, real(0), sgn, M.r[ix(d.nds[d.spos[q]], tau)], M.r[ix(d.nda[d.sposa[q]], taum)]);
+            unit_next(q, real(0), real(0), sgn);
             B += (double)S(LL.usl, q);
             absB += fabs((double)S(LL.usl, q));
         }
         *np = 0;
         double c = 0, cmin = 0;
-        real tcur = 0, delta = 0;
+        real tcur = 0, delta = 0, tP = 0;
         int nx = 0;
+        bool haveP = next_clamp(nu, sgn, &tP);
         while (true) {
             // the next primary breakpoint among the units, or a ray step beyond the last one
-            real tP = 0;
-            bool haveP = false;
-            for (int q = 0; q < nu; ++q) {
-                real tq = S(LL.ucl, q);
-                if (!isfinite(tq)) continue;
-                if (!haveP || sgn * (tq - tP) < 0) {
-                    tP = tq;
-                    haveP = true;
-                }
-            }
             real target;
             if (!haveP) {
                 double sl = (double)sgn * B;  // the outgoing slope at the last point (walk!'s probe)
@@ -736,19 +749,18 @@ struct Lane {
             } else {
                 target = tP;
             }
-            // the secondary points before the target
+            // the secondary points before the target (no unit's clamp lies before it)
             while (true) {
                 real tS = 0;
                 int qS = -1;
                 for (int q = 0; q < nu; ++q) {
-                    if (S(LL.uk, q) < 0) continue;
                     real tq = S(LL.ut, q);
                     if (qS < 0 || sgn * (tq - tS) < 0) {
                         tS = tq;
                         qS = q;
                     }
                 }
-                if (qS < 0 || !(sgn * (target - tS) > 0)) break;
+                if (qS < 0 || !isfinite(tS) || !(sgn * (target - tS) > 0)) break;
                 c += B * (double)(tS - tcur);
                 tcur = tS;
                 if (*np >= M.maxpts) return -1;
@@ -773,12 +785,13 @@ struct Lane {
                     B += (double)S(LL.usl, q) - (double)old;
                     absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
                 }
+            if (haveP) haveP = next_clamp(nu, sgn, &tP);
             if (c - cmin > (double)M.maxnats) return 1;
         }
     }
 
     // sample_line! (src/local.jl:1501); *guard on buffer overflow (t = 0)
-    __device__ real sample_line(real ucat, real uoff, bool *guard) const {
+    __device__ __noinline__ real sample_line(real ucat, real uoff, bool *guard) const {
         *guard = false;
         int nr = 0, nl = 0;
         bool sep = separable();
@@ -838,7 +851,7 @@ struct Lane {
     }
 
     // commit_block! / apply_step! (src/local.jl:2495, :2507)
-    __device__ void commit(real t) const {
+    __device__ __noinline__ void commit(real t) const {
         eval(t);
         int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nku = d.hdr[4], nns = d.hdr[5], nga = d.hdr[6],
             nna = d.hdr[7], nth = d.hdr[8];
@@ -859,7 +872,7 @@ struct Lane {
 // ---------------------------------------------------------------------------------------------
 // warp-uniform move construction
 // ---------------------------------------------------------------------------------------------
-struct Stream {  // the tile stream (TAG_LIST), every lane holds the same copy
+struct Stream {  // the class stream (TAG_LIST), every lane holds the same copy
     uint64_t seed;
     uint32_t tile, cls, sweep, j;
     __device__ double next() {
@@ -878,7 +891,7 @@ struct Stream {  // the tile stream (TAG_LIST), every lane holds the same copy
 // the move list of a tile (local_sweep!, src/local.jl:1964-1974): atoms, then nextra family draws,
 // shuffled (Fisher-Yates). Encoding: atom a -> a, family f -> -(f + 1).
 template <class real>
-__device__ void build_list(const DevModel<real> &M, Desc<real> &d, Stream &st, int lane) {
+__device__ __noinline__ void build_list(const DevModel<real> &M, Desc<real> &d, Stream &st, int lane) {
     int na = M.natoms, n = na + M.nextra;
     __syncwarp();
     for (int i = lane; i < na; i += 32) d.moves[i] = i;
@@ -927,7 +940,7 @@ __device__ inline real kappa_d(const DevModel<real> &M, int j) {
 // Build the warp-uniform part of move `mv` (lane 0 writes shared memory). Returns the family
 // index for the statistics (ESM_NFAM for atoms) or -1 when the selection rejects the move.
 template <class real>
-__device__ int prep_move(const DevModel<real> &M, Desc<real> &d, Stream &st, int mv, int lane) {
+__device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, Stream &st, int mv, int lane) {
     int N = M.N;
     int *h = d.hdr;
     // every lane computes the same selection; lane 0 writes (after every lane left the last move)
@@ -1294,7 +1307,7 @@ __device__ int prep_move(const DevModel<real> &M, Desc<real> &d, Stream &st, int
 // per-lane part of the kinks (prorata!, src/local.jl:1782): Q, e, P per leak node and the
 // kinked coefficients sigma/kappa; a lane without dispatch at a node has no kink there
 template <class real>
-__device__ void lane_kinks(const Lane<real> &Ln) {
+__device__ __noinline__ void lane_kinks(const Lane<real> &Ln) {
     const DevModel<real> &M = Ln.M;
     const Desc<real> &d = Ln.d;
     int nk = d.hdr[3], nku = d.hdr[4];
@@ -1336,26 +1349,21 @@ __device__ void lane_kinks(const Lane<real> &Ln) {
 // ---------------------------------------------------------------------------------------------
 // the kernel: one colour class of one sweep
 // ---------------------------------------------------------------------------------------------
+// The move list of a colour class and the descriptor of each of its moves. The list and the
+// selection draws come from one stream per (class, sweep) (TAG_LIST with tile word 0), shared by
+// every task of the class; the selection reads only capacities and static tables, so every
+// descriptor is the same for all tasks and is built once here, by one warp, in stream order.
+// Descriptor mi goes to descs + mi * stride; its header word 12 holds the family index (-1: no move).
 template <class real>
-__global__ void __launch_bounds__(128) k_class_pass(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps, int ntile,
-                                                   int wpt, uint32_t sweep, int cls, int limit, real *scratch,
-                                                   unsigned long long *stats, size_t smem_per_warp) {
+__global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevModel<real> M, uint32_t sweep, int cls,
+                                                  int nrun, char *descs, size_t stride) {
     extern __shared__ __align__(16) char smem[];
-    __shared__ Desc<real> sdesc[4];
-    __shared__ LaneLayout sLL;
-    __shared__ unsigned long long scnt[4][2 * (ESM_NFAM + 1) + 1];
-    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ Desc<real> sd;
+    int lane = threadIdx.x;
     int nmoves = M.natoms + M.nextra;
-    if (lane == 0) sdesc[wib] = carve_desc<real>(smem + wib * smem_per_warp, M, nmoves);
-    if (threadIdx.x == 0) sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
-    for (int i = lane; i < 2 * (ESM_NFAM + 1) + 1; i += 32) scnt[wib][i] = 0;
-    __syncthreads();
-    Desc<real> &d = sdesc[wib];
-    const LaneLayout &LL = sLL;
-    int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-    int nw = gridDim.x * (blockDim.x >> 5);
-    real *slab = scratch + (size_t)gw * LL.total * 32;
-    // zero the dense marks once
+    if (lane == 0) sd = carve_desc<real>(smem, M, nmoves);
+    __syncwarp();
+    Desc<real> &d = sd;
     for (int i = lane; i < M.N; i += 32) {
         d.dth[i] = 0;
         d.nmarks[i] = 0;
@@ -1363,57 +1371,96 @@ __global__ void __launch_bounds__(128) k_class_pass(const __grid_constant__ DevM
     }
     for (int i = lane; i < M.L; i += 32) d.lmark[i] = 0;
     __syncwarp();
+    Stream st{M.seed, 0u, (uint32_t)cls, sweep, 0u};
+    build_list(M, d, st, lane);
+    for (int mi = 0; mi < nrun; ++mi) {
+        int fi = prep_move(M, d, st, d.moves[mi], lane);
+        if (lane == 0) d.hdr[12] = fi;
+        __syncwarp();
+        const int4 *src = (const int4 *)smem;
+        int4 *dst = (int4 *)(descs + (size_t)mi * stride);
+        for (size_t i = lane; i < stride / 16; i += 32) dst[i] = src[i];
+        __syncwarp();
+    }
+}
+
+// Move mi of the class (its descriptor built by k_prep_moves) for every (step, replica) task: a
+// warp owns 32 tasks of a tile (span consecutive steps x replicas, replica fastest), each lane
+// walks and samples its own line conditional. One launch per move keeps every warp of the grid
+// in the same code.
+template <class real>
+__global__ void __launch_bounds__(128) k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps,
+                                             int ntile, int wpt, uint32_t sweep, int mi, const char *descs,
+                                             size_t stride, real *scratch, unsigned long long *stats) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ Desc<real> sd;
+    __shared__ LaneLayout sLL;
+    __shared__ unsigned long long scnt[2 * (ESM_NFAM + 1) + 1];
+    const int nst = 2 * (ESM_NFAM + 1) + 1;
+    {
+        const int4 *src = (const int4 *)(descs + (size_t)mi * stride);
+        int4 *dst = (int4 *)smem;
+        for (size_t i = threadIdx.x; i < stride / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    if (threadIdx.x == 0) {
+        sd = carve_desc<real>(smem, M, M.natoms + M.nextra);
+        sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    }
+    for (int i = threadIdx.x; i < nst; i += blockDim.x) scnt[i] = 0;
+    __syncthreads();
+    Desc<real> &d = sd;
+    const LaneLayout &LL = sLL;
+    int fi = d.hdr[12];
+    if (fi < 0) return;  // not a valid move: nothing to do (block-uniform)
+    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+    int nw = gridDim.x * (blockDim.x >> 5);
+    real *slab = scratch + (size_t)gw * LL.total * 32;
     Lane<real> Ln(M, d, slab, lane, LL);
+    unsigned long long tried = 0, moved = 0, guards = 0;
     for (int item = gw; item < ntile * wpt; item += nw) {
         int tile = item / wpt, grp = item % wpt;
         int task = grp * 32 + lane;
         int sit = task / M.R;
         Ln.rep = task % M.R;
         int q = tile * M.span + sit;
-        Ln.active = sit < M.span && q < nsteps;
+        if (!(sit < M.span && q < nsteps)) continue;
         int T = M.T;
-        Ln.tau = Ln.active ? steps[q] : 0;
+        Ln.tau = steps[q];
         Ln.taum = (Ln.tau - 1 + T) % T;
         Ln.tau1 = (Ln.tau + 1) % T;
-        Stream st{M.seed, (uint32_t)tile, (uint32_t)cls, sweep, 0u};
-        build_list(M, d, st, lane);
-        int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
-        for (int mi = 0; mi < nrun; ++mi) {
-            int fi = prep_move(M, d, st, d.moves[mi], lane);
-            if (fi < 0) continue;
-            if (!Ln.active) continue;
-            lane_kinks(Ln);
-            double uc, uo, uj, un;
-            uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
-            bool guard;
-            real t = Ln.sample_line((real)uc, (real)uo, &guard);
-            if (guard) atomicAdd(&scnt[wib][2 * (ESM_NFAM + 1)], 1ull);
-            if (fi == ESM_FAM_XLOCC && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
-                int nk = d.hdr[3];
-                bool any = false;
-                real lj = 0;
-                for (int k = 0; k < nk; ++k) {
-                    if (Ln.S(LL.kv, k) == 0) continue;
-                    any = true;
-                    real Q = Ln.S(LL.kq, k);
-                    lj += Ln.S(LL.knm, k) *
-                          log(fabs((fmax(Q + d.kg[k] * t, real(0)) + Ln.S(LL.ke, k)) / Ln.S(LL.kp, k)));
-                }
-                if (any) {
-                    uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep,
-                             &uj, &un);
-                    if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
-                }
+        lane_kinks(Ln);
+        double uc, uo, uj, un;
+        uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
+        bool guard;
+        real t = Ln.sample_line((real)uc, (real)uo, &guard);
+        if (guard) ++guards;
+        if (fi == ESM_FAM_XLOCC && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
+            int nk = d.hdr[3];
+            bool any = false;
+            real lj = 0;
+            for (int k = 0; k < nk; ++k) {
+                if (Ln.S(LL.kv, k) == 0) continue;
+                any = true;
+                real Q = Ln.S(LL.kq, k);
+                lj += Ln.S(LL.knm, k) * log(fabs((fmax(Q + d.kg[k] * t, real(0)) + Ln.S(LL.ke, k)) / Ln.S(LL.kp, k)));
             }
-            if (t != 0) Ln.commit(t);
-            atomicAdd(&scnt[wib][2 * fi], 1ull);
-            if (t != 0) atomicAdd(&scnt[wib][2 * fi + 1], 1ull);
+            if (any) {
+                uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uj,
+                         &un);
+                if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+            }
         }
-        __syncwarp();
+        if (t != 0) Ln.commit(t);
+        ++tried;
+        if (t != 0) ++moved;
     }
-    __syncwarp();
-    for (int i = lane; i < 2 * (ESM_NFAM + 1) + 1; i += 32)
-        if (scnt[wib][i]) atomicAdd(&stats[i], scnt[wib][i]);
+    if (tried) atomicAdd(&scnt[2 * fi], tried);
+    if (moved) atomicAdd(&scnt[2 * fi + 1], moved);
+    if (guards) atomicAdd(&scnt[2 * (ESM_NFAM + 1)], guards);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nst; i += blockDim.x)
+        if (scnt[i]) atomicAdd(&stats[i], scnt[i]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1425,6 +1472,7 @@ size_t linemove_scratch_reals(const DevModel<real> &M) {
     return (size_t)LL.total * 32;
 }
 
+// bytes of one move descriptor (the per-move buffer stride and the dynamic shared memory of k_move)
 template <class real>
 size_t linemove_smem_per_warp(const DevModel<real> &M) {
     return (desc_bytes(M, M.natoms + M.nextra) + 15) & ~(size_t)15;
@@ -1432,23 +1480,31 @@ size_t linemove_smem_per_warp(const DevModel<real> &M) {
 
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
-                              int limit, real *scratch, int max_warps, unsigned long long *stats, cudaStream_t s) {
+                              int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
+                              cudaStream_t s) {
+    int nmoves = M.natoms + M.nextra;
+    int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
+    size_t stride = linemove_smem_per_warp(M);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_prep_moves<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_prep_moves<real><<<1, 32, stride, s>>>(M, sweep, cls, nrun, descs, stride);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     int ntile = (nsteps + M.span - 1) / M.span;
     int wpt = (M.span * M.R + 31) / 32;
     int items = ntile * wpt;
     int nwarps = items < max_warps ? items : max_warps;
-    int wpb = 4;
-    int blocks = (nwarps + wpb - 1) / wpb;
-    size_t spw = linemove_smem_per_warp(M);
-    size_t smem = spw * wpb;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_class_pass<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    int blocks = (nwarps + 3) / 4;
+    for (int mi = 0; mi < nrun; ++mi) {
+        k_move<real><<<blocks, 128, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
+                                                  stats);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    k_class_pass<real><<<blocks, wpb * 32, smem, s>>>(M, steps, nsteps, ntile, wpt, sweep, cls, limit, scratch, stats,
-                                                      spw);
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 }  // namespace esm

@@ -943,19 +943,20 @@ static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthr
     int ntile = ((int)steps.size() + span - 1) / span;
     int R = c.o.R;
     int nst = 2 * (ESM_NFAM + 1) + 1;
+    // one move list per (class, sweep), shared by every task of the class (the stream's tile word is 0)
+    TileStream ts0{c.o.seed, 0u, (uint32_t)cls, sweep};
+    vector<MoveRef> moves;
+    move_list(c, ts0, moves);
 #pragma omp parallel num_threads(nthreads)
     {
         vector<int64_t> loc(nst, 0);
         WS ws, wa;
         ws.init(c.m);
         wa.init(c.m);
-        vector<MoveRef> moves;
 #pragma omp for schedule(dynamic, 1)
         for (int tile = 0; tile < ntile; ++tile) {
-            TileStream ts{c.o.seed, (uint32_t)tile, (uint32_t)cls, sweep};
-            move_list(c, ts, moves);
             for (int q = tile * span; q < std::min((int)steps.size(), (tile + 1) * span); ++q)
-                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts, steps[q], rep, sweep, loc.data(), ws, wa, limit);
+                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts0, steps[q], rep, sweep, loc.data(), ws, wa, limit);
         }
 #pragma omp critical
         for (int i = 0; i < nst; ++i) stats[i] += loc[i];
@@ -1594,7 +1595,8 @@ void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
 // the move list of a tile (diagnostics): kind (-1 atom, else family), field, atom
 int orc_move_list(void *p, int64_t sweep, int cls, int tile, int *kinds, int *fields, int *atoms, int maxn) {
     Ctx *c = (Ctx *)p;
-    TileStream ts{c->o.seed, (uint32_t)tile, (uint32_t)cls, (uint32_t)sweep};
+    (void)tile;  // the list is shared by all tiles of the class
+    TileStream ts{c->o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
     vector<MoveRef> moves;
     move_list(*c, ts, moves);
     int n = (int)moves.size() < maxn ? (int)moves.size() : maxn;
