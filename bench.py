@@ -321,8 +321,9 @@ def main():
     e2e = world * args.steps / e2e_wall
     if rank != 0:
         return
-    # roofline of the dominant kernel (the line-move class pass): algorithmic bytes of one launch =
-    # the compulsory FP32 state traffic of one colour class, 4 (11 N + 2 L) (T/2) R bytes
+    # roofline of the dominant kernels (one colour class: k_prep_moves and one k_move launch per
+    # move, timed together as one span): algorithmic bytes of one class pass = the compulsory FP32
+    # state traffic of one colour class, 4 (11 N + 2 L) (T/2) R bytes
     N, L, T = m.N, m.L, m.T
     cls_ms, cls_n = kt["class_pass"]
     alg = 4 * (11 * N + 2 * L) * (T / 2) * R
@@ -343,7 +344,7 @@ def main():
             "config": config_dict(),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": kind,
-                         "kernel": "k_class_pass (line moves of one colour class)",
+                         "kernel": "k_prep_moves + k_move (the line moves of one colour class, one span)",
                          "note": "the exact line sampler is FP32-issue-bound; the HBM bytes are the compulsory state"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "clocks": clocks,

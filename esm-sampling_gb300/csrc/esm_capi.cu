@@ -66,6 +66,7 @@ struct esm_ctx {
     int32_t *d_reg = nullptr, *d_reg2 = nullptr;
     void *d_scratch = nullptr;
     char *d_descs = nullptr;  // the move descriptors of the current class pass
+    unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
     // weather
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
     double *d_wbeta = nullptr, *d_wtheta = nullptr, *d_wxi = nullptr;
@@ -422,7 +423,7 @@ int alloc_state(esm_ctx *c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    c->max_warps = std::max(4, nsm * 16);
+    c->max_warps = std::max(4, nsm * esm::linemove_blocks_per_sm<real>(M));
     size_t per = esm::linemove_scratch_reals<real>(M);
     if ((rc = dalloc(c, &q, per * (size_t)c->max_warps))) return rc;
     c->d_scratch = q;
@@ -430,6 +431,9 @@ int alloc_state(esm_ctx *c) {
     char *dp;
     if ((rc = dalloc(c, &dp, esm::linemove_smem_per_warp<real>(M) * (size_t)(M.natoms + M.nextra)))) return rc;
     c->d_descs = dp;
+    unsigned int *ctr;
+    if ((rc = dalloc(c, &ctr, (size_t)(M.natoms + M.nextra)))) return rc;
+    c->d_item_ctr = ctr;
     return ESM_OK;
 }
 
@@ -529,10 +533,10 @@ int class_pass_any(esm_ctx *c, uint32_t sweep, int cls, int limit = 0) {
     Span sp(c, ESM_KT_CLASS);
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, limit, (double *)c->d_scratch,
-                                          c->max_warps, c->d_stats, c->d_descs, c->stream));
+                                          c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
     else
         CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, limit, (float *)c->d_scratch,
-                                         c->max_warps, c->d_stats, c->d_descs, c->stream));
+                                         c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
     int nmoves = c->Mf.natoms + c->Mf.nextra;
     if (c->precision == 64) nmoves = c->Md.natoms + c->Md.nextra;
     c->launches += 1 + (limit > 0 && limit < nmoves ? limit : nmoves);

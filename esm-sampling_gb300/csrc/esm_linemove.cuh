@@ -15,5 +15,8 @@ size_t linemove_smem_per_warp(const DevModel<real> &M);  // bytes of one move de
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
                               int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
-                              cudaStream_t s);
+                              unsigned int *counters, cudaStream_t s);
+// resident k_move warps per SM (one warp per block)
+template <class real>
+int linemove_blocks_per_sm(const DevModel<real> &M);
 }  // namespace esm

@@ -704,18 +704,41 @@ struct Lane {
         unit_next(q, t, f, sgn);
     }
 
-    // the next clamp among the units (primary breakpoint); false if none is left
-    __device__ bool next_clamp(int nu, real sgn, real *tP) const {
-        bool have = false;
-        for (int q = 0; q < nu; ++q) {
-            real tq = S(LL.ucl, q);
-            if (!isfinite(tq)) continue;
-            if (!have || sgn * (tq - *tP) < 0) {
-                *tP = tq;
-                have = true;
+    // the first minimum in walking order of S(off, 0..n) and its index (-1 if n = 0). The loads
+    // go out eight at a time: one scan costs about one memory latency, not n of them.
+    __device__ inline int scan_min(int off, int n, real sgn, real *vmin) const {
+        int qb = -1;
+        real vb = 0;
+        int q = 0;
+        for (; q + 8 <= n; q += 8) {
+            real v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = S(off, q + i);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (qb < 0 || sgn * (v[i] - vb) < 0) {
+                    vb = v[i];
+                    qb = q + i;
+                }
+        }
+        for (; q < n; ++q) {
+            real v = S(off, q);
+            if (qb < 0 || sgn * (v - vb) < 0) {
+                vb = v;
+                qb = q;
             }
         }
-        return have;
+        *vmin = vb;
+        return qb;
+    }
+
+    // the next clamp among the units (primary breakpoint); false if none is left
+    __device__ bool next_clamp(int nu, real sgn, real *tP) const {
+        real v;
+        int q = scan_min(LL.ucl, nu, sgn, &v);
+        if (q < 0 || !isfinite(v)) return false;
+        *tP = v;
+        return true;
     }
 
     // walk! for a separable move; same returns as walk()
@@ -752,14 +775,7 @@ struct Lane {
             // the secondary points before the target (no unit's clamp lies before it)
             while (true) {
                 real tS = 0;
-                int qS = -1;
-                for (int q = 0; q < nu; ++q) {
-                    real tq = S(LL.ut, q);
-                    if (qS < 0 || sgn * (tq - tS) < 0) {
-                        tS = tq;
-                        qS = q;
-                    }
-                }
+                int qS = scan_min(LL.ut, nu, sgn, &tS);
                 if (qS < 0 || !isfinite(tS) || !(sgn * (target - tS) > 0)) break;
                 c += B * (double)(tS - tcur);
                 tcur = tS;
@@ -778,13 +794,21 @@ struct Lane {
             cmin = fmin(cmin, c);
             // every unit with an event here (its clamp, or a secondary that fell on it) moves on; a
             // new piece starts strictly after its start, so this ends
-            for (int q = 0; q < nu; ++q)
-                while (S(LL.uk, q) >= 0 && S(LL.ut, q) == target) {
-                    real old = S(LL.usl, q);
-                    unit_pass(q, target, sgn);
-                    B += (double)S(LL.usl, q) - (double)old;
-                    absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
+            for (int q0 = 0; q0 < nu; q0 += 8) {
+                real v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = q0 + i < nu ? S(LL.ut, q0 + i) : real(0);
+                for (int i = 0; i < 8 && q0 + i < nu; ++i) {
+                    if (v[i] != target) continue;  // (a finite event time: uk >= 0)
+                    int q = q0 + i;
+                    while (S(LL.ut, q) == target) {
+                        real old = S(LL.usl, q);
+                        unit_pass(q, target, sgn);
+                        B += (double)S(LL.usl, q) - (double)old;
+                        absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
+                    }
                 }
+            }
             if (haveP) haveP = next_clamp(nu, sgn, &tP);
             if (c - cmin > (double)M.maxnats) return 1;
         }
@@ -1384,41 +1408,44 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
     }
 }
 
-// Move mi of the class (its descriptor built by k_prep_moves) for every (step, replica) task: a
-// warp owns 32 tasks of a tile (span consecutive steps x replicas, replica fastest), each lane
-// walks and samples its own line conditional. One launch per move keeps every warp of the grid
-// in the same code.
+// Move mi of the class (its descriptor built by k_prep_moves) for every (step, replica) task. One
+// warp per block: a warp copies the descriptor to its shared memory, then takes items (32 tasks of
+// a tile: span consecutive steps x replicas, replica fastest) from a per-move counter until none
+// is left, and each lane walks and samples its own line conditional. One launch per move keeps
+// every warp of the grid in the same code; taking items one at a time balances the warps, whose
+// walks differ in length.
 template <class real>
-__global__ void __launch_bounds__(128) k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps,
-                                             int ntile, int wpt, uint32_t sweep, int mi, const char *descs,
-                                             size_t stride, real *scratch, unsigned long long *stats) {
+__global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps,
+                                            int ntile, int wpt, uint32_t sweep, int mi, const char *descs,
+                                            size_t stride, real *scratch, unsigned long long *stats,
+                                            unsigned int *next_item) {
     extern __shared__ __align__(16) char smem[];
     __shared__ Desc<real> sd;
     __shared__ LaneLayout sLL;
-    __shared__ unsigned long long scnt[2 * (ESM_NFAM + 1) + 1];
-    const int nst = 2 * (ESM_NFAM + 1) + 1;
+    int lane = threadIdx.x;
     {
         const int4 *src = (const int4 *)(descs + (size_t)mi * stride);
         int4 *dst = (int4 *)smem;
-        for (size_t i = threadIdx.x; i < stride / 16; i += blockDim.x) dst[i] = src[i];
+        for (size_t i = lane; i < stride / 16; i += 32) dst[i] = src[i];
     }
-    if (threadIdx.x == 0) {
+    if (lane == 0) {
         sd = carve_desc<real>(smem, M, M.natoms + M.nextra);
         sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
     }
-    for (int i = threadIdx.x; i < nst; i += blockDim.x) scnt[i] = 0;
-    __syncthreads();
+    __syncwarp();
     Desc<real> &d = sd;
     const LaneLayout &LL = sLL;
     int fi = d.hdr[12];
-    if (fi < 0) return;  // not a valid move: nothing to do (block-uniform)
-    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-    int nw = gridDim.x * (blockDim.x >> 5);
-    real *slab = scratch + (size_t)gw * LL.total * 32;
+    if (fi < 0) return;  // not a valid move: nothing to do (grid-uniform)
+    real *slab = scratch + (size_t)blockIdx.x * LL.total * 32;
     Lane<real> Ln(M, d, slab, lane, LL);
     unsigned long long tried = 0, moved = 0, guards = 0;
-    for (int item = gw; item < ntile * wpt; item += nw) {
+    int nitems = ntile * wpt;
+    while (true) {
+        unsigned int it = 0;
+        if (lane == 0) it = atomicAdd(next_item, 1u);
+        int item = (int)__shfl_sync(0xffffffffu, it, 0);
+        if (item >= nitems) break;
         int tile = item / wpt, grp = item % wpt;
         int task = grp * 32 + lane;
         int sit = task / M.R;
@@ -1455,12 +1482,17 @@ __global__ void __launch_bounds__(128) k_move(const __grid_constant__ DevModel<r
         ++tried;
         if (t != 0) ++moved;
     }
-    if (tried) atomicAdd(&scnt[2 * fi], tried);
-    if (moved) atomicAdd(&scnt[2 * fi + 1], moved);
-    if (guards) atomicAdd(&scnt[2 * (ESM_NFAM + 1)], guards);
-    __syncthreads();
-    for (int i = threadIdx.x; i < nst; i += blockDim.x)
-        if (scnt[i]) atomicAdd(&stats[i], scnt[i]);
+    // per-warp counts (tasks tried / moved, guard events) into the class totals
+    for (int o = 16; o > 0; o >>= 1) {
+        tried += __shfl_xor_sync(0xffffffffu, tried, o);
+        moved += __shfl_xor_sync(0xffffffffu, moved, o);
+        guards += __shfl_xor_sync(0xffffffffu, guards, o);
+    }
+    if (lane == 0) {
+        if (tried) atomicAdd(&stats[2 * fi], tried);
+        if (moved) atomicAdd(&stats[2 * fi + 1], moved);
+        if (guards) atomicAdd(&stats[2 * (ESM_NFAM + 1)], guards);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1478,10 +1510,20 @@ size_t linemove_smem_per_warp(const DevModel<real> &M) {
     return (desc_bytes(M, M.natoms + M.nextra) + 15) & ~(size_t)15;
 }
 
+// warps of k_move resident per SM (one warp per block), for the scratch slabs of a context
+template <class real>
+int linemove_blocks_per_sm(const DevModel<real> &M) {
+    int nb = 0;
+    size_t stride = linemove_smem_per_warp(M);
+    cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real>, 32, stride) != cudaSuccess || nb < 1) nb = 16;
+    return nb;
+}
+
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
                               int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
-                              cudaStream_t s) {
+                              unsigned int *counters, cudaStream_t s) {
     int nmoves = M.natoms + M.nextra;
     int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
     size_t stride = linemove_smem_per_warp(M);
@@ -1491,17 +1533,17 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
         cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_prep_moves<real><<<1, 32, stride, s>>>(M, sweep, cls, nrun, descs, stride);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(unsigned int) * nrun, s);
     if (e != cudaSuccess) return e;
+    k_prep_moves<real><<<1, 32, stride, s>>>(M, sweep, cls, nrun, descs, stride);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     int ntile = (nsteps + M.span - 1) / M.span;
     int wpt = (M.span * M.R + 31) / 32;
     int items = ntile * wpt;
-    int nwarps = items < max_warps ? items : max_warps;
-    int blocks = (nwarps + 3) / 4;
+    int warps = items < max_warps ? items : max_warps;
     for (int mi = 0; mi < nrun; ++mi) {
-        k_move<real><<<blocks, 128, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
-                                                  stats);
+        k_move<real><<<warps, 32, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch, stats,
+                                               counters + mi);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
