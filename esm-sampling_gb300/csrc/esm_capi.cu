@@ -36,6 +36,13 @@ struct DevBuf {
 
 }  // namespace
 
+// device buffers of esm_state_save
+struct esm_snap {
+    void *theta = nullptr, *g = nullptr, *e = nullptr, *z = nullptr;
+    int32_t *reg = nullptr;
+    double *k = nullptr;
+};
+
 struct esm_ctx {
     int precision = 32;
     int R = 0;
@@ -66,6 +73,9 @@ struct esm_ctx {
     int32_t *d_reg = nullptr, *d_reg2 = nullptr;
     void *d_scratch = nullptr;
     char *d_descs = nullptr;  // the move descriptors of the current class pass
+    esm_snap *snap = nullptr;  // esm_state_save buffers (device memory in allocs)
+    bool has_snap = false;
+    unsigned long long *d_occ = nullptr;
     unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
     // weather
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
@@ -698,6 +708,7 @@ int esm_destroy(esm_ctx *c) {
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     for (void *p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
+    delete c->snap;
     delete c;
     return ESM_OK;
 }
@@ -819,6 +830,39 @@ int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
     return ESM_OK;
 }
 
+// follow_capacities! (src/replicas.jl:448) from d_k to d_knew: the dispatchable units at fixed
+// output, rebuild, the kop curve, rebuild; d_k becomes the followed capacities
+int follow_any(esm_ctx *c, double kappa_min) {
+    int K = c->K, rc;
+    {
+    Span sp(c, ESM_KT_LANGEVIN);
+    CK(cudaMemcpyAsync(c->d_kold, c->d_k, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->precision == 64)
+        CK(esm::launch_follow_disp<double>(c->Md, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
+    else
+        CK(esm::launch_follow_disp<float>(c->Mf, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
+    k_mix<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, c->d_kmid);
+    CK(cudaGetLastError());
+    }
+    if ((rc = set_kc_any(c, c->d_kmid))) return rc;
+    if ((rc = rebuild_any(c))) return rc;
+    {
+    Span sp(c, ESM_KT_LANGEVIN);
+    esm::k_kop_capacity<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, kappa_min,
+                                                                 c->d_k1);
+    CK(cudaGetLastError());
+    if (c->precision == 64)
+        CK(esm::launch_kop<double>(c->Md, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
+    else
+        CK(esm::launch_kop<float>(c->Mf, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
+    }
+    CK(cudaMemcpyAsync(c->d_k, c->d_k1, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = set_kc_any(c, c->d_k))) return rc;
+    if ((rc = rebuild_any(c))) return rc;
+    c->launches += 4;
+    return ESM_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Capacity scores whose call allocates nothing. For callers that must not allocate device memory
 // in the call: a caller whose device memory is owned by a caching allocator (PyTorch's, a memory
@@ -908,30 +952,8 @@ int esm_langevin_step(esm_ctx *c, const double *w, const double *eta, const doub
                                                             c->d_hi, xi ? c->d_xi : nullptr, c->seed, (uint32_t)it,
                                                             c->d_knew, c->d_nclip);
     CK(cudaGetLastError());
-    // follow_capacities! (src/replicas.jl:448): dispatchable at fixed output, rebuild, kop curve, rebuild
-    if (c->precision == 64)
-        CK(esm::launch_follow_disp<double>(c->Md, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
-    else
-        CK(esm::launch_follow_disp<float>(c->Mf, c->d_disp, c->d_kold, c->d_knew, c->d_lo, c->d_hi, c->stream));
-    k_mix<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, c->d_kmid);
-    CK(cudaGetLastError());
     }
-    if ((rc = set_kc_any(c, c->d_kmid))) return rc;
-    if ((rc = rebuild_any(c))) return rc;
-    {
-    Span sp(c, ESM_KT_LANGEVIN);
-    esm::k_kop_capacity<<<(K + 127) / 128, 128, 0, c->stream>>>(K, c->d_ukind, c->d_kold, c->d_knew, kappa_min,
-                                                                 c->d_k1);
-    CK(cudaGetLastError());
-    if (c->precision == 64)
-        CK(esm::launch_kop<double>(c->Md, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
-    else
-        CK(esm::launch_kop<float>(c->Mf, c->d_kold, c->d_k1, c->d_lo, c->d_hi, kappa_min, c->stream));
-    }
-    CK(cudaMemcpyAsync(c->d_k, c->d_k1, sizeof(double) * K, cudaMemcpyDeviceToDevice, c->stream));
-    if ((rc = set_kc_any(c, c->d_k))) return rc;
-    if ((rc = rebuild_any(c))) return rc;
-    c->launches += 5;
+    if ((rc = follow_any(c, kappa_min))) return rc;
     if (knew_out) CK(cudaMemcpyAsync(knew_out, c->d_k, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
     int nclip = 0;
     CK(cudaMemcpyAsync(&nclip, c->d_nclip, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1064,3 +1086,113 @@ int esm_timing(esm_ctx *c, double *out) {
 void *esm_stream(esm_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// delayed-acceptance support: capacities set to given values (with following), state snapshots,
+// regime occupancy
+// ---------------------------------------------------------------------------------------------
+int esm_follow_capacities(esm_ctx *c, const double *knew, double kappa_min, double *k_out) {
+    if (!c || !knew) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    CK(cudaMemcpyAsync(c->d_knew, knew, sizeof(double) * c->K, cudaMemcpyHostToDevice, c->stream));
+    int rc = follow_any(c, kappa_min);
+    if (rc) return rc;
+    if (k_out) CK(cudaMemcpyAsync(k_out, c->d_k, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_scores = false;
+    return ESM_OK;
+}
+
+namespace {
+size_t state_bytes(const esm_ctx *c, int which) {
+    size_t TR = (size_t)c->T * c->R, w = c->precision == 64 ? 8 : 4;
+    switch (which) {
+        case 0: return w * c->N * TR;
+        case 1: return w * c->D * TR;
+        case 2: return w * c->S * TR;
+        default: return w * c->n0 * TR;
+    }
+}
+int snap_copy(esm_ctx *c, bool save) {
+    esm_snap &sn = *c->snap;
+    void *live[4] = {c->theta, c->g, c->e, c->z};
+    void *back[4] = {sn.theta, sn.g, sn.e, sn.z};
+    for (int i = 0; i < 4; ++i) {
+        size_t n = state_bytes(c, i);
+        if (n) CK(cudaMemcpyAsync(save ? back[i] : live[i], save ? live[i] : back[i], n, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    }
+    size_t TR = (size_t)c->T * c->R;
+    CK(cudaMemcpyAsync(save ? sn.reg : c->d_reg, save ? c->d_reg : sn.reg, sizeof(int32_t) * TR,
+                       cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(save ? sn.k : c->d_k, save ? c->d_k : sn.k, sizeof(double) * c->K, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    return ESM_OK;
+}
+}  // namespace
+
+int esm_state_save(esm_ctx *c) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    int rc;
+    if (!c->snap) {
+        esm_snap *sn = new esm_snap();
+        c->snap = sn;
+        char *p;
+        for (int i = 0; i < 4; ++i) {
+            if ((rc = dalloc(c, &p, std::max<size_t>(state_bytes(c, i), 1)))) return rc;
+            (i == 0 ? sn->theta : i == 1 ? sn->g : i == 2 ? sn->e : sn->z) = p;
+        }
+        if ((rc = dalloc(c, &sn->reg, (size_t)c->T * c->R))) return rc;
+        if ((rc = dalloc(c, &sn->k, (size_t)c->K))) return rc;
+    }
+    if ((rc = snap_copy(c, true))) return rc;
+    c->has_snap = true;
+    return ESM_OK;
+}
+
+int esm_state_restore(esm_ctx *c) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_snap) return fail(c, ESM_ESTATE, "no saved state");
+    int rc = snap_copy(c, false);
+    if (rc) return rc;
+    if ((rc = set_kc_any(c, c->d_k))) return rc;
+    if ((rc = rebuild_any(c))) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_scores = false;
+    return ESM_OK;
+}
+
+namespace {
+// occupancy of (regime, season) over the steps and replicas: season of 0-based step t with steps
+// of h hours, season (src/weather.jl:50) on the 1-based step
+__global__ void k_occupancy(int T, int R, int nreg, double h, const int32_t *reg, unsigned long long *cnt) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= (size_t)T * R) return;
+    int t = (int)(i / R);
+    long day = (long)((double)t * h / 24.0) + 1;
+    int sea = (day >= 335 || day <= 59) ? 0 : day <= 151 ? 1 : day <= 243 ? 2 : 3;
+    int k = reg[i];
+    if (k >= 0 && k < nreg) atomicAdd(&cnt[k * 4 + sea], 1ull);
+}
+}  // namespace
+
+int esm_regime_occupancy(esm_ctx *c, double *occ) {
+    if (!c || !occ) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    int n = c->nreg * 4;
+    if (!c->d_occ) {
+        int rc = dalloc(c, &c->d_occ, (size_t)n);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(c->d_occ, 0, sizeof(unsigned long long) * n, c->stream));
+    size_t TR = (size_t)c->T * c->R;
+    k_occupancy<<<(unsigned)((TR + 255) / 256), 256, 0, c->stream>>>(c->T, c->R, c->nreg, c->dt, c->d_reg, c->d_occ);
+    CK(cudaGetLastError());
+    c->launches += 1;
+    std::vector<unsigned long long> h(n);
+    CK(cudaMemcpyAsync(h.data(), c->d_occ, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; ++i) occ[i] = (double)h[i] / (double)TR;
+    return ESM_OK;
+}

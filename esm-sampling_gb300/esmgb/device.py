@@ -21,7 +21,8 @@ NSTAT = 2 * (9 + 1) + 1
 EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
            "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
-           "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static")
+           "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
+           "esm_state_save", "esm_state_restore", "esm_regime_occupancy")
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather")
 
 _lib = None
@@ -61,6 +62,10 @@ def load(build_if_missing=True):
     L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
     L.esm_capacity_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
     L.esm_capacity_scores_static.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
+    L.esm_follow_capacities.argtypes = [C.c_void_p, P_f64, C.c_double, P_f64]
+    L.esm_state_save.argtypes = [C.c_void_p]
+    L.esm_state_restore.argtypes = [C.c_void_p]
+    L.esm_regime_occupancy.argtypes = [C.c_void_p, P_f64]
     L.esm_langevin_step.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_double, C.c_double, C.c_int32, P_f64,
                                     C.c_int64, P_f64, P_i32]
     L.esm_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64]
@@ -172,6 +177,24 @@ class DeviceChain:
         self._check(self.L.esm_capacity_scores_static(self.h, _p(sk), _p(fk), _p(parts)),
                     "esm_capacity_scores_static")
         return sk, fk, parts
+
+    def follow_capacities(self, knew, kmin=1.0):
+        """esm_follow_capacities: every replica follows the capacities to knew; returns the new k."""
+        knew = np.ascontiguousarray(knew, dtype=np.float64)
+        out = np.zeros(self.m.Kunits)
+        self._check(self.L.esm_follow_capacities(self.h, _p(knew), kmin, _p(out)), "esm_follow_capacities")
+        return out
+
+    def state_save(self):
+        self._check(self.L.esm_state_save(self.h), "esm_state_save")
+
+    def state_restore(self):
+        self._check(self.L.esm_state_restore(self.h), "esm_state_restore")
+
+    def regime_occupancy(self):
+        occ = np.zeros(self.m.K * 4)
+        self._check(self.L.esm_regime_occupancy(self.h, _p(occ)), "esm_regime_occupancy")
+        return occ
 
     def langevin_step(self, w, eta, kappa_s, kmin=1.0, clip=0.02, box=True, xi=None, it=0):
         w, eta, kappa_s = (np.ascontiguousarray(x, dtype=np.float64) for x in (w, eta, kappa_s))

@@ -113,3 +113,168 @@ class MLP:
 
     def launch_count(self):
         return int(self.L.esm_mlp_launch_count(self.h))
+
+
+# ---------------------------------------------------------------------------------------------
+# online surrogate of the replica-averaged score
+# ---------------------------------------------------------------------------------------------
+class ScoreSurrogate:
+    """MLP from (capacities / upper bound, regime occupancy) to the replica-averaged score s_bar [K],
+    trained online on the pairs the plain sampler produces (a replay buffer of the latest
+    `capacity` pairs, minibatches of `batch`, Adam at `lr`). Targets are standardised per unit with
+    the mean and deviation of the pairs in the buffer, refreshed at every training call (the
+    sampler's transient moves the scores by orders of magnitude)."""
+
+    def __init__(self, m, hidden=(512, 512, 512), capacity=8192, batch=1024, lr=1e-3, seed=1, min_pairs=64):
+        self.K = m.Kunits
+        self.nin = self.K + 4 * m.K
+        self.hi = np.maximum(np.asarray(m.unit_hi, float), 1.0)
+        self.mlp = MLP([self.nin, *hidden, self.K], batch_max=batch, seed=seed)
+        self.X = np.zeros((capacity, self.nin), np.float32)
+        self.Y = np.zeros((capacity, self.K), np.float64)
+        self.n = self.pos = 0
+        self.batch, self.lr, self.min_pairs = batch, lr, min_pairs
+        self.mu = np.zeros(self.K)
+        self.sd = np.ones(self.K)
+        self.rng = np.random.default_rng(seed)
+        self.losses = []
+
+    def features(self, k, occ):
+        return np.concatenate([np.asarray(k, float) / self.hi, np.asarray(occ, float)]).astype(np.float32)
+
+    def add(self, k, occ, sbar):
+        self.X[self.pos] = self.features(k, occ)
+        self.Y[self.pos] = np.nan_to_num(np.asarray(sbar, float), nan=0.0, posinf=0.0, neginf=0.0)
+        self.pos = (self.pos + 1) % len(self.X)
+        self.n = min(self.n + 1, len(self.X))
+
+    @property
+    def ready(self):
+        return self.n >= self.min_pairs
+
+    def train(self, steps=1):
+        if not self.ready:
+            return None
+        y = self.Y[: self.n]
+        self.mu = y.mean(0)
+        self.sd = np.maximum(y.std(0), 1e-9 + 1e-6 * np.abs(self.mu))
+        loss = None
+        for _ in range(steps):
+            idx = self.rng.integers(0, self.n, size=min(self.batch, self.n))
+            t = (self.Y[idx] - self.mu) / self.sd
+            loss = self.mlp.train_step(self.X[idx], t.astype(np.float32), self.lr)
+        self.losses.append(loss)
+        return loss
+
+    def predict(self, k, occ):
+        y = self.mlp.forward(self.features(k, occ)[None])[0].astype(np.float64)
+        return y * self.sd + self.mu
+
+    def close(self):
+        self.mlp.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# delayed-acceptance Langevin step of the capacities
+# ---------------------------------------------------------------------------------------------
+class DALangevin:
+    """Capacity moves proposed with the surrogate's drift at `mult` times the plain step, accepted in
+    two stages (Christen and Fox 2005):
+
+    - stage 1, with the surrogate: the Metropolis-adjusted Langevin ratio in w = log(k + kappa_s),
+      the log-density difference taken as the trapezoid path integral of the surrogate gradient
+      G_s(w) = (k + kappa_s) g_s + 1, g_s = -fk + (beta_k / beta_v) s_hat;
+    - stage 2, with the plain replica estimate: every replica follows the proposed capacities and
+      sweeps, the plain scores give G(w'), and the move is kept with probability
+      min(1, exp(dU - dU_s)), dU the trapezoid integral of the plain gradient.
+
+    Stage 2 targets what the plain estimate targets; a proposal rejected there restores the state
+    saved before it. An iteration that does not reach stage 2 sweeps at the current capacities (as
+    the plain step does) and refreshes G(w). Every plain evaluation trains the surrogate. Proposals
+    outside [kappa_min, hi] are rejected."""
+
+    def __init__(self, d, m, sur, eta, kappa_s, kmin=1.0, clip=0.02, mult=4.0, weights=None, seed=0,
+                 train_steps=1, blocks=False):
+        self.d, self.m, self.sur = d, m, sur
+        ug = np.asarray(m.unit_group)
+        self.eta_u = np.asarray(eta, float)[ug]
+        self.ks_u = np.asarray(kappa_s, float)[ug]
+        self.moving = self.eta_u > 0
+        # blocks: propose one capacity group per iteration (cycled), fewer dimensions per acceptance
+        self.groups = [np.flatnonzero((ug == gq) & self.moving) for gq in np.unique(ug)] if blocks else None
+        self.groups = [g for g in self.groups if len(g)] if blocks else None
+        self.h = mult * self.eta_u
+        self.clip = mult * clip
+        self.kmin = kmin
+        self.hi = np.asarray(m.unit_hi, float)
+        self.ratio = m.beta_k / m.beta_v
+        self.w = np.full(d.R, 1.0 / d.R) if weights is None else np.asarray(weights, float)
+        self.rng = np.random.default_rng(seed)
+        self.train_steps = train_steps
+        self.k = np.asarray(d.download_k(), float).copy()
+        self.G = self.fk = None
+        self.stats = {"iters": 0, "stage1": 0, "accepted": 0, "plain_evals": 0}
+
+    def grad_w(self, k, sbar, fk):
+        return (k + self.ks_u) * (-fk + self.ratio * sbar) + 1.0
+
+    def _plain(self, it):
+        self.d.sweeps(1, sweep0=it, stats=False)
+        sk, fk, _ = self.d.scores()
+        self.stats["plain_evals"] += 1
+        return self.w @ sk, fk
+
+    def step(self, it):
+        d = self.d
+        if self.groups:
+            mv = np.zeros_like(self.moving)
+            mv[self.groups[self.stats["iters"] % len(self.groups)]] = True
+        else:
+            mv = self.moving
+        self.stats["iters"] += 1
+        occ = d.regime_occupancy()
+        if self.G is None or not self.sur.ready:
+            sbar, self.fk = self._plain(it)
+            self.G = self.grad_w(self.k, sbar, self.fk)
+            self.sur.add(self.k, occ, sbar)
+            self.sur.train(self.train_steps)
+            return False
+        h = self.h
+        w0 = np.log(self.k + self.ks_u)
+        Gs0 = self.grad_w(self.k, self.sur.predict(self.k, occ), self.fk)
+        dr0 = np.clip(h * Gs0, -self.clip, self.clip)
+        w1 = w0.copy()
+        w1[mv] = w0[mv] + dr0[mv] + np.sqrt(2 * h[mv]) * self.rng.standard_normal(mv.sum())
+        k1 = self.k.copy()
+        k1[mv] = np.exp(w1[mv]) - self.ks_u[mv]
+        inside = bool(np.all(k1[mv] >= self.kmin) and np.all(k1[mv] <= self.hi[mv]))
+        go = False
+        if inside:
+            Gs1 = self.grad_w(k1, self.sur.predict(k1, occ), self.fk)
+            dr1 = np.clip(h * Gs1, -self.clip, self.clip)
+            dw = (w1 - w0)[mv]
+            lq_f = -np.sum((dw - dr0[mv]) ** 2 / (4 * h[mv]))
+            lq_b = -np.sum((-dw - dr1[mv]) ** 2 / (4 * h[mv]))
+            dUs = float(np.sum(dw * (Gs0[mv] + Gs1[mv]) / 2))
+            go = np.log(self.rng.random()) < dUs + lq_b - lq_f
+        accepted = False
+        if go:
+            self.stats["stage1"] += 1
+            d.state_save()
+            d.follow_capacities(k1, self.kmin)
+            sbar1, fk1 = self._plain(it)
+            G1 = self.grad_w(k1, sbar1, fk1)
+            self.sur.add(k1, occ, sbar1)
+            dU = float(np.sum(dw * (self.G[mv] + G1[mv]) / 2))
+            if np.log(self.rng.random()) < dU - dUs:
+                self.k, self.G, self.fk = k1, G1, fk1
+                accepted = True
+                self.stats["accepted"] += 1
+            else:
+                d.state_restore()
+        else:
+            sbar, self.fk = self._plain(it)
+            self.G = self.grad_w(self.k, sbar, self.fk)
+            self.sur.add(self.k, occ, sbar)
+        self.sur.train(self.train_steps)
+        return accepted

@@ -183,6 +183,21 @@ int esm_langevin_step(esm_ctx *ctx, const double *w, const double *eta, const do
                       double kappa_min, double clip, int32_t box, const double *xi, int64_t it,
                       double *knew_out, int32_t *nclip_out);
 
+/* The dispatch following of esm_langevin_step for given capacities: every replica follows the
+   capacities from the current k to knew [K] (follow_capacities!, src/replicas.jl:448), which then
+   become the context's k (k_out [K], may be NULL: the followed values, knew within the box). */
+int esm_follow_capacities(esm_ctx *ctx, const double *knew, double kappa_min, double *k_out);
+
+/* Snapshot of the sampler state (fields, weather, regimes, k) into device buffers of the context
+   (allocated by the first call), and its restoration (caches rebuilt). No reference counterpart:
+   the delayed-acceptance capacity step restores the state of a rejected proposal. */
+int esm_state_save(esm_ctx *ctx);
+int esm_state_restore(esm_ctx *ctx);
+
+/* Fraction of (step, replica) pairs in each (regime, season): occ [nreg*4], regime-major, the
+   season of a step as season (src/weather.jl:50). The regime summary fed to the surrogate. */
+int esm_regime_occupancy(esm_ctx *ctx, double *occ);
+
 /* Weather step of the replicas flagged in `moved` [R] (0/1): pCN of angle theta[r] in the VAR
    innovations (src/replicas.jl:105 pcn_weather), then with window[r] > 0 a regime window move of
    that length starting at wstart[r] (:156 regime_window, uniforms from the stream), then the
