@@ -234,7 +234,11 @@ def profile_case(args):
     B.build()
     from esmgb.device import DeviceChain
     from esmgb.model import initial_state, make_model
-    w = SMALL
+    w = dict(SMALL)
+    if args.T:
+        w["T"] = args.T
+    if args.R:
+        w["R"] = args.R
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
     d = DeviceChain(m, w["R"], precision=32, seed=w["seed"])
     d.upload(initial_state(m, w["R"], seed=7))
@@ -262,6 +266,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-replicas", type=int, default=2)
+    ap.add_argument("--T", type=int, default=0, help="--case small: steps (default 584)")
+    ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--case", default="full", choices=["full", "small"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()

@@ -184,6 +184,8 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
 }
 
 #define ESM_MAXROOTS 64
+// reals of a lane's local scratch array (16 KB in FP32); larger layouts use the global slab
+#define ESM_LANE_LOCAL 4096
 
 // ---------------------------------------------------------------------------------------------
 // per-lane context
@@ -192,7 +194,8 @@ template <class real>
 struct Lane {
     const DevModel<real> &M;
     Desc<real> &d;            // the warp's move descriptor (shared memory)
-    real *slab;               // this warp's scratch slab
+    real *slab;               // this lane's scratch: its local array, or its column of the warp's slab
+    int sstride;              // 1 (local array) or 32 (slab interleaved by lane)
     int lane;
     const LaneLayout &LL;     // per-lane scratch layout (shared memory)
     int tau, taum, tau1, rep;
@@ -201,10 +204,11 @@ struct Lane {
     // its terms (the node-balance terms of a move cancel to far less than their size)
     mutable real nzs = 0;
 
-    __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int lane_, const LaneLayout &LL_)
-        : M(M_), d(d_), slab(slab_), lane(lane_), LL(LL_) {}
+    __device__ Lane(const DevModel<real> &M_, Desc<real> &d_, real *slab_, int sstride_, int lane_,
+                    const LaneLayout &LL_)
+        : M(M_), d(d_), slab(slab_), sstride(sstride_), lane(lane_), LL(LL_) {}
 
-    __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * 32 + lane]; }
+    __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * sstride]; }
     __device__ inline size_t ix(int x, int t) const { return sidx(x, t, rep, M.T, M.R); }
 
     __device__ static inline real nzacc(real v, real &A) {
@@ -1437,8 +1441,12 @@ __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<re
     const LaneLayout &LL = sLL;
     int fi = d.hdr[12];
     if (fi < 0) return;  // not a valid move: nothing to do (grid-uniform)
-    real *slab = scratch + (size_t)blockIdx.x * LL.total * 32;
-    Lane<real> Ln(M, d, slab, lane, LL);
+    // per-lane scratch: a local array (cached in L1, written back) when the layout fits it, else
+    // the lane's column of this block's slab in global memory
+    real local[ESM_LANE_LOCAL];
+    bool loc = LL.total <= ESM_LANE_LOCAL;
+    real *slab = loc ? local : scratch + (size_t)blockIdx.x * LL.total * 32 + lane;
+    Lane<real> Ln(M, d, slab, loc ? 1 : 32, lane, LL);
     unsigned long long tried = 0, moved = 0, guards = 0;
     int nitems = ntile * wpt;
     while (true) {
@@ -1501,7 +1509,7 @@ __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<re
 template <class real>
 size_t linemove_scratch_reals(const DevModel<real> &M) {
     LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
-    return (size_t)LL.total * 32;
+    return LL.total <= ESM_LANE_LOCAL ? 0 : (size_t)LL.total * 32;  // 0: the lanes' local arrays suffice
 }
 
 // bytes of one move descriptor (the per-move buffer stride and the dynamic shared memory of k_move)
