@@ -251,6 +251,44 @@ def profile_case(args):
                       "moves_tried": int(st[:20:2].sum()), "guards": int(st[-1])}), flush=True)
 
 
+def batch_case(args):
+    """Many independent models of uneven size on one GPU: N ~ U{10..128}, L = 1.5 N,
+    T in {1460, 2920, 8760}, 16 replicas each (seed-fixed). Every model is a context with its own
+    stream and graph-captured class passes; the host enqueues one sweep on every context, then waits
+    for all, so the models' kernels overlap on the GPU."""
+    from esmgb import build as B
+    B.build()
+    from esmgb.device import DeviceChain
+    from esmgb.model import initial_state, make_model
+    rng = np.random.default_rng(2024)
+    nm = args.models
+    specs = [(int(rng.integers(10, 129)), int(rng.choice([1460, 2920, 8760]))) for _ in range(nm)]
+    chains = []
+    t0 = time.perf_counter()
+    for i, (N, T) in enumerate(specs):
+        m = make_model(N, int(round(1.5 * N)), T, seed=1000 + i)
+        d = DeviceChain(m, 16, precision=32, seed=1000 + i)
+        d.upload(initial_state(m, 16, seed=7))
+        chains.append((m, d))
+    setup = time.perf_counter() - t0
+    for m, d in chains:                       # warm-up: captures each context's class graphs
+        d.sweeps(args.warmup, 0, stats=False)
+    for m, d in chains:
+        d.sync(600.0)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        for m, d in chains:
+            d.sweeps(1, args.warmup + s, stats=False)
+    for m, d in chains:
+        d.sync(600.0)
+    dt = time.perf_counter() - t0
+    moves = sum((sum(len(a.ptr) - 1 for a in m.atoms) + round(4.0 * m.N)) * m.T * 16 for m, _ in chains)
+    print(json.dumps({"case": "batch", "models": nm, "replicas": 16, "sweeps": args.steps,
+                      "model_sweeps_per_s": nm * args.steps / dt, "line_moves_per_s": moves * args.steps / dt,
+                      "wall_s": dt, "setup_s": setup,
+                      "sizes": {"N": [n for n, _ in specs], "T": [t for _, t in specs]}}), flush=True)
+
+
 def config_dict():
     w = WORKLOAD
     return {"workload": "plain replica sampler on GPU: 40 nodes, 60 lines, T=8760 hourly, 64 replicas",
@@ -268,11 +306,14 @@ def main():
     ap.add_argument("--cpu-replicas", type=int, default=2)
     ap.add_argument("--T", type=int, default=0, help="--case small: steps (default 584)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
-    ap.add_argument("--case", default="full", choices=["full", "small"],
+    ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--case", default="full", choices=["full", "small", "batch"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
     if args.case == "small":
         return profile_case(args)
+    if args.case == "batch":
+        return batch_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)

@@ -77,6 +77,8 @@ struct esm_ctx {
     bool has_snap = false;
     unsigned long long *d_occ = nullptr;
     unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
+    uint32_t *d_sweep = nullptr;         // the sweep index of the current class pass
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // a whole class pass, per class
     // weather
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
     double *d_wbeta = nullptr, *d_wtheta = nullptr, *d_wxi = nullptr;
@@ -444,6 +446,7 @@ int alloc_state(esm_ctx *c) {
     unsigned int *ctr;
     if ((rc = dalloc(c, &ctr, (size_t)(M.natoms + M.nextra)))) return rc;
     c->d_item_ctr = ctr;
+    if ((rc = dalloc(c, &c->d_sweep, 1))) return rc;
     return ESM_OK;
 }
 
@@ -537,19 +540,47 @@ int rebuild_any(esm_ctx *c) {
     return ESM_OK;
 }
 
+__global__ void k_set_word(uint32_t *p, uint32_t v) { *p = v; }
+
+int class_pass_launch(esm_ctx *c, int cls, int limit) {
+    int ns = c->class_len[cls];
+    if (c->precision == 64)
+        CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, c->d_sweep, cls, limit, (double *)c->d_scratch,
+                                          c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
+    else
+        CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, c->d_sweep, cls, limit, (float *)c->d_scratch,
+                                         c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
+    return ESM_OK;
+}
+
+// One colour class. A whole class (no move limit) runs as a CUDA graph captured at its first use:
+// the per-move launches (a few hundred) then cost one graph launch; the sweep index is the only
+// argument that changes and is written to the device first.
 int class_pass_any(esm_ctx *c, uint32_t sweep, int cls, int limit = 0) {
     int ns = c->class_len[cls];
     if (ns == 0) return ESM_OK;
     Span sp(c, ESM_KT_CLASS);
-    if (c->precision == 64)
-        CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, sweep, cls, limit, (double *)c->d_scratch,
-                                          c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
-    else
-        CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, sweep, cls, limit, (float *)c->d_scratch,
-                                         c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
-    int nmoves = c->Mf.natoms + c->Mf.nextra;
-    if (c->precision == 64) nmoves = c->Md.natoms + c->Md.nextra;
-    c->launches += 1 + (limit > 0 && limit < nmoves ? limit : nmoves);
+    k_set_word<<<1, 1, 0, c->stream>>>(c->d_sweep, sweep);
+    CK(cudaGetLastError());
+    int nmoves = c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
+    int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
+    c->launches += 2 + nrun;
+    if (limit > 0) return class_pass_launch(c, cls, limit);
+    if (!c->graph[cls]) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = class_pass_launch(c, cls, 0);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CK(e);
+        e = cudaGraphInstantiate(&c->graph[cls], g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+    }
+    CK(cudaGraphLaunch(c->graph[cls], c->stream));
     return ESM_OK;
 }
 
@@ -706,6 +737,8 @@ int esm_destroy(esm_ctx *c) {
         cudaEventDestroy(mk.b);
     }
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
+    for (auto &g : c->graph)
+        if (g) cudaGraphExecDestroy(g);
     for (void *p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c->snap;

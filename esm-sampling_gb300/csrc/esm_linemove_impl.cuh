@@ -1383,7 +1383,7 @@ __device__ __noinline__ void lane_kinks(const Lane<real> &Ln) {
 // descriptor is the same for all tasks and is built once here, by one warp, in stream order.
 // Descriptor mi goes to descs + mi * stride; its header word 12 holds the family index (-1: no move).
 template <class real>
-__global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevModel<real> M, uint32_t sweep, int cls,
+__global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevModel<real> M, const uint32_t *sweep_p, int cls,
                                                   int nrun, char *descs, size_t stride) {
     extern __shared__ __align__(16) char smem[];
     __shared__ Desc<real> sd;
@@ -1399,6 +1399,7 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
     }
     for (int i = lane; i < M.L; i += 32) d.lmark[i] = 0;
     __syncwarp();
+    uint32_t sweep = *sweep_p;
     Stream st{M.seed, 0u, (uint32_t)cls, sweep, 0u};
     build_list(M, d, st, lane);
     for (int mi = 0; mi < nrun; ++mi) {
@@ -1420,7 +1421,7 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
 // walks differ in length.
 template <class real>
 __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps,
-                                            int ntile, int wpt, uint32_t sweep, int mi, const char *descs,
+                                            int ntile, int wpt, const uint32_t *sweep_p, int mi, const char *descs,
                                             size_t stride, real *scratch, unsigned long long *stats,
                                             unsigned int *next_item) {
     extern __shared__ __align__(16) char smem[];
@@ -1447,6 +1448,7 @@ __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<re
     bool loc = LL.total <= ESM_LANE_LOCAL;
     real *slab = loc ? local : scratch + (size_t)blockIdx.x * LL.total * 32 + lane;
     Lane<real> Ln(M, d, slab, loc ? 1 : 32, lane, LL);
+    uint32_t sweep = *sweep_p;
     unsigned long long tried = 0, moved = 0, guards = 0;
     int nitems = ntile * wpt;
     while (true) {
@@ -1518,29 +1520,26 @@ size_t linemove_smem_per_warp(const DevModel<real> &M) {
     return (desc_bytes(M, M.natoms + M.nextra) + 15) & ~(size_t)15;
 }
 
-// warps of k_move resident per SM (one warp per block), for the scratch slabs of a context
+// warps of k_move resident per SM (one warp per block), for the grid and scratch of a context
 template <class real>
 int linemove_blocks_per_sm(const DevModel<real> &M) {
     int nb = 0;
     size_t stride = linemove_smem_per_warp(M);
+    // (the dynamic shared memory limits are set here, at context creation, so that no later call --
+    // possibly under stream capture -- has to)
+    cudaFuncSetAttribute(k_prep_moves<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real>, 32, stride) != cudaSuccess || nb < 1) nb = 16;
     return nb;
 }
 
 template <class real>
-cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, uint32_t sweep, int cls,
+cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
                               int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
                               unsigned int *counters, cudaStream_t s) {
     int nmoves = M.natoms + M.nextra;
     int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
     size_t stride = linemove_smem_per_warp(M);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_prep_moves<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
     cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(unsigned int) * nrun, s);
     if (e != cudaSuccess) return e;
     k_prep_moves<real><<<1, 32, stride, s>>>(M, sweep, cls, nrun, descs, stride);
