@@ -237,6 +237,8 @@ def profile_case(args):
     w = dict(SMALL)
     if args.T:
         w["T"] = args.T
+    if args.N:
+        w["N"], w["L"] = args.N, args.L or int(round(1.5 * args.N))
     if args.R:
         w["R"] = args.R
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
@@ -305,6 +307,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-replicas", type=int, default=2)
     ap.add_argument("--T", type=int, default=0, help="--case small: steps (default 584)")
+    ap.add_argument("--N", type=int, default=0, help="--case small: nodes (default 40)")
+    ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
     ap.add_argument("--case", default="full", choices=["full", "small", "batch"],

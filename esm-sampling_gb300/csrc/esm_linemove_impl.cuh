@@ -50,6 +50,7 @@ struct Desc {
     int *kn;
     real *kg;
     int *ku, *kk, *kupos;
+    real *kda;  // direct coefficient of a kinked unit that the move also moves directly (else 0)
     int *nds, *nda;
     int *gia, *gposa;
     real *gaa;
@@ -82,6 +83,7 @@ __host__ __device__ inline Desc<real> carve_desc(char *base, const DevModel<real
     d.ku = c.take<int>(M.maxku);
     d.kk = c.take<int>(M.maxku);
     d.kupos = c.take<int>(M.maxku);
+    d.kda = c.take<real>(M.maxku);
     d.nds = c.take<int>(M.N);
     d.nda = c.take<int>(M.N);
     d.gia = c.take<int>(4);
@@ -121,6 +123,7 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
     c.take<int>(M.maxku);
     c.take<int>(M.maxku);
     c.take<int>(M.maxku);
+    c.take<real>(M.maxku);
     c.take<int>(M.N);
     c.take<int>(M.N);
     c.take<int>(4);
@@ -139,7 +142,15 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
 struct LaneLayout {
     int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua;
     int ut, uk, usl, ue, un, uh, ui, ucl, ufe, ufn, usw, usa, zr, zl, total;
+    int maxroots;  // capacity of the root buffers ro and gro
 };
+// sign changes one segment of a walk can hold: every touched node's balance at both steps and the
+// three storage secondaries of every storage term at both steps
+template <class real>
+__host__ __device__ inline int linemove_maxroots(const DevModel<real> &M) {
+    return 2 * M.maxn + 6 * M.maxstu;
+}
+
 __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxstu, int maxroots, int maxk, int maxku) {
     LaneLayout L;
     int o = 0;
@@ -156,6 +167,7 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
     L.dca = o; o += maxstu;
     L.dps = o; o += maxstu;
     L.dpa = o; o += maxstu;
+    L.maxroots = maxroots;
     L.ro = o; o += maxroots;
     L.gro = o; o += maxroots;
     L.kq = o; o += maxk;
@@ -183,7 +195,6 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
     return L;
 }
 
-#define ESM_MAXROOTS 64
 // reals of a lane's local scratch array (16 KB in FP32); larger layouts use the global slab
 #define ESM_LANE_LOCAL 4096
 
@@ -249,12 +260,12 @@ struct Lane {
             S(LL.drs, d.gpos[q]) -= dp;
         }
         for (int q = 0; q < nku; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
-            real ak = S(LL.kua, q);
-            if (ak == 0) continue;
+            real ak = S(LL.kua, q), a = d.kda[q];
+            if (ak == 0 && a == 0) continue;
             int j = d.ku[q];
             real k = M.kc_d[j], A = M.d_avail[j];
             real dyc, dex;
-            clamp_diff<real>(M.g[ix(j, tau)], ak * S(LL.kph, d.kk[q]), &dyc, &dex);
+            clamp_diff<real>(M.g[ix(j, tau)], t * a + ak * S(LL.kph, d.kk[q]), &dyc, &dex);
             real dp = A * k * dyc;
             D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.drs, d.kupos[q]) -= dp;
@@ -349,10 +360,10 @@ struct Lane {
                     for (int h = 0; h < 3; ++h)
                         if (root_of(a3[h], b3[h], lo, hi, sgn, &x)) {
                             if (stor) {
-                                if (*ngro >= ESM_MAXROOTS) return false;
+                                if (*ngro >= LL.maxroots) return false;
                                 S(LL.gro, (*ngro)++) = x;
                             } else {
-                                if (*nro >= ESM_MAXROOTS) return false;
+                                if (*nro >= LL.maxroots) return false;
                                 S(LL.ro, (*nro)++) = x;
                             }
                         }
@@ -362,14 +373,14 @@ struct Lane {
             for (int q = 0; q < nns; ++q) {
                 real b = M.r[ix(d.nds[q], tau)] + S(LL.drs, q);
                 if (root_of(S(LL.sps, q), b, lo, hi, sgn, &x)) {
-                    if (*nro >= ESM_MAXROOTS) return false;
+                    if (*nro >= LL.maxroots) return false;
                     S(LL.ro, (*nro)++) = x;
                 }
             }
             for (int q = 0; q < nna; ++q) {
                 real b = M.r[ix(d.nda[q], taum)] + S(LL.dra, q);
                 if (root_of(S(LL.spa, q), b, lo, hi, sgn, &x)) {
-                    if (*nro >= ESM_MAXROOTS) return false;
+                    if (*nro >= LL.maxroots) return false;
                     S(LL.ro, (*nro)++) = x;
                 }
             }
@@ -419,12 +430,11 @@ struct Lane {
             consider((real(1) - y0) / a);
         }
         for (int q = 0; q < nku; ++q) {
-            real ak = S(LL.kua, q);
-            if (ak == 0) continue;
+            real ak = S(LL.kua, q), a = d.kda[q];
+            if (ak == 0 && a == 0) continue;
             int kq = d.kk[q];
             real Q = S(LL.kq, kq), gk = d.kg[kq];
             real y0 = M.g[ix(d.ku[q], tau)];
-            real a = 0;
             real offs[4] = {real(0), real(0), -ak * Q, ak * Q};
             real sls[4] = {a + ak * gk, a, a, a + ak * gk};
             for (int h = 0; h < 4; ++h) {
@@ -687,7 +697,7 @@ struct Lane {
             S(LL.ut, q) = tn;
             S(LL.uk, q) = end ? (hk == 1 ? real(1) : real(0)) : real(0);
             S(LL.ufn, q) = fn;
-            S(LL.usl, q) = (fn - f) / (tn - t);
+            S(LL.usl, q) = tn != t ? (fn - f) / (tn - t) : real(0);  // (an event at t itself: no extent)
         } else {  // linear to infinity
             real tp = t + sgn * fmax(real(1), fabs(t));
             fn = unit_val(q, tp, &Sw, &Sa);
@@ -887,8 +897,8 @@ struct Lane {
         for (int q = 0; q < nna; ++q) M.r[ix(d.nda[q], taum)] += S(LL.dra, q);
         for (int q = 0; q < ng; ++q) M.g[ix(d.gi[q], tau)] += t * d.ga[q];
         for (int q = 0; q < nku; ++q) {
-            real ak = S(LL.kua, q);
-            if (ak != 0) M.g[ix(d.ku[q], tau)] += t * real(0) + ak * S(LL.kph, d.kk[q]);
+            real ak = S(LL.kua, q), a = d.kda[q];
+            if (ak != 0 || a != 0) M.g[ix(d.ku[q], tau)] += t * a + ak * S(LL.kph, d.kk[q]);
         }
         for (int q = 0; q < nse; ++q) M.e[ix(d.si[q], tau)] += t * d.sa[q];
         for (int q = 0; q < nth; ++q) M.theta[ix(d.thn[q], tau)] += t * d.tha[q];
@@ -1282,6 +1292,16 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
                 ++c;
             }
         nth = c;
+        // a unit moved directly and pro rata is one term (add_kentry! adds to the unit's entry,
+        // src/local.jl:583): its direct coefficient moves into the kinked entry
+        for (int q = 0; q < nku; ++q) {
+            d.kda[q] = 0;
+            for (int p = 0; p < ng; ++p)
+                if (d.gi[p] == d.ku[q] && d.ga[p] != 0) {
+                    d.kda[q] = d.ga[p];
+                    d.ga[p] = 0;
+                }
+        }
         // node lists: ws entries (gens, storage, kinked units), then line ends; wa entries, linked storage
         int nns = 0, nna = 0;
         for (int q = 0; q < ng; ++q) add_node(d, 0, M.d_bus[d.gi[q]], &nns, &d.gpos[q]);
@@ -1435,7 +1455,7 @@ __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<re
     }
     if (lane == 0) {
         sd = carve_desc<real>(smem, M, M.natoms + M.nextra);
-        sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+        sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, linemove_maxroots(M), M.maxk, M.maxku);
     }
     __syncwarp();
     Desc<real> &d = sd;
@@ -1510,7 +1530,7 @@ __global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<re
 // ---------------------------------------------------------------------------------------------
 template <class real>
 size_t linemove_scratch_reals(const DevModel<real> &M) {
-    LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, ESM_MAXROOTS, M.maxk, M.maxku);
+    LaneLayout LL = lane_layout(M.maxpts, M.maxn, M.maxstu, linemove_maxroots(M), M.maxk, M.maxku);
     return LL.total <= ESM_LANE_LOCAL ? 0 : (size_t)LL.total * 32;  // 0: the lanes' local arrays suffice
 }
 
