@@ -400,6 +400,7 @@ int build_model(esm_ctx *c, const esm_model *m, const esm_opts *o) {
     M.maxk = maxleak;
     M.maxku = maxleak * maxunits;
     M.maxstu = maxstu;
+    if (M.maxpts == 0) M.maxpts = esm_auto_max_points(maxstu);
     return ESM_OK;
 }
 
@@ -625,7 +626,7 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     *out = c;
     if (o->precision != 32 && o->precision != 64) return fail(c, ESM_EINVAL, "precision must be 32 or 64");
     if (o->R < 1 || m->N < 2 || m->T < 2 || m->K < 1) return fail(c, ESM_EINVAL, "bad sizes");
-    if (o->max_points < 8) return fail(c, ESM_EINVAL, "max_points must be >= 8");
+    if (o->max_points != 0 && o->max_points < 8) return fail(c, ESM_EINVAL, "max_points must be 0 (automatic) or >= 8");
     c->precision = o->precision;
     c->R = o->R;
     c->N = m->N;

@@ -111,7 +111,7 @@ class ModelBuffers:
         self.natoms = int(fap[-1])
 
 
-def make_opts(R, precision=32, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=192, span=0,
+def make_opts(R, precision=32, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
               rates=FAMILY_RATES) -> EsmOpts:
     o = EsmOpts()
     o.R, o.precision, o.seed, o.extra, o.maxnats, o.kappa_min = R, precision, seed, extra, maxnats, kappa_min

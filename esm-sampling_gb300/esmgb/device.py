@@ -88,7 +88,7 @@ class DeviceChain:
     """One chain of R replicas on the GPU (an ``esm_ctx``)."""
 
     def __init__(self, model: SynthModel, R: int, precision: int = 32, seed: int = 1, extra: float = 4.0,
-                 maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 192, span: int = 0):
+                 maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 0, span: int = 0):
         self.L = load()
         self.m = model
         self.R = R

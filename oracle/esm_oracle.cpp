@@ -1519,6 +1519,13 @@ void *orc_create(const esm_model *em, const esm_opts *eo) {
     Opts &o = c->o;
     o.R = eo->R;
     o.max_points = eo->max_points;
+    if (o.max_points == 0) {  // automatic, as esm_auto_max_points
+        int mx = 1;
+        for (int f = 0; f < m.nfields; ++f)
+            if (m.frole[f] == ESM_ROLE_SE)
+                for (int a = m.fap[f]; a < m.fap[f + 1]; ++a) mx = std::max(mx, m.ap[a + 1] - m.ap[a]);
+        o.max_points = esm_auto_max_points(mx);
+    }
     o.span = eo->span;
     o.seed = eo->seed;
     o.extra = eo->extra;

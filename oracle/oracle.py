@@ -95,7 +95,7 @@ def langevin_update(k, g, xi, eta, ks, kmin=1.0, clip=np.inf, hi=None):
 class Oracle:
     """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
 
-    def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=192, span=0,
+    def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
                  threads=None):
         import sys
         sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
