@@ -50,7 +50,7 @@ struct esm_ctx {
     std::string err;
     int64_t launches = 0;
     bool has_state = false, has_scores = false;
-    int max_warps = 0;
+    int max_warps = 0;  // k_move blocks (one warp each) resident on the device
     esm::DevModel<float> Mf;
     esm::DevModel<double> Md;
     vector<void *> allocs;
@@ -432,7 +432,8 @@ int alloc_state(esm_ctx *c) {
     if ((rc = dalloc(c, &q, std::max(M.Nren, 1)))) return rc;
     M.kc_r = q;
     c->kc_r = q;
-    // line-move scratch for a persistent grid
+    // line-move grid (resident one-warp blocks) and, when the lane layout exceeds the local arrays,
+    // one global scratch slab per block
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

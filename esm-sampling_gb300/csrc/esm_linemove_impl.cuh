@@ -1,14 +1,15 @@
-// Line-move colour-class kernel: the exact line-conditional dispatch moves of one parity class of
-// the local sweep (src/local.jl:1927 local_sweep!, the threaded body :1954-2051) for every replica.
+// Line-move kernels: the exact line-conditional dispatch moves of one parity class of the local
+// sweep (src/local.jl:1927 local_sweep!, the threaded body :1954-2051) for every replica.
 //
-// Mapping. A warp owns one "tile" (span consecutive steps of the class) and 32 (step, replica)
-// tasks of it, the replica index fastest, so that every state access of the warp is one coalesced
-// 128-byte line of the (X, T, R) arrays. All tasks of a tile run the same move list (the move
-// selection reads only capacities and static tables, src/local.jl:14 "selection uses only (k, x)"),
-// so the move's structure -- entries, lines, touched nodes, storage terms -- is warp-uniform and
-// is built once in shared memory; each lane then walks its own piecewise-exponential line
-// conditional (walk!, src/local.jl:1294) and draws t (sample_line!, :1501) with its own uniforms.
-// Per-lane walk buffers live in a global scratch slab, interleaved by lane (coalesced).
+// Mapping. All (step, replica) tasks of a class run the same move list (the move selection reads
+// only capacities and static tables, src/local.jl:14 "selection uses only (k, x)"), so a move's
+// structure -- entries, lines, touched nodes, storage terms -- is the same for every task and is
+// built once per class pass (k_prep_moves). k_move then runs one move for every task: a warp owns
+// 32 tasks of a tile (span consecutive steps x replicas, replica fastest, so that every state
+// access of the warp is one coalesced 128-byte line of the (X, T, R) arrays), and each lane walks
+// its own piecewise-exponential line conditional (walk!, src/local.jl:1294) and draws t
+// (sample_line!, :1501) with its own uniforms. Per-lane walk buffers live in a local array when
+// they fit it, else in a per-block global slab interleaved by lane.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
