@@ -311,6 +311,8 @@ def main():
     ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
+                                               "the autotuner's choice")
     ap.add_argument("--case", default="full", choices=["full", "small", "batch"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
@@ -333,6 +335,14 @@ def main():
     from esmgb import replicas as RP
     m, st, d = setup_chain(32)
     R = d.R
+    # the line-move grid picked by the library's autotuner (one timed colour class per candidate,
+    # state restored), untimed setup; --grid WPBxWPS fixes it instead (profiler runs)
+    if args.grid:
+        wpb, wps = (int(x) for x in args.grid.lower().split("x"))
+        d.set_move_grid(wpb, wps)
+        grid, grid_ms = d.move_grid()[:2], {}
+    else:
+        grid, grid_ms = d.autotune_moves(sweep=0)
     ctl = RP.ReplicaCtl(M=R)
     rng = np.random.Generator(np.random.PCG64(rank + 1))
     # iterations placed so that the timed region contains a weather burst (every 40 steps)
@@ -399,6 +409,8 @@ def main():
                          "note": "the exact line sampler is FP32-issue-bound; the HBM bytes are the compulsory state"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "clocks": clocks,
+            "move_grid": {"warps_per_block": grid[0], "warps_per_sm": grid[1],
+                          "autotune_ms_per_class": {f"{a}x{b}": round(v, 1) for (a, b), v in grid_ms.items()}},
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
             "line_moves_per_s": moves * args.steps / (dev_ms / 1000.0) * world,
             "wall_device_loop_s": wall_dev}

@@ -50,7 +50,10 @@ struct esm_ctx {
     std::string err;
     int64_t launches = 0;
     bool has_state = false, has_scores = false;
-    int max_warps = 0;  // k_move blocks (one warp each) resident on the device
+    int move_wpb = 1;           // k_move block shape: warps per block (1, 2 or 4)
+    int max_warps = 0;          // k_move warps launched per move: the resident limit or a tuned count
+    int warps_cap[3] = {0, 0, 0};  // the resident limit per block shape (1, 2, 4 warps per block)
+    int nsm = 0;
     esm::DevModel<float> Mf;
     esm::DevModel<double> Md;
     vector<void *> allocs;
@@ -437,9 +440,16 @@ int alloc_state(esm_ctx *c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    c->max_warps = std::max(4, nsm * esm::linemove_blocks_per_sm<real>(M));
+    int wmax = 0;
+    for (int i = 0; i < 3; ++i) {
+        c->warps_cap[i] = std::max(4, nsm * esm::linemove_blocks_per_sm<real>(M, 1 << i));
+        wmax = std::max(wmax, c->warps_cap[i]);
+    }
+    c->nsm = nsm;
+    c->move_wpb = 1;
+    c->max_warps = c->warps_cap[0];
     size_t per = esm::linemove_scratch_reals<real>(M);
-    if ((rc = dalloc(c, &q, per * (size_t)c->max_warps))) return rc;
+    if ((rc = dalloc(c, &q, per * (size_t)wmax))) return rc;
     c->d_scratch = q;
     // the move descriptors of a class pass
     char *dp;
@@ -548,10 +558,12 @@ int class_pass_launch(esm_ctx *c, int cls, int limit) {
     int ns = c->class_len[cls];
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, c->d_sweep, cls, limit, (double *)c->d_scratch,
-                                          c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
+                                          c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr,
+                                          c->stream));
     else
         CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, c->d_sweep, cls, limit, (float *)c->d_scratch,
-                                         c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, c->stream));
+                                         c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr,
+                                         c->stream));
     return ESM_OK;
 }
 
@@ -1196,6 +1208,91 @@ int esm_state_restore(esm_ctx *c) {
     CK(cudaStreamSynchronize(c->stream));
     c->has_scores = false;
     return ESM_OK;
+}
+
+int esm_set_move_grid(esm_ctx *c, int32_t warps_per_block, int32_t warps_per_sm) {
+    if (!c) return ESM_EINVAL;
+    int wi = warps_per_block == 1 ? 0 : warps_per_block == 2 ? 1 : warps_per_block == 4 ? 2 : -1;
+    if (wi < 0) return fail(c, ESM_EINVAL, "warps_per_block must be 1, 2 or 4");
+    if (warps_per_sm < 0) return fail(c, ESM_EINVAL, "warps_per_sm must be >= 0");
+    int cap = c->warps_cap[wi];
+    int w = warps_per_sm == 0 ? cap : std::min(cap, std::max(4, warps_per_sm * c->nsm));
+    if (w == c->max_warps && warps_per_block == c->move_wpb) return ESM_OK;
+    int rc = esm_sync(c, 600.0);  // the captured class passes hold the old grid: drop them
+    if (rc) return rc;
+    for (auto &g : c->graph)
+        if (g) {
+            CK(cudaGraphExecDestroy(g));
+            g = nullptr;
+        }
+    c->move_wpb = warps_per_block;
+    c->max_warps = w;
+    return ESM_OK;
+}
+
+int esm_move_grid(const esm_ctx *c, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limits_per_sm) {
+    if (!c || c->nsm < 1) return ESM_EINVAL;
+    if (warps_per_block) *warps_per_block = c->move_wpb;
+    if (warps_per_sm) *warps_per_sm = (c->max_warps + c->nsm - 1) / c->nsm;
+    if (limits_per_sm)
+        for (int i = 0; i < 3; ++i) limits_per_sm[i] = (c->warps_cap[i] + c->nsm - 1) / c->nsm;
+    return ESM_OK;
+}
+
+int esm_autotune_moves(esm_ctx *c, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    int list[ESM_TUNE_MAX][2], n = 0;
+    for (int wi = 0; wi < 3; ++wi) {
+        int lim = (c->warps_cap[wi] + c->nsm - 1) / c->nsm;
+        for (int w : {8, 16, 24, 32, 40})
+            if (w < lim && w % (1 << wi) == 0 && n < ESM_TUNE_MAX - 3 + wi) {
+                list[n][0] = 1 << wi;
+                list[n++][1] = w;
+            }
+        list[n][0] = 1 << wi;
+        list[n++][1] = lim;
+    }
+    int rc;
+    if ((rc = esm_state_save(c))) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int bw = c->move_wpb, bs = (c->max_warps + c->nsm - 1) / c->nsm;
+    double tbest = 1e300;
+    for (int i = 0; i < n && !rc; ++i) {
+        if ((rc = esm_set_move_grid(c, list[i][0], list[i][1]))) break;
+        // one untimed pass captures the class graph for this grid, then one timed pass from the same state
+        if ((rc = class_pass_any(c, (uint32_t)sweep, 0))) break;
+        if ((rc = esm_state_restore(c))) break;
+        if (cudaEventRecord(e0, c->stream) != cudaSuccess) rc = fail(c, ESM_ECUDA, "event record");
+        if (!rc) rc = class_pass_any(c, (uint32_t)sweep, 0);
+        if (!rc && cudaEventRecord(e1, c->stream) != cudaSuccess) rc = fail(c, ESM_ECUDA, "event record");
+        if (!rc) rc = esm_sync(c, 600.0);
+        float t = 0;
+        if (!rc && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) rc = fail(c, ESM_ECUDA, "event time");
+        if (!rc) rc = esm_state_restore(c);
+        if (rc) break;
+        if (cand) {
+            cand[2 * i] = list[i][0];
+            cand[2 * i + 1] = list[i][1];
+        }
+        if (ms) ms[i] = t;
+        if (t < tbest) {
+            tbest = t;
+            bw = list[i][0];
+            bs = list[i][1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (ncand) *ncand = n;
+    if (best) {
+        best[0] = bw;
+        best[1] = bs;
+    }
+    return esm_set_move_grid(c, bw, bs);
 }
 
 namespace {

@@ -6,10 +6,10 @@
 namespace esm {
 template size_t linemove_scratch_reals<float>(const DevModel<float> &);
 template size_t linemove_smem_per_warp<float>(const DevModel<float> &);
-template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int *, int, const uint32_t *, int, int, float *, int,
+template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int *, int, const uint32_t *, int, int, float *, int, int,
                                               unsigned long long *, char *, unsigned int *,
                                               cudaStream_t);
-template int linemove_blocks_per_sm<float>(const DevModel<float> &);
+template int linemove_blocks_per_sm<float>(const DevModel<float> &, int);
 template cudaError_t launch_rebuild<float>(const DevModel<float> &, cudaStream_t);
 template cudaError_t launch_scores<float>(const DevModel<float> &, double *, double *, cudaStream_t);
 template cudaError_t launch_score_finish<float>(const DevModel<float> &, const double *, const double *, const double *,

@@ -6,10 +6,10 @@
 namespace esm {
 template size_t linemove_scratch_reals<double>(const DevModel<double> &);
 template size_t linemove_smem_per_warp<double>(const DevModel<double> &);
-template cudaError_t launch_class_pass<double>(const DevModel<double> &, const int *, int, const uint32_t *, int, int, double *, int,
+template cudaError_t launch_class_pass<double>(const DevModel<double> &, const int *, int, const uint32_t *, int, int, double *, int, int,
                                               unsigned long long *, char *, unsigned int *,
                                               cudaStream_t);
-template int linemove_blocks_per_sm<double>(const DevModel<double> &);
+template int linemove_blocks_per_sm<double>(const DevModel<double> &, int);
 template cudaError_t launch_rebuild<double>(const DevModel<double> &, cudaStream_t);
 template cudaError_t launch_scores<double>(const DevModel<double> &, double *, double *, cudaStream_t);
 template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *, const double *,

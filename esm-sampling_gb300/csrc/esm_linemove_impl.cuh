@@ -142,7 +142,7 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
 // per-lane scratch layout (reals), interleaved by lane within a warp slab
 struct LaneLayout {
     int pr, cr, pl, cl, lm, drs, dra, sps, spa, dcs, dca, dps, dpa, ro, gro, kq, ke, kp, knm, kph, kv, kua;
-    int ut, uk, usl, ue, un, uh, ui, ucl, ufe, ufn, usw, usa, zr, zl, total;
+    int ut, uk, usl, ue, un, uh, ui, hk, hu, ufe, ufn, usw, usa, zr, zl, total;
     int maxroots;  // capacity of the root buffers ro and gro
 };
 // sign changes one segment of a walk can hold: every touched node's balance at both steps and the
@@ -185,7 +185,8 @@ __host__ __device__ inline LaneLayout lane_layout(int maxpts, int maxn, int maxs
     L.un = o; o += maxstu;
     L.uh = o; o += maxstu;
     L.ui = o; o += maxstu;
-    L.ucl = o; o += maxstu;
+    L.hk = o; o += maxstu;
+    L.hu = o; o += maxstu;
     L.ufe = o; o += maxstu;
     L.ufn = o; o += maxstu;
     L.usw = o; o += maxstu;
@@ -643,7 +644,6 @@ struct Lane {
         };
         cand(real(0) - e0, true);
         cand(real(1) - e0, true);
-        S(LL.ucl, q) = (have && prim) ? ts : real(INFINITY) * sgn;  // the next clamp of this unit
         real th[3];
         int nth = 0;
         th[nth++] = 0;  // the sign changes of the three storage secondaries (src/local.jl:885)
@@ -719,113 +719,139 @@ struct Lane {
         unit_next(q, t, f, sgn);
     }
 
-    // the first minimum in walking order of S(off, 0..n) and its index (-1 if n = 0). The loads
-    // go out eight at a time: one scan costs about one memory latency, not n of them.
-    __device__ inline int scan_min(int off, int n, real sgn, real *vmin) const {
-        int qb = -1;
-        real vb = 0;
-        int q = 0;
-        for (; q + 8 <= n; q += 8) {
-            real v[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) v[i] = S(off, q + i);
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (qb < 0 || sgn * (v[i] - vb) < 0) {
-                    vb = v[i];
-                    qb = q + i;
+    // A min-heap of the units with a pending event, keyed by sgn * (event time): the next event of
+    // the walk is at the top, and passing it costs log2(units) steps instead of a scan of all units.
+    __device__ inline void heap_up(int i) const {
+        real k = S(LL.hk, i), u = S(LL.hu, i);
+        while (i > 0) {
+            int p = (i - 1) >> 1;
+            real kp = S(LL.hk, p);
+            if (!(k < kp)) break;
+            S(LL.hk, i) = kp;
+            S(LL.hu, i) = S(LL.hu, p);
+            i = p;
+        }
+        S(LL.hk, i) = k;
+        S(LL.hu, i) = u;
+    }
+    __device__ inline void heap_down(int i, int n) const {
+        real k = S(LL.hk, i), u = S(LL.hu, i);
+        while (true) {
+            int l = 2 * i + 1;
+            if (l >= n) break;
+            int m = l;
+            real km = S(LL.hk, l);
+            if (l + 1 < n) {
+                real kr = S(LL.hk, l + 1);
+                if (kr < km) {
+                    m = l + 1;
+                    km = kr;
                 }
-        }
-        for (; q < n; ++q) {
-            real v = S(off, q);
-            if (qb < 0 || sgn * (v - vb) < 0) {
-                vb = v;
-                qb = q;
             }
+            if (!(km < k)) break;
+            S(LL.hk, i) = km;
+            S(LL.hu, i) = S(LL.hu, m);
+            i = m;
         }
-        *vmin = vb;
-        return qb;
+        S(LL.hk, i) = k;
+        S(LL.hu, i) = u;
     }
 
-    // the next clamp among the units (primary breakpoint); false if none is left
-    __device__ bool next_clamp(int nu, real sgn, real *tP) const {
-        real v;
-        int q = scan_min(LL.ucl, nu, sgn, &v);
-        if (q < 0 || !isfinite(v)) return false;
-        *tP = v;
-        return true;
-    }
-
-    // walk! for a separable move; same returns as walk()
+    // walk! for a separable move; same returns as walk(). The events of all units -- every
+    // unit's clamps (the primary breakpoints), storage thresholds and node-balance roots -- are
+    // visited in walking order, one point each; the stop test runs at every clamp (walk!'s test
+    // at its primary breakpoints), and once every clamp ahead is passed the walk takes ray steps.
     __device__ __noinline__ int walk_sep(int pofs, int cofs, int *np, real sgn) const {
         int nu = d.hdr[1];
         double B = 0;     // summed slope of the potential at the current position
         double absB = 0;  // the sum of the magnitudes of the units' slopes (round-off scale)
+        int nh = 0;       // units in the heap
+        int ncl = 0;      // clamps ahead (each unit's 0 and 1 crossings in this direction)
         for (int q = 0; q < nu; ++q) {
+            real a = d.sa[q], e0 = M.e[ix(d.si[q], tau)];
+            real c0 = (real(0) - e0) / a, c1 = (real(1) - e0) / a;
+            ncl += (isfinite(c0) && sgn * c0 > 0) + (isfinite(c1) && sgn * c1 > 0);
             unit_piece(q, real(0), sgn, M.r[ix(d.nds[d.spos[q]], tau)], M.r[ix(d.nda[d.sposa[q]], taum)]);
             unit_next(q, real(0), real(0), sgn);
             B += (double)S(LL.usl, q);
             absB += fabs((double)S(LL.usl, q));
+            real tq = S(LL.ut, q);
+            if (isfinite(tq)) {
+                S(LL.hk, nh) = sgn * tq;
+                S(LL.hu, nh) = real(q);
+                heap_up(nh);
+                ++nh;
+            }
         }
         *np = 0;
         double c = 0, cmin = 0;
-        real tcur = 0, delta = 0, tP = 0;
+        real tcur = 0, delta = 0;
         int nx = 0;
-        bool haveP = next_clamp(nu, sgn, &tP);
+        bool ray = ncl == 0;
+        // the unit at the top passes its event at t: its next event re-keys it (or it leaves)
+        auto pass_top = [&](real t) {
+            int q = (int)S(LL.hu, 0);
+            real old = S(LL.usl, q);
+            unit_pass(q, t, sgn);
+            B += (double)S(LL.usl, q) - (double)old;
+            absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
+            real tn = S(LL.ut, q);
+            if (isfinite(tn)) {
+                S(LL.hk, 0) = sgn * tn;
+            } else {
+                --nh;
+                S(LL.hk, 0) = S(LL.hk, nh);
+                S(LL.hu, 0) = S(LL.hu, nh);
+            }
+            if (nh > 0) heap_down(0, nh);
+        };
+        auto point = [&](real t) -> bool {
+            if (*np >= M.maxpts) return false;
+            push(pofs, cofs, np, t, (real)c, real(4.8e-7) * (real)(fabs(c) + absB * fabs((double)t)));
+            cmin = fmin(cmin, c);
+            return true;
+        };
         while (true) {
-            // the next primary breakpoint among the units, or a ray step beyond the last one
-            real target;
-            if (!haveP) {
-                double sl = (double)sgn * B;  // the outgoing slope at the last point (walk!'s probe)
+            if (!ray) {
+                if (nh == 0) {  // (no event left before the clamps the count expects)
+                    ray = true;
+                    continue;
+                }
+                int q = (int)S(LL.hu, 0);
+                real tS = S(LL.ut, q);
+                bool clamp = S(LL.uk, q) == real(1);
+                c += B * (double)(tS - tcur);
+                tcur = tS;
+                if (!point(tS)) return -1;
+                pass_top(tS);
+                if (clamp) {
+                    --ncl;
+                    if (c - cmin > (double)M.maxnats) return 1;
+                    if (ncl <= 0) ray = true;
+                }
+            } else {
+                // every clamp is behind: ray steps (the outgoing slope is the summed slope)
+                double sl = (double)sgn * B;
                 if (sl > 0)
                     delta = fmin(real(2) * M.maxnats / (real)sl, real(1e3) * fmax(fabs(tcur), real(1e-3)));
                 else
                     delta = delta == 0 ? fmax(fabs(tcur), real(1e-6)) : real(2) * delta;
-                target = tcur + sgn * delta;
-                nx += 1;
-                if (nx > 80) return 0;
-            } else {
-                target = tP;
-            }
-            // the secondary points before the target (no unit's clamp lies before it)
-            while (true) {
-                real tS = 0;
-                int qS = scan_min(LL.ut, nu, sgn, &tS);
-                if (qS < 0 || !isfinite(tS) || !(sgn * (target - tS) > 0)) break;
-                c += B * (double)(tS - tcur);
-                tcur = tS;
-                if (*np >= M.maxpts) return -1;
-                push(pofs, cofs, np, tS, (real)c, real(4.8e-7) * (real)(fabs(c) + absB * fabs((double)tS)));
-                cmin = fmin(cmin, c);
-                real old = S(LL.usl, qS);
-                unit_pass(qS, tS, sgn);
-                B += (double)S(LL.usl, qS) - (double)old;
-                absB = fmax(absB, absB + fabs((double)S(LL.usl, qS)) - fabs((double)old));
-            }
-            c += B * (double)(target - tcur);
-            tcur = target;
-            if (*np >= M.maxpts) return -1;
-            push(pofs, cofs, np, target, (real)c, real(4.8e-7) * (real)(fabs(c) + absB * fabs((double)target)));
-            cmin = fmin(cmin, c);
-            // every unit with an event here (its clamp, or a secondary that fell on it) moves on; a
-            // new piece starts strictly after its start, so this ends
-            for (int q0 = 0; q0 < nu; q0 += 8) {
-                real v[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[i] = q0 + i < nu ? S(LL.ut, q0 + i) : real(0);
-                for (int i = 0; i < 8 && q0 + i < nu; ++i) {
-                    if (v[i] != target) continue;  // (a finite event time: uk >= 0)
-                    int q = q0 + i;
-                    while (S(LL.ut, q) == target) {
-                        real old = S(LL.usl, q);
-                        unit_pass(q, target, sgn);
-                        B += (double)S(LL.usl, q) - (double)old;
-                        absB = fmax(absB, absB + fabs((double)S(LL.usl, q)) - fabs((double)old));
-                    }
+                real target = tcur + sgn * delta;
+                if (++nx > 80) return 0;
+                while (nh > 0) {  // the events before the target
+                    real tS = S(LL.ut, (int)S(LL.hu, 0));
+                    if (!(sgn * (target - tS) > 0)) break;
+                    c += B * (double)(tS - tcur);
+                    tcur = tS;
+                    if (!point(tS)) return -1;
+                    pass_top(tS);
                 }
+                c += B * (double)(target - tcur);
+                tcur = target;
+                if (!point(target)) return -1;
+                while (nh > 0 && S(LL.ut, (int)S(LL.hu, 0)) == target) pass_top(target);
+                if (c - cmin > (double)M.maxnats) return 1;
             }
-            if (haveP) haveP = next_clamp(nu, sgn, &tP);
-            if (c - cmin > (double)M.maxnats) return 1;
         }
     }
 
@@ -1440,34 +1466,45 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
 // is left, and each lane walks and samples its own line conditional. One launch per move keeps
 // every warp of the grid in the same code; taking items one at a time balances the warps, whose
 // walks differ in length.
-template <class real>
-__global__ void __launch_bounds__(32) k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps,
-                                            int ntile, int wpt, const uint32_t *sweep_p, int mi, const char *descs,
-                                            size_t stride, real *scratch, unsigned long long *stats,
-                                            unsigned int *next_item) {
+// Register bound per block shape (WPB warps per block, so many blocks resident per SM): one-warp
+// blocks keep the registers the kernel wants (80, 24 warps per SM), two- and four-warp blocks trade
+// registers for resident warps (64 and 48 registers: 32 and 40 warps per SM).
+template <int WPB>
+struct MoveBounds {
+    static constexpr int min_blocks = WPB == 1 ? 24 : WPB == 2 ? 16 : 10;
+};
+
+template <class real, int WPB>
+__global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
+    k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps, int ntile, int wpt,
+           const uint32_t *sweep_p, int mi, const char *descs, size_t stride, real *scratch,
+           unsigned long long *stats, unsigned int *next_item) {
     extern __shared__ __align__(16) char smem[];
     __shared__ Desc<real> sd;
     __shared__ LaneLayout sLL;
-    int lane = threadIdx.x;
-    {
+    int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    {  // the block's warps share one copy of the descriptor
         const int4 *src = (const int4 *)(descs + (size_t)mi * stride);
         int4 *dst = (int4 *)smem;
-        for (size_t i = lane; i < stride / 16; i += 32) dst[i] = src[i];
+        for (size_t i = threadIdx.x; i < stride / 16; i += 32 * WPB) dst[i] = src[i];
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         sd = carve_desc<real>(smem, M, M.natoms + M.nextra);
         sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, linemove_maxroots(M), M.maxk, M.maxku);
     }
-    __syncwarp();
+    if (WPB == 1)
+        __syncwarp();
+    else
+        __syncthreads();
     Desc<real> &d = sd;
     const LaneLayout &LL = sLL;
     int fi = d.hdr[12];
     if (fi < 0) return;  // not a valid move: nothing to do (grid-uniform)
     // per-lane scratch: a local array (cached in L1, written back) when the layout fits it, else
-    // the lane's column of this block's slab in global memory
+    // the lane's column of this warp's slab in global memory
     real local[ESM_LANE_LOCAL];
     bool loc = LL.total <= ESM_LANE_LOCAL;
-    real *slab = loc ? local : scratch + (size_t)blockIdx.x * LL.total * 32 + lane;
+    real *slab = loc ? local : scratch + ((size_t)blockIdx.x * WPB + wib) * LL.total * 32 + lane;
     Lane<real> Ln(M, d, slab, loc ? 1 : 32, lane, LL);
     uint32_t sweep = *sweep_p;
     unsigned long long tried = 0, moved = 0, guards = 0;
@@ -1541,23 +1578,34 @@ size_t linemove_smem_per_warp(const DevModel<real> &M) {
     return (desc_bytes(M, M.natoms + M.nextra) + 15) & ~(size_t)15;
 }
 
-// warps of k_move resident per SM (one warp per block), for the grid and scratch of a context
+// warps of k_move resident per SM with blocks of wpb warps (1, 2 or 4), for the grid and scratch
+// of a context
 template <class real>
-int linemove_blocks_per_sm(const DevModel<real> &M) {
+int linemove_blocks_per_sm(const DevModel<real> &M, int wpb) {
     int nb = 0;
     size_t stride = linemove_smem_per_warp(M);
     // (the dynamic shared memory limits are set here, at context creation, so that no later call --
     // possibly under stream capture -- has to)
     cudaFuncSetAttribute(k_prep_moves<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_move<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real>, 32, stride) != cudaSuccess || nb < 1) nb = 16;
-    return nb;
+    cudaError_t e;
+    if (wpb == 4) {
+        cudaFuncSetAttribute(k_move<real, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real, 4>, 128, stride);
+    } else if (wpb == 2) {
+        cudaFuncSetAttribute(k_move<real, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real, 2>, 64, stride);
+    } else {
+        cudaFuncSetAttribute(k_move<real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move<real, 1>, 32, stride);
+    }
+    if (e != cudaSuccess || nb < 1) nb = 16 / wpb;
+    return nb * wpb;
 }
 
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
-                              int limit, real *scratch, int max_warps, unsigned long long *stats, char *descs,
-                              unsigned int *counters, cudaStream_t s) {
+                              int limit, real *scratch, int wpb, int max_warps, unsigned long long *stats,
+                              char *descs, unsigned int *counters, cudaStream_t s) {
     int nmoves = M.natoms + M.nextra;
     int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
     size_t stride = linemove_smem_per_warp(M);
@@ -1569,9 +1617,17 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
     int wpt = (M.span * M.R + 31) / 32;
     int items = ntile * wpt;
     int warps = items < max_warps ? items : max_warps;
+    int blocks = (warps + wpb - 1) / wpb;
     for (int mi = 0; mi < nrun; ++mi) {
-        k_move<real><<<warps, 32, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch, stats,
-                                               counters + mi);
+        if (wpb == 4)
+            k_move<real, 4><<<blocks, 128, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
+                                                       stats, counters + mi);
+        else if (wpb == 2)
+            k_move<real, 2><<<blocks, 64, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
+                                                      stats, counters + mi);
+        else
+            k_move<real, 1><<<blocks, 32, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
+                                                      stats, counters + mi);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -22,7 +22,9 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
-           "esm_state_save", "esm_state_restore", "esm_regime_occupancy")
+           "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
+           "esm_autotune_moves")
+TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather")
 
 _lib = None
@@ -70,6 +72,9 @@ def load(build_if_missing=True):
                                     C.c_int64, P_f64, P_i32]
     L.esm_weather_step.argtypes = [C.c_void_p, P_i32, P_f64, P_i32, P_i32, P_f64, C.c_int64]
     L.esm_sync.argtypes = [C.c_void_p, C.c_double]
+    L.esm_set_move_grid.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.esm_move_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
+    L.esm_autotune_moves.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
     L.esm_launch_count.restype = C.c_int64
     L.esm_launch_count.argtypes = [C.c_void_p]
     L.esm_set_timing.argtypes = [C.c_void_p, C.c_int32]
@@ -215,6 +220,28 @@ class DeviceChain:
         xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
         self._check(self.L.esm_weather_step(self.h, _p(moved, P_i32), _p(theta), _p(window, P_i32),
                                             _p(wstart, P_i32), _p(xi), it), "esm_weather_step")
+
+    def set_move_grid(self, warps_per_block=1, warps_per_sm=0):
+        """Line-move grid: blocks of 1, 2 or 4 warps, resident warps per SM (0: that shape's limit)."""
+        self._check(self.L.esm_set_move_grid(self.h, int(warps_per_block), int(warps_per_sm)), "esm_set_move_grid")
+
+    def move_grid(self):
+        """(warps per block, warps per SM, limits per SM of the 1-, 2- and 4-warp shapes)."""
+        b, w, lim = np.zeros(1, np.int32), np.zeros(1, np.int32), np.zeros(3, np.int32)
+        self._check(self.L.esm_move_grid(self.h, _p(b, P_i32), _p(w, P_i32), _p(lim, P_i32)), "esm_move_grid")
+        return int(b[0]), int(w[0]), tuple(int(x) for x in lim)
+
+    def autotune_moves(self, sweep=0):
+        """Pick the line-move grid by timing one colour class per candidate (the state is restored
+        after each); returns ((warps per block, warps per SM), {(wpb, wps): ms})."""
+        best = np.zeros(2, np.int32)
+        cand = np.zeros(2 * TUNE_MAX, np.int32)
+        ms = np.zeros(TUNE_MAX)
+        n = np.zeros(1, np.int32)
+        self._check(self.L.esm_autotune_moves(self.h, sweep, _p(best, P_i32), _p(cand, P_i32), _p(ms), _p(n, P_i32)),
+                    "esm_autotune_moves")
+        return (int(best[0]), int(best[1])), {(int(cand[2 * i]), int(cand[2 * i + 1])): float(ms[i])
+                                              for i in range(int(n[0]))}
 
     def sync(self, timeout_s=60.0):
         self._check(self.L.esm_sync(self.h, timeout_s), "esm_sync")

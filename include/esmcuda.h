@@ -202,6 +202,27 @@ int esm_follow_capacities(esm_ctx *ctx, const double *knew, double kappa_min, do
 int esm_state_save(esm_ctx *ctx);
 int esm_state_restore(esm_ctx *ctx);
 
+/* The line-move grid. k_move runs as blocks of 1, 2 or 4 warps whose warps take work items from a
+   per-move counter, so any grid is correct. The block shape sets the register budget (80, 64 and
+   48 registers per thread) and with it the warps an SM holds (up to 24, 32 and 40); the warp count
+   trades latency hiding against the cache footprint of the warps' walk scratch. esm_set_move_grid
+   sets warps_per_block (1, 2, 4) and warps_per_sm (0: the resident limit of that shape; capped at
+   it) and drops the captured class graphs; the default is one-warp blocks at their limit.
+   esm_move_grid reads the current shape, warps per SM and the limits of the three shapes
+   (limits_per_sm[3]). No reference counterpart (the reference threads the steps of a class on the
+   host, src/local.jl:1954). */
+int esm_set_move_grid(esm_ctx *ctx, int32_t warps_per_block, int32_t warps_per_sm);
+int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limits_per_sm);
+
+/* Autotuner of the line-move grid: for each candidate (warps_per_block, warps_per_sm) -- the three
+   block shapes at their resident limits and at 8, 16, 24, 32, 40 warps per SM below them -- one
+   colour class of sweep `sweep` is run and timed (CUDA events on the context's stream) from the
+   current state, which is then restored, and the fastest grid is kept. The chain state is
+   unchanged; the esm_state_save slot is overwritten. Outputs (each may be NULL): the chosen pair
+   best[2], the candidate pairs cand[2*ESM_TUNE_MAX], their times in ms ms[ESM_TUNE_MAX], their count. */
+#define ESM_TUNE_MAX 16
+int esm_autotune_moves(esm_ctx *ctx, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand);
+
 /* Fraction of (step, replica) pairs in each (regime, season): occ [nreg*4], regime-major, the
    season of a step as season (src/weather.jl:50). The regime summary fed to the surrogate. */
 int esm_regime_occupancy(esm_ctx *ctx, double *occ);

@@ -101,6 +101,48 @@ def test_class_pass_fp64(base):
     assert frac <= 0.02
 
 
+@pytest.mark.parametrize("wpb,wps", [(1, 8), (2, 0), (4, 0), (4, 16)])
+def test_class_pass_fp64_grids(base, wpb, wps):
+    """The same class pass with every k_move block shape and a reduced grid: the work items are
+    taken from a per-move counter, so the grid must not change the result."""
+    m, st = base
+    d = DeviceChain(m, 32, precision=64, seed=5)
+    d.upload(st)
+    d.set_move_grid(wpb, wps)
+    assert d.move_grid()[0] == wpb
+    d.rebuild()
+    o = Oracle(m, 32, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    sd = d.class_pass(3, 0)
+    so = o.class_pass(3, 0)
+    assert np.array_equal(sd[:20:2], so[:20:2])
+    assert sd[-1] == so[-1] == 0
+    frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
+    assert frac <= 0.02
+
+
+def test_autotune_keeps_state(base):
+    """esm_autotune_moves times candidate grids from the current state and restores it: the chain
+    state after tuning equals the state before, and a sweep afterwards matches an untuned chain."""
+    m, st = base
+    d = DeviceChain(m, 32, precision=64, seed=5)
+    d.upload(st)
+    before = d.download()
+    (wpb, wps), times = d.autotune_moves(sweep=3)
+    assert (wpb, wps) in times and len(times) >= 3
+    assert d.move_grid()[:2] == (wpb, wps)
+    after = d.download()
+    for k in ("theta", "g", "e", "z", "k"):
+        assert np.array_equal(before[k], after[k]), k
+    d2 = DeviceChain(m, 32, precision=64, seed=5)
+    d2.upload(st)
+    s1, s2 = d.sweeps(1, 4), d2.sweeps(1, 4)
+    assert np.array_equal(s1, s2)
+    a, b = d.download(), d2.download()
+    assert (np.abs(a["g"] - b["g"]).max(0) > 1e-9).mean() <= 0.02
+
+
 @pytest.mark.parametrize("limit", [1, 5, 20])
 def test_moves_fp32(equilibrated, limit):
     """The first `limit` moves of every task of the FP32 build on identical states. A task whose
