@@ -2,9 +2,11 @@
 """Replica-sampler step throughput on GB300 (the hot path of ESM-Sampling's `sampler = "replicas"`).
 
 A step is one replica step of one chain (replica_step!, src/replicas.jl:676): the scheduled weather
-bursts with their compensated re-initialisation, one operation sweep (local_sweep!, plain families)
-of every replica, the capacity scores, the replica-averaged Langevin step of the shared capacities
-and the dispatch following. Workload: 40 nodes, 60 lines, hourly T = 8760, 64 weather replicas
+bursts with their compensated re-initialisation, one operation sweep of every replica (operation_sweep!,
+src/local.jl:2401: the local sweep with the plain families; with --storage-ms also the storage
+multiscale sweep with probability 1/2, as operation_sweep! runs it), the capacity scores, the
+replica-averaged Langevin step of the shared capacities and the dispatch following. The storage
+multiscale sweep is also timed on its own (one forced sweep) and reported as `storage_ms`. Workload: 40 nodes, 60 lines, hourly T = 8760, 64 weather replicas
 (the "plain method on GPU" configuration), synthetic seeded data.
 
   value  device throughput: sweeps of all replicas per second from CUDA-event spans on the
@@ -95,13 +97,13 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def setup_chain(precision=32):
+def setup_chain(precision=32, storage_ms=0):
     from esmgb.device import DeviceChain
     from esmgb.model import initial_state, make_model
     w = WORKLOAD
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
     st = initial_state(m, w["R"], seed=7)
-    d = DeviceChain(m, w["R"], precision=precision, seed=w["seed"])
+    d = DeviceChain(m, w["R"], precision=precision, seed=w["seed"], storage_ms=storage_ms)
     d.upload(st)
     return m, st, d
 
@@ -182,17 +184,21 @@ def e2e_loop(d, m, ctl, R_set, it0, n, rng):
     return h2d / n, d2h / n
 
 
-def cpu_sample(threads, sweeps=1, R=2):
-    """The oracle on the host cores: one operation sweep and the scores of R of the replicas."""
+def cpu_sample(threads, sweeps=1, R=2, storage_ms=0):
+    """The oracle on the host cores: operation sweeps from sweep 1 and the scores of R of the
+    replicas; with storage_ms, two sweeps (the storage multiscale sweep runs in sweep 1, not in 2:
+    its coin, probability 1/2)."""
+    if storage_ms:
+        sweeps = 2
     from esmgb.model import initial_state, make_model
     from oracle.oracle import Oracle
     w = WORKLOAD
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
     st = initial_state(m, R, seed=7)
-    o = Oracle(m, R, seed=w["seed"], threads=threads)
+    o = Oracle(m, R, seed=w["seed"], threads=threads, storage_ms=storage_ms)
     o.set_state(st)
     t0 = time.perf_counter()
-    o.sweeps(sweeps, 0)
+    o.sweeps(sweeps, 1)
     o.scores()
     dt = time.perf_counter() - t0
     return sweeps * (R / w["R"]) / dt, dt
@@ -206,16 +212,16 @@ def run_reference(args):
     from oracle import oracle as O
     O.build()
     for _ in range(args.warmup):
-        cpu_sample(threads, 1, 1)
+        cpu_sample(threads, 1, 1, int(args.storage_ms))
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, _ = cpu_sample(threads, 1, 1)
+        v, _ = cpu_sample(threads, 1, 1, int(args.storage_ms))
         vals.append(v)
     wall = time.perf_counter() - t0
     value = args.steps / sum(1.0 / v for v in vals)
-    sample = (f"each step: one operation sweep and the capacity scores of 1 of the 64 replicas "
-              f"(T = 8760), scaled to 64 replicas")
+    sample = (f"each step: one operation sweep (with --storage-ms: sweeps 1 and 2, the storage multiscale sweep "
+              f"in the first) and the capacity scores of 1 of the 64 replicas (T = 8760), scaled to 64 replicas")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -311,6 +317,8 @@ def main():
     ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--storage-ms", action="store_true",
+                    help="operation sweeps include the storage multiscale sweep (probability 1/2)")
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
     ap.add_argument("--case", default="full", choices=["full", "small", "batch"],
@@ -333,7 +341,7 @@ def main():
     from esmgb import build as B
     B.build()
     from esmgb import replicas as RP
-    m, st, d = setup_chain(32)
+    m, st, d = setup_chain(32, storage_ms=int(args.storage_ms))
     R = d.R
     # the line-move grid picked by the library's autotuner (one timed colour class per candidate,
     # state restored), untimed setup; --grid WPBxWPS fixes it instead (profiler runs)
@@ -380,6 +388,12 @@ def main():
     d.sync(600.0)
     e2e_wall = time.perf_counter() - t0
     e2e = world * args.steps / e2e_wall
+    # the storage multiscale sweep on its own (one forced sweep, every class pass), device time
+    d.sync(600.0)
+    d.set_timing(True)
+    sms = d.storage_ms(it0 + args.warmup + 2 * args.steps, force=True)
+    d.sync(600.0)
+    sms_ms = d.timing()["storage"][0]
     if rank != 0:
         return
     # roofline of the dominant kernels (one colour class: k_prep_moves and one k_move launch per
@@ -413,16 +427,19 @@ def main():
                           "autotune_ms_per_class": {f"{a}x{b}": round(v, 1) for (a, b), v in grid_ms.items()}},
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
             "line_moves_per_s": moves * args.steps / (dev_ms / 1000.0) * world,
+            "storage_ms": {"ms_per_sweep": sms_ms, "moves": int(sms[0]), "moves_taken": int(sms[1]),
+                           "note": "storage multiscale sweep (plateau moves) timed alone; it runs in half of "
+                                   "the operation sweeps with --storage-ms"},
             "wall_device_loop_s": wall_dev}
     if not args.no_cpu_baseline:
         try:
             from oracle import oracle as O
             O.build()
             threads = os.cpu_count() or 1
-            v, dt = cpu_sample(threads, 1, args.cpu_replicas)
+            v, dt = cpu_sample(threads, 1, args.cpu_replicas, int(args.storage_ms))
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": f"one operation sweep and the scores of {args.cpu_replicas} of the "
-                                              f"64 replicas at T = 8760 ({dt:.1f} s), scaled to 64 replicas"}
+                                    "sample": f"operation sweep(s) from sweep 1 and the scores of {args.cpu_replicas} "
+                                              f"of the 64 replicas at T = 8760 ({dt:.1f} s), scaled to 64 replicas"}
         except Exception as e:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
     print(json.dumps(line), flush=True)

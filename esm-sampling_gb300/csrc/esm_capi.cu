@@ -81,6 +81,12 @@ struct esm_ctx {
     unsigned long long *d_occ = nullptr;
     unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
     uint32_t *d_sweep = nullptr;         // the sweep index of the current class pass
+    // storage multiscale sweep
+    int storage_ms = 0;
+    std::vector<int> sgp, sgu;           // storage groups (host copies)
+    int sms_threads = 0;
+    void *d_sms_scratch = nullptr;
+    unsigned long long *d_sms_stats = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // a whole class pass, per class
     // weather
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
@@ -98,8 +104,8 @@ struct esm_ctx {
     };
     vector<Mark> marks;
     vector<cudaEvent_t> pool;
-    double acc_ms[ESM_KT_N] = {0, 0, 0, 0, 0};
-    double acc_n[ESM_KT_N] = {0, 0, 0, 0, 0};
+    double acc_ms[ESM_KT_N] = {};
+    double acc_n[ESM_KT_N] = {};
 };
 
 namespace {
@@ -459,6 +465,13 @@ int alloc_state(esm_ctx *c) {
     if ((rc = dalloc(c, &ctr, (size_t)(M.natoms + M.nextra)))) return rc;
     c->d_item_ctr = ctr;
     if ((rc = dalloc(c, &c->d_sweep, 1))) return rc;
+    // storage multiscale sweep: resident threads of its kernel and, when the lane layout exceeds the
+    // local arrays, one global scratch column per thread
+    c->sms_threads = esm::plateau_threads<real>(M);
+    size_t sper = esm::plateau_scratch_reals<real>(M);
+    if ((rc = dalloc(c, &q, sper * (size_t)c->sms_threads))) return rc;
+    c->d_sms_scratch = q;
+    if ((rc = dalloc(c, &c->d_sms_stats, 3))) return rc;
     return ESM_OK;
 }
 
@@ -666,6 +679,18 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         if ((rc = build_model<double>(c, m, o))) return rc;
         if ((rc = alloc_shadow(c))) return rc;
     }
+    // storage multiscale sweep: the groups and the limits of its kernel
+    c->storage_ms = o->storage_ms != 0;
+    if (m->nsgroups > 0 && m->sgroup_ptr && m->sgroup_units) {
+        c->sgp.assign(m->sgroup_ptr, m->sgroup_ptr + m->nsgroups + 1);
+        c->sgu.assign(m->sgroup_units, m->sgroup_units + c->sgp[m->nsgroups]);
+    }
+    for (size_t g = 0; g + 1 < c->sgp.size(); ++g)
+        if (c->sgp[g + 1] - c->sgp[g] > ESM_PLAT_MAXU)
+            return fail(c, ESM_EINVAL, "a storage group has more than %d units", ESM_PLAT_MAXU);
+    for (int n = 0; n < m->N; ++n)
+        if (m->units_ptr[n + 1] - m->units_ptr[n] > ESM_PLAT_MAXK)
+            return fail(c, ESM_EINVAL, "a node has more than %d dispatchable units", ESM_PLAT_MAXK);
     // classes
     c->ncls = c->T % 2 ? 3 : 2;
     c->class_len.assign(3, 0);
@@ -831,6 +856,110 @@ int esm_class_pass(esm_ctx *c, int64_t sweep, int32_t cls, int32_t move_limit, i
     return stats_out(c, stats);
 }
 
+namespace {
+// sequential uniforms of one Philox stream (the oracle's PStream)
+struct HStream {
+    uint64_t seed;
+    uint32_t tag, w1, w2, w3, j = 0;
+    double next() {
+        double u0, u1;
+        esm::uniform2(seed, tag, j >> 1, w1, w2, w3, &u0, &u1);
+        double u = (j & 1) ? u1 : u0;
+        ++j;
+        return u;
+    }
+    int pick(int n) {
+        int i = (int)floor(next() * n);
+        return i >= n ? n - 1 : i;
+    }
+};
+
+// The class passes of the storage multiscale sweep of one operation sweep (storage_ms_sweep!,
+// src/flowmoves.jl:255): its coin (probability 1/2, operation_sweep!, src/local.jl:2417; skipped
+// with force), the lengths 2 .. 128 below T/2 in random order, per length a random offset and the
+// order of the two block parities; then the 8 move selections of every pass (a cell-class aggregate
+// with probability 1/2, else one unit). The oracle draws the same streams.
+int sms_plan(const esm_ctx *c, uint32_t sweep, bool force, std::vector<esm::PlatMoves> &out) {
+    out.clear();
+    HStream st{c->seed, ESM_TAG_SMS, 0u, 0u, sweep};
+    bool run = st.next() < 0.5;
+    if ((!run && !force) || c->S == 0) return 0;
+    int lens[7], nl = 0;
+    for (int L = 2; L <= 128; L *= 2)
+        if (L < c->T / 2) lens[nl++] = L;
+    for (int i = nl - 1; i >= 1; --i) std::swap(lens[i], lens[st.pick(i + 1)]);
+    int ng = (int)c->sgp.size() - 1;
+    for (int q = 0; q < nl; ++q) {
+        int L = lens[q];
+        int o = st.pick(L);
+        bool swap01 = st.next() >= 0.5;
+        int nb = 0;
+        for (int b0 = o; b0 + L <= c->T - 1; b0 += L) ++nb;
+        if (nb < 2) continue;
+        int li = 0;
+        while ((2 << li) < L) ++li;
+        for (int h = 0; h < 2; ++h) {
+            esm::PlatMoves mv{};
+            mv.L = L;
+            mv.o = o;
+            mv.cls = swap01 ? 1 - h : h;
+            mv.li = li;
+            mv.nb = (nb - mv.cls + 1) / 2;
+            HStream ms{c->seed, ESM_TAG_SMS, 1u + (uint32_t)li, 2u + (uint32_t)mv.cls, sweep};
+            for (int k = 0; k < 8; ++k) {
+                if (ms.next() < 0.5 && ng > 0) {
+                    int gi = ms.pick(ng);
+                    mv.nu[k] = c->sgp[gi + 1] - c->sgp[gi];
+                    for (int p = 0; p < mv.nu[k]; ++p) mv.j[k][p] = c->sgu[c->sgp[gi] + p];
+                } else {
+                    mv.nu[k] = 1;
+                    mv.j[k][0] = ms.pick(c->S);
+                }
+            }
+            out.push_back(mv);
+        }
+    }
+    return (int)out.size();
+}
+
+// the storage multiscale sweep of one operation sweep: caches rebuilt (LocalCost at the start of
+// storage_ms_sweep!, src/flowmoves.jl:261), then one launch per class pass
+int sms_sweep_any(esm_ctx *c, uint32_t sweep, bool force, int max_passes = 0) {
+    std::vector<esm::PlatMoves> plan;
+    if (sms_plan(c, sweep, force, plan) == 0) return ESM_OK;
+    if (max_passes > 0 && (size_t)max_passes < plan.size()) plan.resize(max_passes);
+    int rc = rebuild_any(c);
+    if (rc) return rc;
+    Span sp(c, ESM_KT_STORAGE);
+    for (auto &mv : plan) {
+        if (c->precision == 64)
+            CK(esm::launch_plateau<double>(c->Md, mv, sweep, (double *)c->d_sms_scratch, c->sms_threads,
+                                           c->d_sms_stats, c->stream));
+        else
+            CK(esm::launch_plateau<float>(c->Mf, mv, sweep, (float *)c->d_sms_scratch, c->sms_threads,
+                                          c->d_sms_stats, c->stream));
+        c->launches += 1;
+    }
+    return ESM_OK;
+}
+}  // namespace
+
+int esm_storage_ms(esm_ctx *c, int64_t sweep, int32_t force, int32_t max_passes, int64_t *stats) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    CK(cudaMemsetAsync(c->d_sms_stats, 0, sizeof(unsigned long long) * 3, c->stream));
+    int rc = sms_sweep_any(c, (uint32_t)sweep, force != 0, max_passes);
+    if (rc) return rc;
+    c->has_scores = false;
+    if (stats) {
+        unsigned long long h[3];
+        CK(cudaMemcpyAsync(h, c->d_sms_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        if ((rc = esm_sync(c, 600.0))) return rc;
+        for (int i = 0; i < 3; ++i) stats[i] += (int64_t)h[i];
+    }
+    return ESM_OK;
+}
+
 int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) {
     if (!c) return ESM_EINVAL;
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
@@ -843,6 +972,7 @@ int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) 
         class_order(c, sw, order, &nc);
         for (int q = 0; q < nc; ++q)
             if ((rc = class_pass_any(c, sw, order[q]))) return rc;
+        if (c->storage_ms && (rc = sms_sweep_any(c, sw, false))) return rc;
     }
     c->has_scores = false;
     return stats_out(c, stats);

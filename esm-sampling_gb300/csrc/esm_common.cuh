@@ -10,6 +10,8 @@
 #define ESM_TAG_LANE 0x4C414E45u
 #define ESM_TAG_LGV 0x4C475600u
 #define ESM_TAG_WTH 0x57544800u
+#define ESM_TAG_SMS 0x534D5300u
+#define ESM_TAG_SML 0x534D4C00u
 
 namespace esm {
 

@@ -19,4 +19,21 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
 // resident k_move warps per SM with blocks of wpb (1, 2 or 4) warps
 template <class real>
 int linemove_blocks_per_sm(const DevModel<real> &M, int wpb);
+
+// ---- storage multiscale sweep (esm_plateau.cuh)
+#define ESM_PLAT_MAXU 32  // units of one plateau move (a cell-class aggregate)
+#define ESM_PLAT_MAXK 8   // dispatchable units at one node taking part in the compensation
+// the moves of one class pass, drawn on the host
+struct PlatMoves {
+    int L, o, cls, li, nb;      // length, offset, block parity, length index, blocks of the class
+    int nu[8];                  // units per move
+    int j[8][ESM_PLAT_MAXU];    // storage unit indices (into stor)
+};
+template <class real>
+int plateau_threads(const DevModel<real> &M);  // resident threads of k_plateau
+template <class real>
+size_t plateau_scratch_reals(const DevModel<real> &M);  // global scratch per thread (0: local arrays)
+template <class real>
+cudaError_t launch_plateau(const DevModel<real> &M, const PlatMoves &mv, uint32_t sweep, real *scratch, int threads,
+                           unsigned long long *stats, cudaStream_t s);
 }  // namespace esm

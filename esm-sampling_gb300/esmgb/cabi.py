@@ -39,6 +39,7 @@ class EsmModel(C.Structure):
         ("xpart_ptr", P_i32), ("xpart", P_i32), ("xnod_ptr", P_i32), ("xnod", P_i32), ("xval", P_f64),
         ("xlk_ptr", P_i32), ("xlkn", P_i32), ("xlkg", P_f64),
         ("reroute", P_f64), ("comp", P_i32),
+        ("nsgroups", C.c_int32), ("sgroup_ptr", P_i32), ("sgroup_units", P_i32),
     ]
 
 
@@ -46,7 +47,7 @@ class EsmOpts(C.Structure):
     _fields_ = [
         ("R", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64), ("extra", C.c_double),
         ("maxnats", C.c_double), ("kappa_min", C.c_double), ("max_points", C.c_int32), ("span", C.c_int32),
-        ("family_rates", C.c_double * NFAM),
+        ("family_rates", C.c_double * NFAM), ("storage_ms", C.c_int32),
     ]
 
 
@@ -106,16 +107,31 @@ class ModelBuffers:
         s.xpart_ptr, s.xpart, s.xnod_ptr, s.xnod = ip(m.xpart_ptr), ip(m.xpart), ip(m.xnod_ptr), ip(m.xnod)
         s.xval, s.xlk_ptr, s.xlkn, s.xlkg = fp(m.xval), ip(m.xlk_ptr), ip(m.xlkn), fp(m.xlkg)
         s.reroute, s.comp = fp(m.reroute.ravel()), ip(m.comp)
+        gptr, gunits = storage_groups(m)
+        s.nsgroups, s.sgroup_ptr, s.sgroup_units = len(gptr) - 1, ip(gptr), ip(gunits)
         self.struct = s
         self._keep = keep
         self.natoms = int(fap[-1])
 
 
+def storage_groups(m: SynthModel):
+    """The cell-class aggregates of the storage multiscale sweep (src/flowmoves.jl:270-274): the
+    storage units grouped by (country cell of their node, carrier), keys in sorted order, units in
+    storage order; CSR (ptr, units as indices into stor)."""
+    groups = {}
+    for j, u in enumerate(m.stor):
+        groups.setdefault((int(m.country[m.unit_bus[u]]), int(m.unit_group[u])), []).append(j)
+    keys = sorted(groups)
+    ptr = np.cumsum([0] + [len(groups[k]) for k in keys]).astype(np.int32)
+    units = np.array([j for k in keys for j in groups[k]], np.int32)
+    return ptr, units
+
+
 def make_opts(R, precision=32, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-              rates=FAMILY_RATES) -> EsmOpts:
+              rates=FAMILY_RATES, storage_ms=0) -> EsmOpts:
     o = EsmOpts()
     o.R, o.precision, o.seed, o.extra, o.maxnats, o.kappa_min = R, precision, seed, extra, maxnats, kappa_min
-    o.max_points, o.span = max_points, span
+    o.max_points, o.span, o.storage_ms = max_points, span, int(storage_ms)
     for i, r in enumerate(rates):
         o.family_rates[i] = r
     return o

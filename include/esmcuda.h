@@ -107,6 +107,11 @@ typedef struct esm_model {
     /* global re-routing (src/local.jl:44 GridSolver): column n of the grounded inverse */
     const double *reroute;                 /* [N*N], element (i, n) at i*N + n */
     const int32_t *comp;                   /* AC component per node */
+    /* storage multiscale sweep (src/flowmoves.jl:255 storage_ms_sweep!): the storage units grouped
+       by (cell of their node in the country partition, carrier) -- the cell-class aggregates of its
+       plateau moves -- as CSR over indices into stor */
+    int32_t nsgroups;
+    const int32_t *sgroup_ptr, *sgroup_units;
 } esm_model;
 
 /* Sampler options (src/run.jl:20 local_extra; src/local.jl:1294 maxnats; ReplicaCtl defaults
@@ -122,6 +127,9 @@ typedef struct esm_opts {
                                   esm_auto_max_points of the largest state-of-charge atom */
     int32_t span;              /* class steps sharing one move list (0: max(1, 32/R)) */
     double family_rates[ESM_NFAM];
+    int32_t storage_ms;        /* 1: an operation sweep runs, after the local sweep, the storage multiscale
+                                  sweep with probability 1/2 (operation_sweep!, src/local.jl:2417);
+                                  0: the local sweep only */
 } esm_opts;
 
 /* The automatic point cap: 192, or 4 points per unit of the largest state-of-charge atom when that
@@ -161,6 +169,17 @@ int esm_operation_sweeps(esm_ctx *ctx, int32_t n, int64_t sweep0, int64_t *stats
 /* One colour class of one sweep (parity tests): class cls (0: even 0-based steps, 1: odd, 2: the
    last step of an odd year); only the first move_limit entries of every move list when > 0. */
 int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int32_t move_limit, int64_t *stats);
+
+/* The storage multiscale sweep of sweep `sweep` (storage_ms_sweep!, src/flowmoves.jl:255) in its
+   plateau form: for the dyadic lengths 2 .. 128 below T/2 (random order, random offset), blocks of
+   one parity at a time, 8 moves per block, each raising the state of charge of one storage unit or
+   of a cell-class aggregate (esm_model.sgroup_*) over the block's instants with pro-rata
+   compensation at its end steps and the Jacobian test. It runs with probability 1/2 per sweep
+   (operation_sweep!, src/local.jl:2417) unless force is set; esm_operation_sweeps calls it after
+   the local sweep when esm_opts.storage_ms is 1. max_passes > 0 runs only the first class passes
+   of the sweep (a diagnostic, as move_limit of esm_class_pass). stats (may be NULL) += (moves
+   tried, moves taken, guard events). */
+int esm_storage_ms(esm_ctx *ctx, int64_t sweep, int32_t force, int32_t max_passes, int64_t *stats);
 
 /* Capacity scores per replica: sk [R*K] (s_k = -beta_v dC/dk + dlogJ/dk, node space) and the
    capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with
@@ -236,7 +255,7 @@ int esm_weather_step(esm_ctx *ctx, const int32_t *moved, const double *theta,
                      const int32_t *window, const int32_t *wstart, const double *xi, int64_t it);
 
 /* Kernel families of the device timing (esm_timing). */
-enum { ESM_KT_CLASS = 0, ESM_KT_REBUILD, ESM_KT_SCORE, ESM_KT_LANGEVIN, ESM_KT_WEATHER, ESM_KT_N };
+enum { ESM_KT_CLASS = 0, ESM_KT_REBUILD, ESM_KT_SCORE, ESM_KT_LANGEVIN, ESM_KT_WEATHER, ESM_KT_STORAGE, ESM_KT_N };
 
 /* Device timing: while on, every launch of the library is bracketed by CUDA events on the
    context's stream. esm_timing writes out[2*i] = accumulated milliseconds and out[2*i+1] = launches

@@ -51,6 +51,7 @@ struct Model {
     vector<int> xpp, xp, xnp, xn, xlp, xln;
     vector<double> xv, xlg, Z;
     vector<int> comp;
+    vector<int> sgp, sgu;   // storage groups (country cell, carrier) -> indices into stor
     vector<int> theta_nnz;  // theta atoms touching node n
     vector<int> disp_of_unit, stor_of_unit;
 };
@@ -65,6 +66,7 @@ struct Opts {
     uint64_t seed;
     double extra, maxnats, kmin;
     double rates[ESM_NFAM];
+    int storage_ms;
 };
 
 struct Ctx {
@@ -75,6 +77,7 @@ struct Ctx {
     vector<int> reg;
     vector<double> sk_last, fk_last;  // scores of the last capacity_scores call
     bool has_scores = false;
+    int64_t sms_stats[3] = {0, 0, 0};  // storage multiscale moves of orc_sweeps: tried, taken, guards
 };
 
 static inline size_t ix(const Ctx &c, int x, int t, int rep) {
@@ -422,26 +425,31 @@ static double eval_ws(const Ctx &c, WS &w, int rep, double t, const WS *next, ve
     return D;
 }
 
-// a prepared block move over (tau-1, tau) (BlockMove, src/local.jl:1196): ws = step tau, wa = tau-1
+// a prepared block move over consecutive steps (BlockMove, src/local.jl:1196), steps in time
+// order: (tau-1, tau) for the local families, b0 .. b0+L for a storage plateau
 struct Mover {
     const Ctx *c;
-    WS *ws, *wa;
+    vector<WS *> w;
     int rep;
     double beta;
     vector<double> sec;
-    double eval(double t) {  // mv_eval! (src/local.jl:1219): later step first
+    double eval(double t) {  // mv_eval! (src/local.jl:1219): later steps first
         sec.clear();
         double D = 0.0;
-        D += eval_ws(*c, *ws, rep, t, nullptr, sec);
-        D += eval_ws(*c, *wa, rep, t, ws, sec);
+        int n = (int)w.size();
+        for (int q = n - 1; q >= 0; --q) D += eval_ws(*c, *w[q], rep, t, q + 1 < n ? w[q + 1] : nullptr, sec);
         return D;
     }
-    bool hasstor() const { return !ws->stu.empty() || !wa->stu.empty(); }
-    void mask(vector<char> &g) const {  // storage_mask! (src/local.jl:1244)
+    bool hasstor() const {
+        for (const WS *x : w)
+            if (!x->stu.empty()) return true;
+        return false;
+    }
+    void mask(vector<char> &g) const {  // storage_mask! (src/local.jl:1244), in evaluation order
         g.clear();
-        for (const WS *w : {ws, wa}) {
-            for (size_t j = 0; j < w->stu.size() * 3; ++j) g.push_back(1);
-            for (size_t j = 0; j < w->nodes.size(); ++j) g.push_back(0);
+        for (int q = (int)w.size() - 1; q >= 0; --q) {
+            for (size_t j = 0; j < w[q]->stu.size() * 3; ++j) g.push_back(1);
+            for (size_t j = 0; j < w[q]->nodes.size(); ++j) g.push_back(0);
         }
     }
 };
@@ -571,7 +579,7 @@ static int walk(Walk &W, Mover &mv, vector<double> &bp, double sgn, double maxna
 // walk exceeded the point cap (the move is then not taken)
 static double sample_line(Mover &mv, double maxnats, int cap, double u_cat, double u_off, bool *guard) {
     vector<double> right, left;
-    for (const WS *w : {mv.wa, mv.ws})
+    for (const WS *w : mv.w)
         for (double x : w->bps) {
             if (!std::isfinite(x)) continue;
             if (x > 0.0)
@@ -633,7 +641,7 @@ static void commit(Ctx &c, Mover &mv, double t) {
     if (t == 0.0) return;
     mv.eval(t);
     const Model &m = c.m;
-    for (WS *w : {mv.wa, mv.ws}) {
+    for (WS *w : mv.w) {
         int tau = w->tau;
         for (auto &en : w->ent) {
             double d = t * en.a + (en.kid >= 0 ? en.ak * w->kinks[en.kid].phi : 0.0);
@@ -708,7 +716,7 @@ static inline double kappa_unit(const Ctx &c, int j) {  // kappa_unit (src/local
 }
 
 // prorata! (src/local.jl:1782), plain model (no tracking kinks)
-static bool prorata(const Ctx &c, WS &w, int rep, int mnode, double g, vector<Kink> *jac) {
+static bool prorata(const Ctx &c, WS &w, int rep, int mnode, double g, vector<Kink> *jac, double qadj = 0.0) {
     const Model &m = c.m;
     if (g == 0.0) return false;
     int tau = w.tau;
@@ -725,7 +733,7 @@ static bool prorata(const Ctx &c, WS &w, int rep, int mnode, double g, vector<Ki
     }
     if (nu == 0) return false;
     if (fabs(Pm) < 1e-6) return false;
-    double Q = c.r[ix(c, mnode, tau, rep)] + Qs + 0.0;
+    double Q = c.r[ix(c, mnode, tau, rep)] + Qs + qadj;
     double e = Pm - std::max(Q, 0.0);
     double nm = (double)(nu - 1);
     w.kinks.push_back(Kink{Q, g, 0.0, Pm, e, nm});
@@ -878,7 +886,7 @@ static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int t
     int taum = (tau - 1 + T) % T;
     TileStream ts = ts0;  // the selection draws continue after the list draws
     vector<Kink> jac;
-    Mover mv{&c, &ws, &wa, rep, m.beta_v, {}};
+    Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
     size_t nrun = limit > 0 && (size_t)limit < moves.size() ? (size_t)limit : moves.size();
     for (size_t mi = 0; mi < nrun; ++mi) {
         ws.clear();
@@ -980,6 +988,196 @@ static void class_order(const Ctx &c, uint32_t sweep, int order[3], int *ncls) {
         j = std::min(1, (int)floor(u1 * 2));
         std::swap(order[1], order[j]);
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// storage multiscale sweep (storage_ms_sweep!, src/flowmoves.jl:255) in its plateau form (the
+// shapes need the flow basis, src/flowmoves.jl:302): energy of one storage unit, or of the units
+// of one carrier in one country cell, moved from step b0 to step b0 + L of a dyadic block
+// ------------------------------------------------------------------------------------------
+struct PStream {  // sequential uniforms of one Philox stream (tag, words 1-3)
+    uint64_t seed;
+    uint32_t tag, w1, w2, w3, j = 0;
+    double next() {
+        double u0, u1;
+        orc_uniform2(seed, tag, j >> 1, w1, w2, w3, &u0, &u1);
+        double u = (j & 1) ? u1 : u0;
+        ++j;
+        return u;
+    }
+    int pick(int n) {
+        int i = (int)floor(next() * n);
+        return i >= n ? n - 1 : i;
+    }
+};
+
+struct SmsPass {
+    int li, L, o, cls;
+};
+
+// The class passes of the storage multiscale sweep of one operation sweep: its coin (probability
+// 1/2, operation_sweep!, src/local.jl:2417; skipped with force), the lengths 2, 4, ..., 128 below
+// T/2 in random order, per length a random offset and the order of the two block parities.
+static int sms_plan(uint64_t seed, int T, uint32_t sweep, bool force, SmsPass *out) {
+    PStream st{seed, ESM_TAG_SMS, 0u, 0u, sweep};
+    bool run = st.next() < 0.5;
+    if (!run && !force) return 0;
+    int lens[7], nl = 0;
+    for (int L = 2; L <= 128; L *= 2)
+        if (L < T / 2) lens[nl++] = L;
+    for (int i = nl - 1; i >= 1; --i) {
+        int j = st.pick(i + 1);
+        std::swap(lens[i], lens[j]);
+    }
+    int n = 0;
+    for (int q = 0; q < nl; ++q) {
+        int L = lens[q];
+        int o = st.pick(L);
+        bool swap01 = st.next() >= 0.5;
+        int nb = 0;
+        for (int b0 = o; b0 + L <= T - 1; b0 += L) ++nb;
+        if (nb < 2) continue;
+        int li = 0;
+        while ((2 << li) < L) ++li;
+        out[n++] = SmsPass{li, L, o, swap01 ? 1 : 0};
+        out[n++] = SmsPass{li, L, o, swap01 ? 0 : 1};
+    }
+    return n;
+}
+
+// soc_qadj (src/local.jl:1826): nominal minus actual injection of the moved storage units at node
+// mnode and step tau
+static double soc_qadj(const Ctx &c, const vector<int> &us, int mnode, int tau, int rep) {
+    const Model &m = c.m;
+    int t1 = (tau + 1) % m.T;
+    double q = 0.0;
+    for (int j : us) {
+        int u = m.stor[j];
+        if (m.ubus[u] != mnode) continue;
+        double ye = c.e[ix(c, j, tau, rep)], ye1 = c.e[ix(c, j, t1, rep)];
+        double k = kcl(c, u), pc, mcx;
+        soc_power(m, u, m.dt, clampd(ye, 0.0, 1.0), clampd(ye1, 0.0, 1.0), &pc, &mcx);
+        q += k * m.uhours[u] * (ye1 - ye) / m.dt - k * (pc - mcx);
+    }
+    return q;
+}
+
+// prep_storage_ms! (src/flowmoves.jl:187), plateau: the state of charge of the units rises by t at
+// the instants b0+1 .. b0+L; the power changes at steps b0 (+kappa_s t) and b0+L (-kappa_s t) and
+// the dispatch at those nodes follows pro rata (prorata! with soc_qadj)
+static bool prep_plateau(const Ctx &c, vector<WS> &wss, int b0, int L, const vector<int> &us, int rep,
+                         vector<Kink> *jac) {
+    const Model &m = c.m;
+    int n = L + 1;
+    for (int q = 0; q < n; ++q) {
+        wss[q].clear();
+        wss[q].tau = b0 + q;
+    }
+    jac->clear();
+    for (int j : us)
+        for (int jj = 1; jj <= L; ++jj) wss[jj].add_entry(EK_SE, j, 1.0);
+    for (int q = 0; q < n; ++q) {
+        vector<int> gn;
+        vector<double> gv;
+        for (int j : us) {
+            int u = m.stor[j];
+            double ks = kcl(c, u) * m.uhours[u] / m.dt;
+            double e0 = q == 0 ? 0.0 : 1.0, e1 = q + 1 <= L ? 1.0 : 0.0;
+            double dg = ks * (e1 - e0);
+            if (dg == 0.0) continue;
+            int node = m.ubus[u];
+            size_t p = std::find(gn.begin(), gn.end(), node) - gn.begin();
+            if (p == gn.size()) {
+                gn.push_back(node);
+                gv.push_back(0.0);
+            }
+            gv[p] += dg;
+        }
+        for (size_t p = 0; p < gn.size(); ++p)
+            prorata(c, wss[q], rep, gn[p], gv[p], jac, soc_qadj(c, us, gn[p], wss[q].tau, rep));
+    }
+    bool nonempty = false;
+    for (int q = 0; q < n; ++q) {
+        finalize_ws(c, wss[q], rep);
+        nonempty |= !wss[q].ent.empty();
+    }
+    for (int q = 0; q + 1 < n; ++q) link_soc(m, wss[q], wss[q + 1]);
+    return nonempty;
+}
+
+// the 8 move selections of a class (shared by its blocks and replicas: selection reads only k and
+// the static tables): a cell-class aggregate with probability 1/2, else one unit
+static void sms_moves(const Ctx &c, uint32_t sweep, const SmsPass &ps, vector<vector<int>> &moves) {
+    const Model &m = c.m;
+    PStream st{c.o.seed, ESM_TAG_SMS, 1u + (uint32_t)ps.li, 2u + (uint32_t)ps.cls, sweep};
+    int ng = (int)m.sgp.size() - 1;
+    moves.assign(8, {});
+    for (int q = 0; q < 8; ++q) {
+        if (st.next() < 0.5 && ng > 0) {
+            int gi = st.pick(ng);
+            for (int p = m.sgp[gi]; p < m.sgp[gi + 1]; ++p) moves[q].push_back(m.sgu[p]);
+        } else {
+            moves[q].push_back(st.pick(m.S));
+        }
+    }
+}
+
+// one class pass: every block of the class parity, every replica, the 8 moves in order
+static void sms_pass(Ctx &c, uint32_t sweep, const SmsPass &ps, int64_t *stats3, int nthreads) {
+    const Model &m = c.m;
+    int T = m.T, R = c.o.R, L = ps.L;
+    vector<int> blocks;
+    int k = 0;
+    for (int b0 = ps.o; b0 + L <= T - 1; b0 += L, ++k)
+        if (k % 2 == ps.cls) blocks.push_back(b0);
+    vector<vector<int>> moves;
+    sms_moves(c, sweep, ps, moves);
+    int nb = (int)blocks.size();
+#pragma omp parallel num_threads(nthreads)
+    {
+        int64_t loc[3] = {0, 0, 0};
+        vector<WS> wss(L + 1);
+        for (auto &w : wss) w.init(m);
+        vector<Kink> jac;
+#pragma omp for schedule(dynamic, 1)
+        for (int q = 0; q < nb * R; ++q) {
+            int b0 = blocks[q / R], rep = q % R;
+            for (int mi = 0; mi < 8; ++mi) {
+                if (!prep_plateau(c, wss, b0, L, moves[mi], rep, &jac)) continue;
+                Mover mv{&c, {}, rep, m.beta_v, {}};
+                for (auto &w : wss) mv.w.push_back(&w);
+                uint32_t w0 = 2u * (8u * (uint32_t)ps.li + (uint32_t)mi);
+                double uc, uo, uj, un;
+                orc_uniform2(c.o.seed, ESM_TAG_SML, w0, (uint32_t)b0, (uint32_t)rep, sweep, &uc, &uo);
+                orc_uniform2(c.o.seed, ESM_TAG_SML, w0 + 1, (uint32_t)b0, (uint32_t)rep, sweep, &uj, &un);
+                bool guard = false;
+                double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
+                if (guard) loc[2] += 1;
+                if (t != 0.0 && !jac.empty()) {  // logjac (src/local.jl:1871)
+                    double lj = 0.0;
+                    for (auto &kk : jac) lj += kk.nm * log(fabs((std::max(kk.Q + kk.g * t, 0.0) + kk.e) / kk.Pm));
+                    if (uj >= exp(std::min(0.0, lj))) t = 0.0;
+                }
+                commit(c, mv, t);
+                loc[0] += 1;
+                loc[1] += t != 0.0;
+            }
+        }
+        for (auto &w : wss) w.clear();
+#pragma omp critical
+        for (int i = 0; i < 3; ++i) stats3[i] += loc[i];
+    }
+}
+
+// the storage multiscale sweep of one operation sweep (caches rebuilt first, as LocalCost at the
+// sweep's start, src/flowmoves.jl:261)
+static void sms_sweep(Ctx &c, uint32_t sweep, bool force, int64_t *stats3, int nthreads, int max_passes = 0) {
+    SmsPass ps[14];
+    int n = sms_plan(c.o.seed, c.m.T, sweep, force, ps);
+    if (max_passes > 0 && max_passes < n) n = max_passes;
+    if (n == 0 || c.m.S == 0) return;
+    rebuild(c, nthreads);
+    for (int i = 0; i < n; ++i) sms_pass(c, sweep, ps[i], stats3, nthreads);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1506,6 +1704,8 @@ void *orc_create(const esm_model *em, const esm_opts *eo) {
     m.xlg = cp_(em->xlkg, m.xlp[npair]);
     m.Z = cp_(em->reroute, (size_t)N * N);
     m.comp = cp_(em->comp, N);
+    m.sgp = cp_(em->sgroup_ptr, (size_t)em->nsgroups + 1);
+    m.sgu = cp_(em->sgroup_units, (size_t)m.sgp[em->nsgroups]);
     m.theta_nnz.assign(N, 0);
     for (int f = 0; f < m.nfields; ++f) {
         if (m.frole[f] != ESM_ROLE_THETA) continue;
@@ -1532,6 +1732,7 @@ void *orc_create(const esm_model *em, const esm_opts *eo) {
     o.maxnats = eo->maxnats;
     o.kmin = eo->kappa_min;
     for (int q = 0; q < ESM_NFAM; ++q) o.rates[q] = eo->family_rates[q];
+    o.storage_ms = eo->storage_ms;
     size_t TR = (size_t)m.T * o.R;
     c->theta.assign(N * TR, 0.0);
     c->g.assign(m.D * TR, 0.0);
@@ -1596,7 +1797,31 @@ void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
         int order[3], ncls;
         class_order(*c, sw, order, &ncls);
         for (int q = 0; q < ncls; ++q) class_pass(*c, sw, order[q], stats, nthreads);
+        if (c->o.storage_ms) {
+            int64_t s3[3] = {0, 0, 0};
+            sms_sweep(*c, sw, false, s3, nthreads);
+            for (int i = 0; i < 3; ++i) c->sms_stats[i] += s3[i];
+        }
     }
+}
+
+// the storage multiscale sweep of sweep `sweep` (with force, whatever its coin; max_passes > 0: its
+// first class passes only); stats3 += (moves tried, moves taken, guard events)
+void orc_storage_ms(void *p, int64_t sweep, int force, int max_passes, int64_t *stats3, int nthreads) {
+    sms_sweep(*(Ctx *)p, (uint32_t)sweep, force != 0, stats3, nthreads, max_passes);
+}
+
+// the class passes of the storage multiscale sweep of a sweep: (length, offset, parity) each
+int orc_storage_ms_plan(void *p, int64_t sweep, int force, int32_t *out) {
+    Ctx *c = (Ctx *)p;
+    SmsPass ps[14];
+    int n = sms_plan(c->o.seed, c->m.T, (uint32_t)sweep, force != 0, ps);
+    for (int i = 0; i < n; ++i) {
+        out[3 * i] = ps[i].L;
+        out[3 * i + 1] = ps[i].o;
+        out[3 * i + 2] = ps[i].cls;
+    }
+    return n;
 }
 
 // the move list of a tile (diagnostics): kind (-1 atom, else family), field, atom

@@ -53,6 +53,9 @@ def lib():
         L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
         L.orc_set_caches.argtypes = [C.c_void_p, P_f64, P_f64]
         L.orc_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i64, C.c_int]
+        L.orc_storage_ms.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i64, C.c_int]
+        L.orc_storage_ms_plan.argtypes = [C.c_void_p, C.c_int64, C.c_int, P_i32]
+        L.orc_storage_ms_plan.restype = C.c_int
         L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
         L.orc_class_order.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32]
         L.orc_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_int]
@@ -96,14 +99,14 @@ class Oracle:
     """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
 
     def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-                 threads=None):
+                 threads=None, storage_ms=0):
         import sys
         sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
         from esmgb.cabi import ModelBuffers, make_opts
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
-        self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span)
+        self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span, storage_ms=storage_ms)
         self.threads = threads or os.cpu_count() or 1
         self.h = lib().orc_create(C.byref(self.buf.struct), C.byref(self.opts))
 
@@ -156,6 +159,19 @@ class Oracle:
         st = np.zeros(NSTAT, np.int64)
         lib().orc_sweeps(self.h, n, sweep0, _p(st, P_i64), self.threads)
         return st
+
+    def storage_ms(self, sweep, force=True, max_passes=0):
+        """The storage multiscale sweep of `sweep` (src/flowmoves.jl:255, plateau moves; max_passes
+        > 0: its first class passes only); returns (moves tried, moves taken, guard events)."""
+        st = np.zeros(3, np.int64)
+        lib().orc_storage_ms(self.h, sweep, int(force), int(max_passes), _p(st, P_i64), self.threads)
+        return st
+
+    def storage_ms_plan(self, sweep, force=True):
+        """Its class passes: [(length, offset, block parity)]."""
+        out = np.zeros(3 * 14, np.int32)
+        n = lib().orc_storage_ms_plan(self.h, sweep, int(force), _p(out, P_i32))
+        return [tuple(int(x) for x in out[3 * i:3 * i + 3]) for i in range(n)]
 
     def move_list(self, sweep, cls, tile, maxn=4096):
         k, f, a = (np.zeros(maxn, np.int32) for _ in range(3))

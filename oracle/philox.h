@@ -15,6 +15,11 @@
  *              h = 0: (u_cat, u_off), h = 1: (u_jac, -)
  *   TAG_LGV    counter (j >> 1, group, it, 0)          Langevin normals (Box-Muller)
  *   TAG_WTH    counter (j >> 1, t, rep, it)            weather normals / uniforms
+ *   TAG_SMS    counter (j >> 1, 0, 0, sweep)           storage multiscale sweep of a sweep: its coin,
+ *                                                       the order of the lengths, offsets, class order
+ *              counter (j >> 1, 1 + li, 2 + cls, sweep) the 8 move selections of a class of length 2^(li+1)
+ *   TAG_SML    counter (2 (8 li + m) + h, b0, rep, sweep)  per block-replica draws of move m:
+ *              h = 0: (u_cat, u_off), h = 1: (u_jac, -)
  */
 #ifndef ESM_ORACLE_PHILOX_H
 #define ESM_ORACLE_PHILOX_H
@@ -26,6 +31,8 @@
 #define ESM_TAG_LANE 0x4C414E45u
 #define ESM_TAG_LGV 0x4C475600u
 #define ESM_TAG_WTH 0x57544800u
+#define ESM_TAG_SMS 0x534D5300u
+#define ESM_TAG_SML 0x534D4C00u
 
 static inline void orc_philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                               uint32_t out[4]) {
