@@ -98,7 +98,7 @@ struct PLane {
 
     // storage term of unit u at block step q (0..L): the change of its cost; *dj the injection
     // change, *d1 the new d (src/energy.jl:448 soc_cost in difference form)
-    __device__ inline real sterm(int u, int q, real t, real *dj, real *d1) const {
+    __device__ __noinline__ real sterm(int u, int q, real t, real *dj, real *d1) const {
         int j = uj[u];
         int tau = b0 + q;
         real k = M.kc_s[j];
@@ -114,7 +114,7 @@ struct PLane {
     }
 
     // the compensation at the end steps (prorata! with soc_qadj), per (end, unit)
-    __device__ void kinks() const {
+    __device__ __noinline__ void kinks() const {
         for (int s = 0; s < 2; ++s) {
             int tau = tau_end(s), t1 = (tau + 1) % M.T;
             for (int u = 0; u < U; ++u) {
@@ -170,7 +170,7 @@ struct PLane {
     // the box (a state of charge at or beyond a bound moves the term for every t). While t is in the
     // interval, the other interior terms are exactly unchanged. A unit with more than NACT such
     // steps gets an empty interval (evaluated whole).
-    __device__ void intervals() const {
+    __device__ __noinline__ void intervals() const {
         for (int u = 0; u < U; ++u) {
             int j = uj[u];
             real mn = 2, mx = -1;
@@ -222,7 +222,7 @@ struct PLane {
 
     // mv_eval! of the block (src/local.jl:1219): beta * DeltaC(t); the end steps' secondaries into
     // s3/sb (the interior ones are evaluated where they change, in collect)
-    __device__ real eval(real t) const {
+    __device__ __noinline__ real eval(real t) const {
         real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
         real D = 0, A = 0;
         for (int i = 0; i < 2 * U; ++i) {
@@ -278,7 +278,7 @@ struct PLane {
         return M.beta_v * D;
     }
 
-    __device__ void save_prev() const {
+    __device__ __noinline__ void save_prev() const {
         for (int i = 0; i < 6 * U; ++i) S(LL.p3, i) = S(LL.s3, i);
         for (int i = 0; i < 2 * U; ++i) S(LL.pb, i) = S(LL.sb, i);
     }
@@ -302,7 +302,7 @@ struct PLane {
     // sign changes of the secondaries between prev (at lo) and cur (at hi): storage ones into gro
     // (when storage splitting applies), node balances into ro; interior steps of the units whose
     // states leave their interval in [lo, hi]
-    __device__ bool collect(real lo, real hi, real sgn, bool want_stor, bool want_other, int *nro, int *ngro) const {
+    __device__ __noinline__ bool collect(real lo, real hi, real sgn, bool want_stor, bool want_other, int *nro, int *ngro) const {
         real x;
         for (int i = 0; i < 2 * U; ++i) {
             if (want_stor)
@@ -337,7 +337,7 @@ struct PLane {
         return true;
     }
 
-    __device__ void sort_buf(int off, int n, real sgn) const {
+    __device__ __noinline__ void sort_buf(int off, int n, real sgn) const {
         for (int i = 1; i < n; ++i) {
             real x = S(off, i);
             int j = i - 1;
@@ -351,7 +351,7 @@ struct PLane {
 
     // next primary breakpoint beyond tp (finalize! of every step, scanned): the kink points, the
     // clamps of the kinked dispatch, the clamps of the moved states of charge
-    __device__ bool next_bp(real tp, real sgn, real *out) const {
+    __device__ __noinline__ bool next_bp(real tp, real sgn, real *out) const {
         bool have = false;
         real best = 0;
         auto consider = [&](real x) {
@@ -417,7 +417,7 @@ struct PLane {
         ++*np;
     }
 
-    __device__ bool piece_roots(int pofs, int cofs, int *np, real a, real b, real sgn, real *cmin) const {
+    __device__ __noinline__ bool piece_roots(int pofs, int cofs, int *np, real a, real b, real sgn, real *cmin) const {
         int nro = 0, ngro = 0;
         if (!collect(a, b, sgn, false, true, &nro, &ngro)) return false;
         if (nro == 0) return true;
@@ -433,7 +433,7 @@ struct PLane {
     }
 
     // walk! (src/local.jl:1294) with storage splitting; 1 proper, 0 improper, -1 buffer overflow
-    __device__ int walk(int pofs, int cofs, int *np, real sgn) const {
+    __device__ __noinline__ int walk(int pofs, int cofs, int *np, real sgn) const {
         real tp = 0, cmin = 0, delta = 0;
         int nx = 0;
         *np = 0;
@@ -518,7 +518,7 @@ struct PLane {
     }
 
     // sample_line! (src/local.jl:1501), as Lane::sample_line
-    __device__ real sample_line(real ucat, real uoff, bool *guard) const {
+    __device__ __noinline__ real sample_line(real ucat, real uoff, bool *guard) const {
         *guard = false;
         int nr = 0, nl = 0;
         int w = walk(LL.pr, LL.cr, &nr, real(1));
@@ -586,7 +586,7 @@ struct PLane {
     }
 
     // commit_block! (src/local.jl:2495): states of charge, kinked dispatch, node balances
-    __device__ void commit(real t) const {
+    __device__ __noinline__ void commit(real t) const {
         eval(t);
         for (int u = 0; u < U; ++u) {
             int n = node(u);
@@ -616,7 +616,7 @@ struct PLane {
 // One class pass of the storage multiscale sweep: threads take (block, replica) tasks (replica
 // fastest) and run the class's moves in order.
 template <class real>
-__global__ void __launch_bounds__(128) k_plateau(const __grid_constant__ DevModel<real> M,
+__global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevModel<real> M,
                                                  const __grid_constant__ PlatMoves mv, uint32_t sweep,
                                                  real *scratch, unsigned long long *stats) {
     PlatLayout LL = plat_layout(M.maxpts, ESM_PLAT_MAXU);
