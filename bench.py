@@ -259,6 +259,26 @@ def profile_case(args):
                       "moves_tried": int(st[:20:2].sum()), "guards": int(st[-1])}), flush=True)
 
 
+def storage_case(args):
+    """One forced storage multiscale sweep after one operation sweep (40 nodes, 64 replicas, T from
+    --T, default 8760), for timing and profiler captures of k_plateau."""
+    from esmgb import build as B
+    B.build()
+    from esmgb.device import DeviceChain
+    from esmgb.model import initial_state, make_model
+    T = args.T or WORKLOAD["T"]
+    m = make_model(WORKLOAD["N"], WORKLOAD["L"], T, seed=WORKLOAD["seed"])
+    d = DeviceChain(m, WORKLOAD["R"], precision=32, seed=WORKLOAD["seed"])
+    d.upload(initial_state(m, WORKLOAD["R"], seed=7))
+    d.sweeps(1, 0, stats=False)
+    d.sync(600.0)
+    d.set_timing(True)
+    st = d.storage_ms(1, force=True)
+    d.sync(600.0)
+    print(json.dumps({"case": "storage", "T": T, "R": WORKLOAD["R"], "moves": [int(x) for x in st],
+                      "storage_ms": d.timing()["storage"][0]}), flush=True)
+
+
 def batch_case(args):
     """Many independent models of uneven size on one GPU: N ~ U{10..128}, L = 1.5 N,
     T in {1460, 2920, 8760}, 16 replicas each (seed-fixed). Every model is a context with its own
@@ -321,13 +341,15 @@ def main():
                     help="operation sweeps include the storage multiscale sweep (probability 1/2)")
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
-    ap.add_argument("--case", default="full", choices=["full", "small", "batch"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
     if args.case == "small":
         return profile_case(args)
     if args.case == "batch":
         return batch_case(args)
+    if args.case == "storage":
+        return storage_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
