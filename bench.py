@@ -4,9 +4,10 @@
 A step is one replica step of one chain (replica_step!, src/replicas.jl:676): the scheduled weather
 bursts with their compensated re-initialisation, one operation sweep of every replica (operation_sweep!,
 src/local.jl:2401: the local sweep with the plain families; with --storage-ms also the storage
-multiscale sweep with probability 1/2, as operation_sweep! runs it), the capacity scores, the
-replica-averaged Langevin step of the shared capacities and the dispatch following. The storage
-multiscale sweep is also timed on its own (one forced sweep) and reported as `storage_ms`. Workload: 40 nodes, 60 lines, hourly T = 8760, 64 weather replicas
+multiscale sweep with probability 1/2 and the long-range storage sweep, as operation_sweep! runs
+them), the capacity scores, the replica-averaged Langevin step of the shared capacities and the
+dispatch following. The two storage sweeps are also timed on their own and reported as
+`storage_ms` and `storage_long`. Workload: 40 nodes, 60 lines, hourly T = 8760, 64 weather replicas
 (the "plain method on GPU" configuration), synthetic seeded data.
 
   value  device throughput: sweeps of all replicas per second from CUDA-event spans on the
@@ -195,7 +196,7 @@ def cpu_sample(threads, sweeps=1, R=2, storage_ms=0):
     w = WORKLOAD
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
     st = initial_state(m, R, seed=7)
-    o = Oracle(m, R, seed=w["seed"], threads=threads, storage_ms=storage_ms)
+    o = Oracle(m, R, seed=w["seed"], threads=threads, storage_ms=storage_ms, storage_long=storage_ms)
     o.set_state(st)
     t0 = time.perf_counter()
     o.sweeps(sweeps, 1)
@@ -275,8 +276,12 @@ def storage_case(args):
     d.set_timing(True)
     st = d.storage_ms(1, force=True)
     d.sync(600.0)
-    print(json.dumps({"case": "storage", "T": T, "R": WORKLOAD["R"], "moves": [int(x) for x in st],
-                      "storage_ms": d.timing()["storage"][0]}), flush=True)
+    ms_ms = d.timing()["storage"][0]
+    sl = d.storage_long(1)
+    d.sync(600.0)
+    print(json.dumps({"case": "storage", "T": T, "R": WORKLOAD["R"], "multiscale": {"moves": [int(x) for x in st],
+                      "ms": ms_ms}, "long_range": {"moves": [int(x) for x in sl], "ms": d.timing()["storage"][0]}}),
+          flush=True)
 
 
 def batch_case(args):
@@ -338,7 +343,7 @@ def main():
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
     ap.add_argument("--storage-ms", action="store_true",
-                    help="operation sweeps include the storage multiscale sweep (probability 1/2)")
+                    help="operation sweeps include the storage sweeps: multiscale (probability 1/2) and long-range")
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
     ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage"],
@@ -364,6 +369,11 @@ def main():
     B.build()
     from esmgb import replicas as RP
     m, st, d = setup_chain(32, storage_ms=int(args.storage_ms))
+    if args.storage_ms:
+        d.close()
+        from esmgb.device import DeviceChain
+        d = DeviceChain(m, WORKLOAD["R"], precision=32, seed=WORKLOAD["seed"], storage_ms=1, storage_long=1)
+        d.upload(st)
     R = d.R
     # the line-move grid picked by the library's autotuner (one timed colour class per candidate,
     # state restored), untimed setup; --grid WPBxWPS fixes it instead (profiler runs)
@@ -416,6 +426,9 @@ def main():
     sms = d.storage_ms(it0 + args.warmup + 2 * args.steps, force=True)
     d.sync(600.0)
     sms_ms = d.timing()["storage"][0]
+    sl = d.storage_long(it0 + args.warmup + 2 * args.steps)
+    d.sync(600.0)
+    sl_ms = d.timing()["storage"][0]
     if rank != 0:
         return
     # roofline of the dominant kernels (one colour class: k_prep_moves and one k_move launch per
@@ -452,6 +465,9 @@ def main():
             "storage_ms": {"ms_per_sweep": sms_ms, "moves": int(sms[0]), "moves_taken": int(sms[1]),
                            "note": "storage multiscale sweep (plateau moves) timed alone; it runs in half of "
                                    "the operation sweeps with --storage-ms"},
+            "storage_long": {"ms_per_sweep": sl_ms, "moves": int(sl[0]), "moves_taken": int(sl[1]),
+                             "note": "long-range storage sweep timed alone; every operation sweep with "
+                                     "--storage-ms"},
             "wall_device_loop_s": wall_dev}
     if not args.no_cpu_baseline:
         try:

@@ -82,8 +82,12 @@ struct esm_ctx {
     unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
     uint32_t *d_sweep = nullptr;         // the sweep index of the current class pass
     // storage multiscale sweep
-    int storage_ms = 0;
+    int storage_ms = 0, storage_long = 0;
     std::vector<int> sgp, sgu;           // storage groups (host copies)
+    std::vector<int> stor;               // flat unit of every storage unit (host copies of the model)
+    std::vector<double> ulo, uhi, uhours;
+    double kappa_min = 1.0;
+    int *d_sl_plan = nullptr;            // the long-range sweep's per-unit move lists
     int sms_threads = 0;
     void *d_sms_scratch = nullptr;
     unsigned long long *d_sms_stats = nullptr;
@@ -681,6 +685,13 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     }
     // storage multiscale sweep: the groups and the limits of its kernel
     c->storage_ms = o->storage_ms != 0;
+    c->storage_long = o->storage_long != 0;
+    c->stor.assign(m->stor, m->stor + m->S);
+    c->ulo.assign(m->unit_lo, m->unit_lo + m->K);
+    c->uhi.assign(m->unit_hi, m->unit_hi + m->K);
+    c->uhours.assign(m->unit_hours, m->unit_hours + m->K);
+    c->kappa_min = o->kappa_min;
+    if ((rc = dalloc(c, &c->d_sl_plan, (size_t)std::max(m->S, 1) * ESM_SL_STRIDE))) return rc;
     if (m->nsgroups > 0 && m->sgroup_ptr && m->sgroup_units) {
         c->sgp.assign(m->sgroup_ptr, m->sgroup_ptr + m->nsgroups + 1);
         c->sgu.assign(m->sgroup_units, m->sgroup_units + c->sgp[m->nsgroups]);
@@ -942,7 +953,72 @@ int sms_sweep_any(esm_ctx *c, uint32_t sweep, bool force, int max_passes = 0) {
     }
     return ESM_OK;
 }
+// The long-range storage sweep's plan (storage_long_sweep!, src/storage_long.jl:245): the storage
+// units with at least 24 h of storage and kappa_s >= kappa_min, each with the level move (p_level
+// = 1) and 4 long-range plateaus of length uniform on 1 .. T-1, in random order, each with a start
+// uniform on the year. The oracle draws the same streams.
+int sl_plan(esm_ctx *c, uint32_t sweep, std::vector<int> &plan) {
+    plan.clear();
+    std::vector<double> k(c->K);
+    CK(cudaMemcpyAsync(k.data(), c->d_k, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
+    int rc = esm_sync(c, 600.0);
+    if (rc) return rc;
+    int T = c->T;
+    for (int j = 0; j < c->S; ++j) {
+        int u = c->stor[j];
+        double kc = std::min(std::max(k[u], c->ulo[u]), c->uhi[u]);
+        if (!(c->uhours[u] >= 24.0 && kc * c->uhours[u] / c->dt >= c->kappa_min)) continue;
+        HStream st{c->seed, ESM_TAG_SLG, (uint32_t)j, 0u, sweep};
+        int L[5], a[5], n = 0;
+        if (st.next() < 1.0) L[n++] = T;
+        for (int q = 0; q < 4; ++q) L[n++] = 1 + st.pick(T - 1);
+        for (int i = n - 1; i >= 1; --i) std::swap(L[i], L[st.pick(i + 1)]);
+        for (int i = 0; i < n; ++i) a[i] = st.pick(T);
+        plan.push_back(j);
+        plan.push_back(n);
+        for (int i = 0; i < 5; ++i) {
+            plan.push_back(i < n ? L[i] : 0);
+            plan.push_back(i < n ? a[i] : 0);
+        }
+    }
+    return ESM_OK;
+}
+
+int sl_sweep_any(esm_ctx *c, uint32_t sweep) {
+    std::vector<int> plan;
+    int rc = sl_plan(c, sweep, plan);
+    if (rc) return rc;
+    int nu = (int)plan.size() / ESM_SL_STRIDE;
+    if (nu == 0) return ESM_OK;
+    if ((rc = rebuild_any(c))) return rc;  // LocalCost at the start (src/storage_long.jl:250)
+    CK(cudaMemcpyAsync(c->d_sl_plan, plan.data(), sizeof(int) * plan.size(), cudaMemcpyHostToDevice, c->stream));
+    Span sp(c, ESM_KT_STORAGE);
+    if (c->precision == 64)
+        CK(esm::launch_storage_long<double>(c->Md, c->d_sl_plan, nu, sweep, (double *)c->d_sms_scratch, c->sms_threads,
+                                            c->d_sms_stats, c->stream));
+    else
+        CK(esm::launch_storage_long<float>(c->Mf, c->d_sl_plan, nu, sweep, (float *)c->d_sms_scratch, c->sms_threads,
+                                           c->d_sms_stats, c->stream));
+    c->launches += 1;
+    return esm_sync(c, 600.0);  // (the host plan buffer is reused by the next call)
+}
 }  // namespace
+
+int esm_storage_long(esm_ctx *c, int64_t sweep, int64_t *stats) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    CK(cudaMemsetAsync(c->d_sms_stats, 0, sizeof(unsigned long long) * 3, c->stream));
+    int rc = sl_sweep_any(c, (uint32_t)sweep);
+    if (rc) return rc;
+    c->has_scores = false;
+    if (stats) {
+        unsigned long long h[3];
+        CK(cudaMemcpyAsync(h, c->d_sms_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        if ((rc = esm_sync(c, 600.0))) return rc;
+        for (int i = 0; i < 3; ++i) stats[i] += (int64_t)h[i];
+    }
+    return ESM_OK;
+}
 
 int esm_storage_ms(esm_ctx *c, int64_t sweep, int32_t force, int32_t max_passes, int64_t *stats) {
     if (!c) return ESM_EINVAL;
@@ -973,6 +1049,7 @@ int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) 
         for (int q = 0; q < nc; ++q)
             if ((rc = class_pass_any(c, sw, order[q]))) return rc;
         if (c->storage_ms && (rc = sms_sweep_any(c, sw, false))) return rc;
+        if (c->storage_long && (rc = sl_sweep_any(c, sw))) return rc;
     }
     c->has_scores = false;
     return stats_out(c, stats);

@@ -12,6 +12,8 @@
 #define ESM_TAG_WTH 0x57544800u
 #define ESM_TAG_SMS 0x534D5300u
 #define ESM_TAG_SML 0x534D4C00u
+#define ESM_TAG_SLG 0x534C4700u
+#define ESM_TAG_SLL 0x534C4C00u
 
 namespace esm {
 

@@ -9,6 +9,8 @@ template int plateau_threads<float>(const DevModel<float> &);
 template size_t plateau_scratch_reals<float>(const DevModel<float> &);
 template cudaError_t launch_plateau<float>(const DevModel<float> &, const PlatMoves &, uint32_t, float *, int,
                                         unsigned long long *, cudaStream_t);
+template cudaError_t launch_storage_long<float>(const DevModel<float> &, const int *, int, uint32_t, float *, int,
+                                             unsigned long long *, cudaStream_t);
 template size_t linemove_scratch_reals<float>(const DevModel<float> &);
 template size_t linemove_smem_per_warp<float>(const DevModel<float> &);
 template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int *, int, const uint32_t *, int, int, float *, int, int,

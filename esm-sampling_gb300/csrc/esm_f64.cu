@@ -9,6 +9,8 @@ template int plateau_threads<double>(const DevModel<double> &);
 template size_t plateau_scratch_reals<double>(const DevModel<double> &);
 template cudaError_t launch_plateau<double>(const DevModel<double> &, const PlatMoves &, uint32_t, double *, int,
                                         unsigned long long *, cudaStream_t);
+template cudaError_t launch_storage_long<double>(const DevModel<double> &, const int *, int, uint32_t, double *, int,
+                                             unsigned long long *, cudaStream_t);
 template size_t linemove_scratch_reals<double>(const DevModel<double> &);
 template size_t linemove_smem_per_warp<double>(const DevModel<double> &);
 template cudaError_t launch_class_pass<double>(const DevModel<double> &, const int *, int, const uint32_t *, int, int, double *, int, int,

@@ -36,4 +36,9 @@ size_t plateau_scratch_reals(const DevModel<real> &M);  // global scratch per th
 template <class real>
 cudaError_t launch_plateau(const DevModel<real> &M, const PlatMoves &mv, uint32_t sweep, real *scratch, int threads,
                            unsigned long long *stats, cudaStream_t s);
+// ---- long-range storage sweep: per unit [stor index, moves, (L, a) per move], at most 5 moves
+#define ESM_SL_STRIDE 12
+template <class real>
+cudaError_t launch_storage_long(const DevModel<real> &M, const int *plan, int nunits, uint32_t sweep, real *scratch,
+                                int threads, unsigned long long *stats, cudaStream_t s);
 }  // namespace esm

@@ -84,6 +84,7 @@ struct PLane {
     real *slab;
     int sstride;
     int L, b0, rep, U;
+    bool lvl = false;  // the level move of the long-range sweep: every instant of the year rises, no end steps
     const int *uj;  // the move's storage units
     mutable real nzs = 0;
 
@@ -93,18 +94,31 @@ struct PLane {
     __device__ inline real &S(int off, int i) const { return slab[(size_t)(off + i) * sstride]; }
     __device__ inline size_t ix(int x, int t) const { return sidx(x, t, rep, M.T, M.R); }
     __device__ inline int node(int u) const { return M.s_bus[uj[u]]; }
-    __device__ inline int tau_end(int s) const { return s == 0 ? b0 : b0 + L; }
+    // block positions: step b0 + q, cyclic (the long-range plateaus wrap); the interior terms (both
+    // states raised) are q0() .. q0() + nq() - 1, the raised states q0() .. q0() + ns() - 1
+    __device__ inline int cyc(int x) const { return x >= M.T ? x - M.T : x; }
+    __device__ inline int stp(int q) const { return cyc(b0 + q); }
+    __device__ inline int q0() const { return lvl ? 0 : 1; }
+    __device__ inline int nq() const { return lvl ? M.T : L - 1; }
+    __device__ inline int ns() const { return lvl ? M.T : L; }
+    __device__ inline int tau_end(int s) const { return s == 0 ? stp(0) : stp(L); }
+    // an interior term whose two states stay strictly inside (0, 1) at t is exactly unchanged
+    __device__ inline bool quiet(int u, int q, real t) const {
+        int tau = stp(q);
+        real y0 = M.e[ix(uj[u], tau)], y1 = M.e[ix(uj[u], cyc(tau + 1))];
+        return y0 > 0 && y0 < 1 && y1 > 0 && y1 < 1 && y0 + t > 0 && y0 + t < 1 && y1 + t > 0 && y1 + t < 1;
+    }
     __device__ inline bool inside(int u, real t) const { return t > S(LL.slo, u) && t < S(LL.shi, u); }
 
     // storage term of unit u at block step q (0..L): the change of its cost; *dj the injection
     // change, *d1 the new d (src/energy.jl:448 soc_cost in difference form)
     __device__ __noinline__ real sterm(int u, int q, real t, real *dj, real *d1) const {
         int j = uj[u];
-        int tau = b0 + q;
+        int tau = stp(q);
         real k = M.kc_s[j];
         return soc_diff<real>(M.s_hours[j], M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], k, k + M.kappa0, M.dt,
-                              M.c_viol, M.e[ix(j, tau)], M.e[ix(j, (tau + 1) % M.T)], q >= 1 ? t : real(0),
-                              q + 1 <= L ? t : real(0), dj, d1);
+                              M.c_viol, M.e[ix(j, tau)], M.e[ix(j, cyc(tau + 1))], (lvl || q >= 1) ? t : real(0),
+                              (lvl || q + 1 <= L) ? t : real(0), dj, d1);
     }
     __device__ inline void sec3(int u, real d, real out[3]) const {
         real ein = M.s_etain[uj[u]];
@@ -176,34 +190,33 @@ struct PLane {
             real mn = 2, mx = -1;
             int na = 0;
             bool over = false;
-            bool prev_out = false;
-            for (int q = 1; q <= L; ++q) {
-                real y = M.e[ix(j, b0 + q)];
-                bool out = !(y > 0 && y < 1);
-                if (!out) {
+            auto list = [&](int qt) {  // an interior term involving a state outside the box
+                for (int i = 0; i < na; ++i)
+                    if (S(LL.act, u * ESM_PLAT_NACT + i) == real(qt)) return;
+                if (na < ESM_PLAT_NACT)
+                    S(LL.act, u * ESM_PLAT_NACT + na++) = real(qt);
+                else
+                    over = true;
+            };
+            for (int p = 0; p < ns(); ++p) {
+                int q = q0() + p;
+                real y = M.e[ix(j, stp(q))];
+                if (y > 0 && y < 1) {
                     mn = fmin(mn, y);
                     mx = fmax(mx, y);
+                    continue;
                 }
-                // interior term q - 1 involves states q - 1 and q; term q involves q and q + 1
-                if (out || prev_out) {
-                    int qt = q - 1;  // the term of step q - 1 (interior when >= 1)
-                    if (qt >= 1) {
-                        if (na < ESM_PLAT_NACT && (na == 0 || S(LL.act, u * ESM_PLAT_NACT + na - 1) != real(qt)))
-                            S(LL.act, u * ESM_PLAT_NACT + na++) = real(qt);
-                        else if (na >= ESM_PLAT_NACT && S(LL.act, u * ESM_PLAT_NACT + na - 1) != real(qt))
-                            over = true;
-                    }
+                // state q is the end value of term q - 1 and the start value of term q
+                if (lvl) {
+                    list(q == 0 ? M.T - 1 : q - 1);
+                    list(q);
+                } else {
+                    if (q - 1 >= 1) list(q - 1);
+                    if (q <= L - 1) list(q);
                 }
-                if (out && q <= L - 1) {  // the term of step q (interior when q <= L - 1)
-                    if (na < ESM_PLAT_NACT && (na == 0 || S(LL.act, u * ESM_PLAT_NACT + na - 1) != real(q)))
-                        S(LL.act, u * ESM_PLAT_NACT + na++) = real(q);
-                    else if (na >= ESM_PLAT_NACT && S(LL.act, u * ESM_PLAT_NACT + na - 1) != real(q))
-                        over = true;
-                }
-                prev_out = out;
             }
             bool ok = !over && mn <= mx;
-            if (!over && mn > mx) {  // every moved state outside the box: no interval, terms listed
+            if (!over && mn > mx) {  // every raised state outside the box: no interval, terms listed
                 S(LL.slo, u) = real(-INFINITY);
                 S(LL.shi, u) = real(INFINITY);
             } else {
@@ -215,9 +228,9 @@ struct PLane {
     }
 
     // the interior step terms of unit u to evaluate at t: every one outside its interval, else the listed
-    __device__ inline int nterms(int u, real t) const { return inside(u, t) ? (int)S(LL.na, u) : L - 1; }
+    __device__ inline int nterms(int u, real t) const { return inside(u, t) ? (int)S(LL.na, u) : nq(); }
     __device__ inline int term_q(int u, real t, int i) const {
-        return inside(u, t) ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : i + 1;
+        return inside(u, t) ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : q0() + i;
     }
 
     // mv_eval! of the block (src/local.jl:1219): beta * DeltaC(t); the end steps' secondaries into
@@ -232,7 +245,7 @@ struct PLane {
         }
         for (int u = 0; u < U; ++u) {
             int n = node(u);
-            for (int s = 0; s < 2; ++s) {  // end steps: storage term, kinked dispatch, node balance
+            for (int s = 0; s < (lvl ? 0 : 2); ++s) {  // end steps: storage term, kinked dispatch, node balance
                 int i = s * U + u, q = s == 0 ? 0 : L, tau = tau_end(s);
                 real dj, d1;
                 real cs = sterm(u, q, t, &dj, &d1);
@@ -265,11 +278,13 @@ struct PLane {
                 S(LL.sb, i) = r0 + dr;
             }
             int nt = nterms(u, t);
+            bool in = inside(u, t);
             for (int i = 0; i < nt; ++i) {  // interior steps: storage term and node balance
                 int q = term_q(u, t, i);
+                if (!in && quiet(u, q, t)) continue;
                 real dj, d1;
                 real cs = sterm(u, q, t, &dj, &d1);
-                real cb = dt * phibal_diff<real>(M.r[ix(n, b0 + q)], dj, M.c_shed, M.c_dump);
+                real cb = dt * phibal_diff<real>(M.r[ix(n, stp(q))], dj, M.c_shed, M.c_dump);
                 D += cs + cb;
                 A += fabs(cs) + fabs(cb);
             }
@@ -315,9 +330,10 @@ struct PLane {
         for (int u = 0; u < U; ++u) {
             bool in = inside(u, lo) && inside(u, hi);
             int n = node(u);
-            int nt = in ? (int)S(LL.na, u) : L - 1;
+            int nt = in ? (int)S(LL.na, u) : nq();
             for (int i = 0; i < nt; ++i) {
-                int q = in ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : i + 1;
+                int q = in ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : q0() + i;
+                if (!in && quiet(u, q, lo) && quiet(u, q, hi)) continue;
                 real dja, d1a, djb, d1b;
                 sterm(u, q, lo, &dja, &d1a);
                 sterm(u, q, hi, &djb, &d1b);
@@ -329,7 +345,7 @@ struct PLane {
                         if (root_of(a3[h], b3[h], lo, hi, sgn, &x) && !add_root(LL.gro, ngro, x)) return false;
                 }
                 if (want_other) {
-                    real r0 = M.r[ix(n, b0 + q)];
+                    real r0 = M.r[ix(n, stp(q))];
                     if (root_of(r0 + dja, r0 + djb, lo, hi, sgn, &x) && !add_root(LL.ro, nro, x)) return false;
                 }
             }
@@ -363,7 +379,7 @@ struct PLane {
                 have = true;
             }
         };
-        for (int i = 0; i < 2 * U; ++i) {
+        for (int i = 0; i < (lvl ? 0 : 2 * U); ++i) {
             if (S(LL.kv, i) == 0) continue;
             real g = S(LL.kg, i), Q = S(LL.kq, i);
             consider(-Q / g);
@@ -392,7 +408,7 @@ struct PLane {
                 for (int i = 0; i < na; ++i) {
                     int q = (int)S(LL.act, u * ESM_PLAT_NACT + i);
                     for (int h = 0; h < 2; ++h) {
-                        real y0 = M.e[ix(j, b0 + q + h)];
+                        real y0 = M.e[ix(j, cyc(stp(q) + h))];
                         if (y0 > 0 && y0 < 1) continue;
                         consider(real(0) - y0);
                         consider(real(1) - y0);
@@ -400,8 +416,8 @@ struct PLane {
                 }
                 continue;
             }
-            for (int q = 1; q <= L; ++q) {
-                real y0 = M.e[ix(j, b0 + q)];
+            for (int p = 0; p < ns(); ++p) {
+                real y0 = M.e[ix(j, stp(q0() + p))];
                 consider(real(0) - y0);
                 consider(real(1) - y0);
             }
@@ -576,7 +592,7 @@ struct PLane {
     __device__ real logjac(real t, bool *any) const {
         real lj = 0;
         *any = false;
-        for (int i = 0; i < 2 * U; ++i) {
+        for (int i = 0; i < (lvl ? 0 : 2 * U); ++i) {
             if (S(LL.kv, i) == 0) continue;
             *any = true;
             real Q = S(LL.kq, i);
@@ -590,7 +606,7 @@ struct PLane {
         eval(t);
         for (int u = 0; u < U; ++u) {
             int n = node(u);
-            for (int s = 0; s < 2; ++s) {  // end steps: the compensation and the node balance
+            for (int s = 0; s < (lvl ? 0 : 2); ++s) {  // end steps: the compensation and the node balance
                 int i = s * U + u, tau = tau_end(s);
                 real ph = S(LL.kph, i);
                 int c = 0;
@@ -601,15 +617,17 @@ struct PLane {
                 M.r[ix(n, tau)] += S(LL.dr, i);
             }
             int nt = nterms(u, t);  // interior steps whose injection changes
+            bool in = inside(u, t);
             for (int i = 0; i < nt; ++i) {
                 int q = term_q(u, t, i);
+                if (!in && quiet(u, q, t)) continue;
                 real dj, d1;
                 sterm(u, q, t, &dj, &d1);
-                M.r[ix(n, b0 + q)] += dj;
+                M.r[ix(n, stp(q))] += dj;
             }
         }
         for (int u = 0; u < U; ++u)
-            for (int q = 1; q <= L; ++q) M.e[ix(uj[u], b0 + q)] += t;
+            for (int p = 0; p < ns(); ++p) M.e[ix(uj[u], stp(q0() + p))] += t;
     }
 };
 
@@ -661,6 +679,69 @@ __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevM
     if (tried) atomicAdd(&stats[0], tried);
     if (moved) atomicAdd(&stats[1], moved);
     if (guards) atomicAdd(&stats[2], guards);
+}
+
+// The long-range storage sweep (storage_long_sweep!, src/storage_long.jl:245): threads take (unit,
+// replica) tasks and run the unit's moves in order -- the level move (every instant of the year
+// rises) and the long-range plateaus (prep_slong!, :77: one unit, the cyclic instants a+1 .. a+L,
+// compensation at steps a and a+L). plan: per unit [stor index, moves, (L, a) per move]; L = T is the
+// level move. The moves of different units touch different nodes (one unit per node and carrier).
+template <class real>
+__global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__ DevModel<real> M, const int *plan,
+                                                        int nunits, uint32_t sweep, real *scratch,
+                                                        unsigned long long *stats) {
+    PlatLayout LL = plat_layout(M.maxpts, ESM_PLAT_MAXU);
+    real local[ESM_PLAT_LOCAL];
+    size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t nthr = (size_t)gridDim.x * blockDim.x;
+    bool loc = LL.total <= ESM_PLAT_LOCAL;
+    real *slab = loc ? local : scratch + gid;
+    PLane<real> Ln(M, LL, slab, loc ? 1 : (int)nthr);
+    unsigned long long tried = 0, moved = 0, guards = 0;
+    size_t ntask = (size_t)nunits * M.R;
+    for (size_t task = gid; task < ntask; task += nthr) {
+        const int *pu = plan + (task / M.R) * ESM_SL_STRIDE;
+        Ln.rep = (int)(task % M.R);
+        Ln.U = 1;
+        Ln.uj = pu;
+        for (int m = 0; m < pu[1]; ++m) {
+            int L = pu[2 + 2 * m], a = pu[3 + 2 * m];
+            Ln.lvl = L >= M.T;
+            Ln.L = Ln.lvl ? M.T : L;
+            Ln.b0 = Ln.lvl ? 0 : a;
+            Ln.intervals();
+            if (!Ln.lvl) Ln.kinks();
+            double uc, uo, uj, un;
+            uniform2(M.seed, ESM_TAG_SLL, 2u * (uint32_t)m, (uint32_t)pu[0], (uint32_t)Ln.rep, sweep, &uc, &uo);
+            bool guard;
+            real t = Ln.sample_line((real)uc, (real)uo, &guard);
+            if (guard) ++guards;
+            if (t != 0 && !Ln.lvl) {
+                bool any;
+                real lj = Ln.logjac(t, &any);
+                if (any) {
+                    uniform2(M.seed, ESM_TAG_SLL, 2u * (uint32_t)m + 1, (uint32_t)pu[0], (uint32_t)Ln.rep, sweep, &uj,
+                             &un);
+                    if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+                }
+            }
+            if (t != 0) Ln.commit(t);
+            ++tried;
+            if (t != 0) ++moved;
+        }
+    }
+    if (tried) atomicAdd(&stats[0], tried);
+    if (moved) atomicAdd(&stats[1], moved);
+    if (guards) atomicAdd(&stats[2], guards);
+}
+
+template <class real>
+cudaError_t launch_storage_long(const DevModel<real> &M, const int *plan, int nunits, uint32_t sweep, real *scratch,
+                                int threads, unsigned long long *stats, cudaStream_t s) {
+    size_t ntask = (size_t)nunits * M.R;
+    int blocks = (int)(((size_t)threads < ntask ? (size_t)threads : ntask) + 127) / 128;
+    k_storage_long<real><<<blocks, 128, 0, s>>>(M, plan, nunits, sweep, scratch, stats);
+    return cudaGetLastError();
 }
 
 // threads of k_plateau resident on the device, and the global scratch it needs per thread (0: the

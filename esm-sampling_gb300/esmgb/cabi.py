@@ -47,7 +47,7 @@ class EsmOpts(C.Structure):
     _fields_ = [
         ("R", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64), ("extra", C.c_double),
         ("maxnats", C.c_double), ("kappa_min", C.c_double), ("max_points", C.c_int32), ("span", C.c_int32),
-        ("family_rates", C.c_double * NFAM), ("storage_ms", C.c_int32),
+        ("family_rates", C.c_double * NFAM), ("storage_ms", C.c_int32), ("storage_long", C.c_int32),
     ]
 
 
@@ -128,10 +128,10 @@ def storage_groups(m: SynthModel):
 
 
 def make_opts(R, precision=32, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-              rates=FAMILY_RATES, storage_ms=0) -> EsmOpts:
+              rates=FAMILY_RATES, storage_ms=0, storage_long=0) -> EsmOpts:
     o = EsmOpts()
     o.R, o.precision, o.seed, o.extra, o.maxnats, o.kappa_min = R, precision, seed, extra, maxnats, kappa_min
-    o.max_points, o.span, o.storage_ms = max_points, span, int(storage_ms)
+    o.max_points, o.span, o.storage_ms, o.storage_long = max_points, span, int(storage_ms), int(storage_long)
     for i, r in enumerate(rates):
         o.family_rates[i] = r
     return o

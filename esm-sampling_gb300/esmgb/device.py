@@ -23,7 +23,7 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
            "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
-           "esm_autotune_moves", "esm_storage_ms")
+           "esm_autotune_moves", "esm_storage_ms", "esm_storage_long")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -74,6 +74,7 @@ def load(build_if_missing=True):
     L.esm_sync.argtypes = [C.c_void_p, C.c_double]
     L.esm_set_move_grid.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     L.esm_storage_ms.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
+    L.esm_storage_long.argtypes = [C.c_void_p, C.c_int64, P_i64]
     L.esm_move_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
     L.esm_autotune_moves.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
     L.esm_launch_count.restype = C.c_int64
@@ -95,13 +96,13 @@ class DeviceChain:
 
     def __init__(self, model: SynthModel, R: int, precision: int = 32, seed: int = 1, extra: float = 4.0,
                  maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 0, span: int = 0,
-                 storage_ms: int = 0):
+                 storage_ms: int = 0, storage_long: int = 0):
         self.L = load()
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
         self.opts: EsmOpts = make_opts(R, precision, seed, extra, maxnats, kappa_min, max_points, span,
-                                       storage_ms=storage_ms)
+                                       storage_ms=storage_ms, storage_long=storage_long)
         h = C.c_void_p()
         rc = self.L.esm_create(C.byref(self.buf.struct), C.byref(self.opts), C.byref(h))
         self.h = h
@@ -173,6 +174,12 @@ class DeviceChain:
         st = np.zeros(3, np.int64)
         self._check(self.L.esm_storage_ms(self.h, sweep, int(force), int(max_passes), _p(st, P_i64)),
                     "esm_storage_ms")
+        return st
+
+    def storage_long(self, sweep):
+        """The long-range storage sweep of `sweep`; returns (tried, taken, guards)."""
+        st = np.zeros(3, np.int64)
+        self._check(self.L.esm_storage_long(self.h, sweep, _p(st, P_i64)), "esm_storage_long")
         return st
 
     def scores(self):

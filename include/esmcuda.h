@@ -130,6 +130,8 @@ typedef struct esm_opts {
     int32_t storage_ms;        /* 1: an operation sweep runs, after the local sweep, the storage multiscale
                                   sweep with probability 1/2 (operation_sweep!, src/local.jl:2417);
                                   0: the local sweep only */
+    int32_t storage_long;      /* 1: then the long-range storage sweep (storage_long_sweep!,
+                                  src/storage_long.jl:245; probability 1, the default of src/run.jl:27) */
 } esm_opts;
 
 /* The automatic point cap: 192, or 4 points per unit of the largest state-of-charge atom when that
@@ -180,6 +182,14 @@ int esm_class_pass(esm_ctx *ctx, int64_t sweep, int32_t cls, int32_t move_limit,
    of the sweep (a diagnostic, as move_limit of esm_class_pass). stats (may be NULL) += (moves
    tried, moves taken, guard events). */
 int esm_storage_ms(esm_ctx *ctx, int64_t sweep, int32_t force, int32_t max_passes, int64_t *stats);
+
+/* The long-range storage sweep of sweep `sweep` (storage_long_sweep!, src/storage_long.jl:245): for
+   every storage unit with at least 24 h of storage and kappa_s >= kappa_min, the level move (every
+   instant of the year rises) and 4 long-range plateaus (prep_slong!, :77: the cyclic instants
+   a+1 .. a+L rise, energy moved from step a to step a+L with pro-rata compensation at both and the
+   Jacobian test), in random order. esm_operation_sweeps calls it after the local (and multiscale)
+   sweep when esm_opts.storage_long is 1. stats (may be NULL) += (moves tried, taken, guard events). */
+int esm_storage_long(esm_ctx *ctx, int64_t sweep, int64_t *stats);
 
 /* Capacity scores per replica: sk [R*K] (s_k = -beta_v dC/dk + dlogJ/dk, node space) and the
    capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with

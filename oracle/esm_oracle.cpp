@@ -66,7 +66,7 @@ struct Opts {
     uint64_t seed;
     double extra, maxnats, kmin;
     double rates[ESM_NFAM];
-    int storage_ms;
+    int storage_ms, storage_long;
 };
 
 struct Ctx {
@@ -433,11 +433,13 @@ struct Mover {
     int rep;
     double beta;
     vector<double> sec;
+    bool cyclic = false;  // the steps cover the whole year: the last step's end value is the first's
     double eval(double t) {  // mv_eval! (src/local.jl:1219): later steps first
         sec.clear();
         double D = 0.0;
         int n = (int)w.size();
-        for (int q = n - 1; q >= 0; --q) D += eval_ws(*c, *w[q], rep, t, q + 1 < n ? w[q + 1] : nullptr, sec);
+        for (int q = n - 1; q >= 0; --q)
+            D += eval_ws(*c, *w[q], rep, t, q + 1 < n ? w[q + 1] : (cyclic ? w[0] : nullptr), sec);
         return D;
     }
     bool hasstor() const {
@@ -1069,9 +1071,9 @@ static bool prep_plateau(const Ctx &c, vector<WS> &wss, int b0, int L, const vec
                          vector<Kink> *jac) {
     const Model &m = c.m;
     int n = L + 1;
-    for (int q = 0; q < n; ++q) {
+    for (int q = 0; q < n; ++q) {  // the steps b0 .. b0 + L, cyclic (the long-range plateaus wrap)
         wss[q].clear();
-        wss[q].tau = b0 + q;
+        wss[q].tau = (b0 + q) % m.T;
     }
     jac->clear();
     for (int j : us)
@@ -1178,6 +1180,103 @@ static void sms_sweep(Ctx &c, uint32_t sweep, bool force, int64_t *stats3, int n
     if (n == 0 || c.m.S == 0) return;
     rebuild(c, nthreads);
     for (int i = 0; i < n; ++i) sms_pass(c, sweep, ps[i], stats3, nthreads);
+}
+
+// ------------------------------------------------------------------------------------------
+// long-range storage sweep (storage_long_sweep!, src/storage_long.jl:245): for every storage unit
+// with at least 24 h of storage and kappa_s >= kappa_min, a level move (every instant of the year
+// rises, no power change inside the box) and 4 long-range plateaus (prep_slong!, :77: the state of
+// charge rises at the cyclic instants a+1 .. a+L, energy moved from step a to step a+L with pro-rata
+// compensation at both), in random order
+// ------------------------------------------------------------------------------------------
+struct SlMove {
+    int L, a;  // length (T: the level move), start step a (0-based)
+};
+
+// the eligible units and their move lists of one sweep (the same streams as the device host side)
+static void sl_plan(const Ctx &c, uint32_t sweep, vector<int> &units, vector<vector<SlMove>> &moves) {
+    const Model &m = c.m;
+    int T = m.T;
+    units.clear();
+    moves.clear();
+    for (int j = 0; j < m.S; ++j) {
+        int u = m.stor[j];
+        if (!(m.uhours[u] >= 24.0 && kcl(c, u) * m.uhours[u] / m.dt >= c.o.kmin)) continue;
+        PStream st{c.o.seed, ESM_TAG_SLG, (uint32_t)j, 0u, sweep};
+        vector<SlMove> mv;
+        if (st.next() < 1.0) mv.push_back(SlMove{T, 0});  // the level move (p_level = 1)
+        for (int q = 0; q < 4; ++q) mv.push_back(SlMove{1 + st.pick(T - 1), 0});
+        for (int i = (int)mv.size() - 1; i >= 1; --i) std::swap(mv[i], mv[st.pick(i + 1)]);
+        for (auto &x : mv) x.a = st.pick(T);
+        units.push_back(j);
+        moves.push_back(mv);
+    }
+}
+
+// the level move (L = T): every instant of unit j rises by t; every step's term sees the next step's
+static bool prep_level(const Ctx &c, vector<WS> &wss, int j, int rep) {
+    const Model &m = c.m;
+    int T = m.T;
+    for (int q = 0; q < T; ++q) {
+        wss[q].clear();
+        wss[q].tau = q;
+        wss[q].add_entry(EK_SE, j, 1.0);
+    }
+    for (int q = 0; q < T; ++q) finalize_ws(c, wss[q], rep);
+    for (int q = 0; q < T; ++q) link_soc(m, wss[q], wss[(q + 1) % T]);
+    return true;
+}
+
+static void sl_sweep(Ctx &c, uint32_t sweep, int64_t *stats3, int nthreads) {
+    const Model &m = c.m;
+    int T = m.T, R = c.o.R;
+    vector<int> units;
+    vector<vector<SlMove>> moves;
+    sl_plan(c, sweep, units, moves);
+    if (units.empty()) return;
+    rebuild(c, nthreads);  // LocalCost at the start (src/storage_long.jl:250)
+    int nu = (int)units.size();
+#pragma omp parallel num_threads(nthreads)
+    {
+        int64_t loc[3] = {0, 0, 0};
+        vector<WS> wss(T);
+        for (auto &w : wss) w.init(m);
+        vector<Kink> jac;
+#pragma omp for schedule(dynamic, 1)
+        for (int q = 0; q < nu * R; ++q) {
+            int ui = q / R, rep = q % R, j = units[ui];
+            for (size_t mi = 0; mi < moves[ui].size(); ++mi) {
+                const SlMove &sm = moves[ui][mi];
+                bool level = sm.L == T;
+                jac.clear();
+                if (level)
+                    prep_level(c, wss, j, rep);
+                else if (!prep_plateau(c, wss, sm.a, sm.L, {j}, rep, &jac))
+                    continue;
+                Mover mv{&c, {}, rep, m.beta_v, {}};
+                mv.cyclic = level;
+                int n = level ? T : sm.L + 1;
+                for (int k = 0; k < n; ++k) mv.w.push_back(&wss[k]);
+                double uc, uo, uj, un;
+                orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi, (uint32_t)j, (uint32_t)rep, sweep, &uc, &uo);
+                orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi + 1, (uint32_t)j, (uint32_t)rep, sweep, &uj, &un);
+                bool guard = false;
+                double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
+                if (guard) loc[2] += 1;
+                if (t != 0.0 && !jac.empty()) {
+                    double lj = 0.0;
+                    for (auto &kk : jac) lj += kk.nm * log(fabs((std::max(kk.Q + kk.g * t, 0.0) + kk.e) / kk.Pm));
+                    if (uj >= exp(std::min(0.0, lj))) t = 0.0;
+                }
+                commit(c, mv, t);
+                loc[0] += 1;
+                loc[1] += t != 0.0;
+            }
+        }
+        for (auto &w : wss) w.clear();
+#pragma omp critical
+        for (int i = 0; i < 3; ++i) stats3[i] += loc[i];
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1733,6 +1832,7 @@ void *orc_create(const esm_model *em, const esm_opts *eo) {
     o.kmin = eo->kappa_min;
     for (int q = 0; q < ESM_NFAM; ++q) o.rates[q] = eo->family_rates[q];
     o.storage_ms = eo->storage_ms;
+    o.storage_long = eo->storage_long;
     size_t TR = (size_t)m.T * o.R;
     c->theta.assign(N * TR, 0.0);
     c->g.assign(m.D * TR, 0.0);
@@ -1802,6 +1902,10 @@ void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
             sms_sweep(*c, sw, false, s3, nthreads);
             for (int i = 0; i < 3; ++i) c->sms_stats[i] += s3[i];
         }
+        if (c->o.storage_long) {
+            int64_t s3[3] = {0, 0, 0};
+            sl_sweep(*c, sw, s3, nthreads);
+        }
     }
 }
 
@@ -1809,6 +1913,29 @@ void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
 // first class passes only); stats3 += (moves tried, moves taken, guard events)
 void orc_storage_ms(void *p, int64_t sweep, int force, int max_passes, int64_t *stats3, int nthreads) {
     sms_sweep(*(Ctx *)p, (uint32_t)sweep, force != 0, stats3, nthreads, max_passes);
+}
+
+// the long-range storage sweep of sweep `sweep`; stats3 += (moves tried, moves taken, guard events)
+void orc_storage_long(void *p, int64_t sweep, int64_t *stats3, int nthreads) {
+    sl_sweep(*(Ctx *)p, (uint32_t)sweep, stats3, nthreads);
+}
+
+// its plan: per eligible unit (stor index) its moves (length, start); returns the number of moves
+int orc_storage_long_plan(void *p, int64_t sweep, int32_t *out, int maxn) {
+    Ctx *c = (Ctx *)p;
+    vector<int> units;
+    vector<vector<SlMove>> moves;
+    sl_plan(*c, (uint32_t)sweep, units, moves);
+    int n = 0;
+    for (size_t u = 0; u < units.size(); ++u)
+        for (auto &x : moves[u])
+            if (n < maxn) {
+                out[3 * n] = units[u];
+                out[3 * n + 1] = x.L;
+                out[3 * n + 2] = x.a;
+                ++n;
+            }
+    return n;
 }
 
 // the class passes of the storage multiscale sweep of a sweep: (length, offset, parity) each

@@ -56,6 +56,9 @@ def lib():
         L.orc_storage_ms.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i64, C.c_int]
         L.orc_storage_ms_plan.argtypes = [C.c_void_p, C.c_int64, C.c_int, P_i32]
         L.orc_storage_ms_plan.restype = C.c_int
+        L.orc_storage_long.argtypes = [C.c_void_p, C.c_int64, P_i64, C.c_int]
+        L.orc_storage_long_plan.argtypes = [C.c_void_p, C.c_int64, P_i32, C.c_int]
+        L.orc_storage_long_plan.restype = C.c_int
         L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
         L.orc_class_order.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32]
         L.orc_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_int]
@@ -99,14 +102,15 @@ class Oracle:
     """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
 
     def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-                 threads=None, storage_ms=0):
+                 threads=None, storage_ms=0, storage_long=0):
         import sys
         sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
         from esmgb.cabi import ModelBuffers, make_opts
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
-        self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span, storage_ms=storage_ms)
+        self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span, storage_ms=storage_ms,
+                              storage_long=storage_long)
         self.threads = threads or os.cpu_count() or 1
         self.h = lib().orc_create(C.byref(self.buf.struct), C.byref(self.opts))
 
@@ -166,6 +170,19 @@ class Oracle:
         st = np.zeros(3, np.int64)
         lib().orc_storage_ms(self.h, sweep, int(force), int(max_passes), _p(st, P_i64), self.threads)
         return st
+
+    def storage_long(self, sweep):
+        """The long-range storage sweep of `sweep` (src/storage_long.jl:245); returns (moves tried,
+        moves taken, guard events)."""
+        st = np.zeros(3, np.int64)
+        lib().orc_storage_long(self.h, sweep, _p(st, P_i64), self.threads)
+        return st
+
+    def storage_long_plan(self, sweep, maxn=4096):
+        """Its moves: [(unit, length, start)] (length T: the level move)."""
+        out = np.zeros(3 * maxn, np.int32)
+        n = lib().orc_storage_long_plan(self.h, sweep, _p(out, P_i32), maxn)
+        return [tuple(int(x) for x in out[3 * i:3 * i + 3]) for i in range(n)]
 
     def storage_ms_plan(self, sweep, force=True):
         """Its class passes: [(length, offset, block parity)]."""

@@ -20,6 +20,8 @@
  *              counter (j >> 1, 1 + li, 2 + cls, sweep) the 8 move selections of a class of length 2^(li+1)
  *   TAG_SML    counter (2 (8 li + m) + h, b0, rep, sweep)  per block-replica draws of move m:
  *              h = 0: (u_cat, u_off), h = 1: (u_jac, -)
+ *   TAG_SLG    counter (j >> 1, unit, 0, sweep)        long-range storage sweep: a unit's move list
+ *   TAG_SLL    counter (2 m + h, unit, rep, sweep)     per unit-replica draws of its move m
  */
 #ifndef ESM_ORACLE_PHILOX_H
 #define ESM_ORACLE_PHILOX_H
@@ -33,6 +35,8 @@
 #define ESM_TAG_WTH 0x57544800u
 #define ESM_TAG_SMS 0x534D5300u
 #define ESM_TAG_SML 0x534D4C00u
+#define ESM_TAG_SLG 0x534C4700u
+#define ESM_TAG_SLL 0x534C4C00u
 
 static inline void orc_philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                               uint32_t out[4]) {
