@@ -41,3 +41,28 @@ def test_moves_keep_the_caches():
     s1 = o.get_state()
     assert np.array_equal(s0["theta"], s1["theta"])
     assert (s1["e"] != s0["e"]).mean() > 0.5  # most states of charge moved
+
+
+def test_long_range_plan_and_caches():
+    """storage_long_sweep! (src/storage_long.jl:245): the units with at least 24 h of storage, each
+    with the level move and 4 cyclic plateaus of length 1 .. T-1; the caches stay consistent."""
+    m, o = _oracle()
+    o.sweeps(1, 0)
+    plan = o.storage_long_plan(3)
+    hours = m.unit_hours[m.stor]
+    units = sorted({p[0] for p in plan})
+    assert units == [j for j in range(m.S) if hours[j] >= 24.0]
+    for j in units:
+        mv = [p for p in plan if p[0] == j]
+        assert len(mv) == 5 and sum(p[1] == m.T for p in mv) == 1
+        assert all(1 <= p[1] <= m.T and 0 <= p[2] < m.T for p in mv)
+    s0 = o.get_state()
+    st = o.storage_long(3)
+    assert st[0] == len(plan) * o.R and st[2] == 0
+    r1, _ = o.caches()
+    o.rebuild()
+    r2, _ = o.caches()
+    assert np.abs(r1 - r2).max() <= 1e-9 * (1 + np.abs(r2).max())
+    s1 = o.get_state()
+    moved = np.abs(s1["e"] - s0["e"]).max(axis=(1, 2)) > 0
+    assert set(np.flatnonzero(moved)) <= set(units)  # only the long-duration units move
