@@ -77,7 +77,11 @@ __host__ __device__ inline PlatLayout plat_layout(int maxpts, int U) {
     return L;
 }
 
-template <class real>
+// COOP: the 32 lanes of a warp run one task together. Every lane runs the walk on its own copy of
+// the scratch (identical contents), and the loops over the block's steps -- the clamp-free interval,
+// the interior terms outside it, the breakpoint scan, the commit -- are split over the lanes and
+// combined by reductions that every lane receives from lane 0, so the control flow stays uniform.
+template <class real, bool COOP = false>
 struct PLane {
     const DevModel<real> &M;
     const PlatLayout &LL;
@@ -87,6 +91,29 @@ struct PLane {
     bool lvl = false;  // the level move of the long-range sweep: every instant of the year rises, no end steps
     const int *uj;  // the move's storage units
     mutable real nzs = 0;
+    int lane = 0;
+    static constexpr int NL = COOP ? 32 : 1;
+    __device__ inline real wsum(real v) const {
+        if constexpr (COOP) {
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            return __shfl_sync(0xffffffffu, v, 0);
+        }
+        return v;
+    }
+    __device__ inline real wmin(real v) const {
+        if constexpr (COOP) {
+            for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+            return __shfl_sync(0xffffffffu, v, 0);
+        }
+        return v;
+    }
+    __device__ inline real wmax(real v) const {
+        if constexpr (COOP) {
+            for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+            return __shfl_sync(0xffffffffu, v, 0);
+        }
+        return v;
+    }
 
     __device__ PLane(const DevModel<real> &M_, const PlatLayout &LL_, real *slab_, int sstride_)
         : M(M_), LL(LL_), slab(slab_), sstride(sstride_) {}
@@ -198,15 +225,7 @@ struct PLane {
                 else
                     over = true;
             };
-            for (int p = 0; p < ns(); ++p) {
-                int q = q0() + p;
-                real y = M.e[ix(j, stp(q))];
-                if (y > 0 && y < 1) {
-                    mn = fmin(mn, y);
-                    mx = fmax(mx, y);
-                    continue;
-                }
-                // state q is the end value of term q - 1 and the start value of term q
+            auto out_state = [&](int q) {  // state q is the end value of term q - 1 and the start of term q
                 if (lvl) {
                     list(q == 0 ? M.T - 1 : q - 1);
                     list(q);
@@ -214,7 +233,32 @@ struct PLane {
                     if (q - 1 >= 1) list(q - 1);
                     if (q <= L - 1) list(q);
                 }
+            };
+            for (int base = 0; base < ns(); base += NL) {
+                int p = base + lane, qo = -1;
+                if (p < ns()) {
+                    int q = q0() + p;
+                    real y = M.e[ix(j, stp(q))];
+                    if (y > 0 && y < 1) {
+                        mn = fmin(mn, y);
+                        mx = fmax(mx, y);
+                    } else {
+                        qo = q;
+                    }
+                }
+                if constexpr (COOP) {  // the states outside the box, in step order, listed on every lane
+                    unsigned bal = __ballot_sync(0xffffffffu, qo >= 0);
+                    while (bal) {
+                        int l = __ffs(bal) - 1;
+                        bal &= bal - 1;
+                        out_state(__shfl_sync(0xffffffffu, qo, l));
+                    }
+                } else if (qo >= 0) {
+                    out_state(qo);
+                }
             }
+            mn = wmin(mn);
+            mx = wmax(mx);
             bool ok = !over && mn <= mx;
             if (!over && mn > mx) {  // every raised state outside the box: no interval, terms listed
                 S(LL.slo, u) = real(-INFINITY);
@@ -279,15 +323,24 @@ struct PLane {
             }
             int nt = nterms(u, t);
             bool in = inside(u, t);
-            for (int i = 0; i < nt; ++i) {  // interior steps: storage term and node balance
+            real Di = 0, Ai = 0;
+            // interior steps: storage term and node balance (the listed ones on every lane; outside
+            // the interval every term, split over the lanes)
+            for (int i = in ? 0 : lane; i < nt; i += in ? 1 : NL) {
                 int q = term_q(u, t, i);
                 if (!in && quiet(u, q, t)) continue;
                 real dj, d1;
                 real cs = sterm(u, q, t, &dj, &d1);
                 real cb = dt * phibal_diff<real>(M.r[ix(n, stp(q))], dj, M.c_shed, M.c_dump);
-                D += cs + cb;
-                A += fabs(cs) + fabs(cb);
+                Di += cs + cb;
+                Ai += fabs(cs) + fabs(cb);
             }
+            if (!in) {
+                Di = wsum(Di);
+                Ai = wsum(Ai);
+            }
+            D += Di;
+            A += Ai;
         }
         if constexpr (sizeof(real) == 4) nzs = M.beta_v * A * real(4.8e-7);
         return M.beta_v * D;
@@ -331,23 +384,56 @@ struct PLane {
             bool in = inside(u, lo) && inside(u, hi);
             int n = node(u);
             int nt = in ? (int)S(LL.na, u) : nq();
-            for (int i = 0; i < nt; ++i) {
-                int q = in ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : q0() + i;
-                if (!in && quiet(u, q, lo) && quiet(u, q, hi)) continue;
-                real dja, d1a, djb, d1b;
-                sterm(u, q, lo, &dja, &d1a);
-                sterm(u, q, hi, &djb, &d1b);
-                if (want_stor) {
-                    real a3[3], b3[3];
-                    sec3(u, d1a, a3);
-                    sec3(u, d1b, b3);
-                    for (int h = 0; h < 3; ++h)
-                        if (root_of(a3[h], b3[h], lo, hi, sgn, &x) && !add_root(LL.gro, ngro, x)) return false;
+            // the listed terms on every lane; outside the interval every term, split over the lanes in
+            // rounds of NL terms, whose roots every lane adds in term order
+            int step = in ? 1 : NL;
+            for (int base = 0; base < nt; base += step) {
+                int i = in ? base : base + lane;
+                real rg[3] = {0, 0, 0}, rr = 0;
+                int ng = 0;
+                bool hr = false;
+                if (i < nt) {
+                    int q = in ? (int)S(LL.act, u * ESM_PLAT_NACT + i) : q0() + i;
+                    if (in || !(quiet(u, q, lo) && quiet(u, q, hi))) {
+                        real dja, d1a, djb, d1b;
+                        sterm(u, q, lo, &dja, &d1a);
+                        sterm(u, q, hi, &djb, &d1b);
+                        if (want_stor) {
+                            real a3[3], b3[3];
+                            sec3(u, d1a, a3);
+                            sec3(u, d1b, b3);
+                            for (int h = 0; h < 3; ++h)
+                                if (root_of(a3[h], b3[h], lo, hi, sgn, &x)) rg[ng++] = x;
+                        }
+                        if (want_other) {
+                            real r0 = M.r[ix(n, stp(q))];
+                            if (root_of(r0 + dja, r0 + djb, lo, hi, sgn, &x)) {
+                                rr = x;
+                                hr = true;
+                            }
+                        }
+                    }
                 }
-                if (want_other) {
-                    real r0 = M.r[ix(n, stp(q))];
-                    if (root_of(r0 + dja, r0 + djb, lo, hi, sgn, &x) && !add_root(LL.ro, nro, x)) return false;
+                bool ok = true;
+                if (COOP && !in) {
+                    unsigned bal = __ballot_sync(0xffffffffu, ng > 0 || hr);
+                    while (bal) {
+                        int l = __ffs(bal) - 1;
+                        bal &= bal - 1;
+                        int nl = __shfl_sync(0xffffffffu, ng, l);
+                        for (int h = 0; h < 3; ++h) {
+                            real xs = __shfl_sync(0xffffffffu, rg[h], l);
+                            if (h < nl) ok = add_root(LL.gro, ngro, xs) && ok;
+                        }
+                        bool hl = __shfl_sync(0xffffffffu, hr, l);
+                        real xr = __shfl_sync(0xffffffffu, rr, l);
+                        if (hl) ok = add_root(LL.ro, nro, xr) && ok;
+                    }
+                } else {
+                    for (int h = 0; h < ng; ++h) ok = add_root(LL.gro, ngro, rg[h]) && ok;
+                    if (hr) ok = add_root(LL.ro, nro, rr) && ok;
                 }
+                if (!ok) return false;
             }
         }
         return true;
@@ -416,11 +502,16 @@ struct PLane {
                 }
                 continue;
             }
-            for (int p = 0; p < ns(); ++p) {
+            for (int p = lane; p < ns(); p += NL) {
                 real y0 = M.e[ix(j, stp(q0() + p))];
                 consider(real(0) - y0);
                 consider(real(1) - y0);
             }
+        }
+        if constexpr (COOP) {  // the nearest candidate over the lanes (a sign flip is exact)
+            real key = wmin(have ? sgn * best : real(INFINITY));
+            have = key < real(INFINITY);
+            best = have ? sgn * key : real(0);
         }
         *out = best;
         return have;
@@ -601,12 +692,14 @@ struct PLane {
         return lj;
     }
 
-    // commit_block! (src/local.jl:2495): states of charge, kinked dispatch, node balances
+    // commit_block! (src/local.jl:2495): states of charge, kinked dispatch, node balances (each
+    // global write by one lane)
     __device__ __noinline__ void commit(real t) const {
         eval(t);
         for (int u = 0; u < U; ++u) {
             int n = node(u);
             for (int s = 0; s < (lvl ? 0 : 2); ++s) {  // end steps: the compensation and the node balance
+                if (lane != 0) break;
                 int i = s * U + u, tau = tau_end(s);
                 real ph = S(LL.kph, i);
                 int c = 0;
@@ -618,7 +711,7 @@ struct PLane {
             }
             int nt = nterms(u, t);  // interior steps whose injection changes
             bool in = inside(u, t);
-            for (int i = 0; i < nt; ++i) {
+            for (int i = lane; i < nt; i += NL) {
                 int q = term_q(u, t, i);
                 if (!in && quiet(u, q, t)) continue;
                 real dj, d1;
@@ -627,13 +720,15 @@ struct PLane {
             }
         }
         for (int u = 0; u < U; ++u)
-            for (int p = 0; p < ns(); ++p) M.e[ix(uj[u], stp(q0() + p))] += t;
+            for (int p = lane; p < ns(); p += NL) M.e[ix(uj[u], stp(q0() + p))] += t;
+        if constexpr (COOP) __syncwarp();
     }
 };
 
 // One class pass of the storage multiscale sweep: threads take (block, replica) tasks (replica
-// fastest) and run the class's moves in order.
-template <class real>
+// fastest) and run the class's moves in order. COOP: one warp per task (long blocks, whose moves
+// loop over up to 128 steps and whose passes have few tasks).
+template <class real, bool COOP>
 __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevModel<real> M,
                                                  const __grid_constant__ PlatMoves mv, uint32_t sweep,
                                                  real *scratch, unsigned long long *stats) {
@@ -643,11 +738,13 @@ __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevM
     size_t nthr = (size_t)gridDim.x * blockDim.x;
     bool loc = LL.total <= ESM_PLAT_LOCAL;
     real *slab = loc ? local : scratch + gid;
-    PLane<real> Ln(M, LL, slab, loc ? 1 : (int)nthr);
+    PLane<real, COOP> Ln(M, LL, slab, loc ? 1 : (int)nthr);
+    Ln.lane = COOP ? (int)(threadIdx.x & 31) : 0;
     Ln.L = mv.L;
     unsigned long long tried = 0, moved = 0, guards = 0;
     size_t ntask = (size_t)mv.nb * M.R;
-    for (size_t task = gid; task < ntask; task += nthr) {
+    size_t t0 = COOP ? gid >> 5 : gid, ts = COOP ? nthr >> 5 : nthr;
+    for (size_t task = t0; task < ntask; task += ts) {
         int k = (int)(task / M.R);
         Ln.rep = (int)(task % M.R);
         Ln.b0 = mv.o + (2 * k + mv.cls) * mv.L;
@@ -676,9 +773,11 @@ __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevM
             if (t != 0) ++moved;
         }
     }
-    if (tried) atomicAdd(&stats[0], tried);
-    if (moved) atomicAdd(&stats[1], moved);
-    if (guards) atomicAdd(&stats[2], guards);
+    if (Ln.lane == 0) {
+        if (tried) atomicAdd(&stats[0], tried);
+        if (moved) atomicAdd(&stats[1], moved);
+        if (guards) atomicAdd(&stats[2], guards);
+    }
 }
 
 // The long-range storage sweep (storage_long_sweep!, src/storage_long.jl:245): threads take (unit,
@@ -696,10 +795,11 @@ __global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__
     size_t nthr = (size_t)gridDim.x * blockDim.x;
     bool loc = LL.total <= ESM_PLAT_LOCAL;
     real *slab = loc ? local : scratch + gid;
-    PLane<real> Ln(M, LL, slab, loc ? 1 : (int)nthr);
+    PLane<real, true> Ln(M, LL, slab, loc ? 1 : (int)nthr);  // one warp per task
+    Ln.lane = threadIdx.x & 31;
     unsigned long long tried = 0, moved = 0, guards = 0;
     size_t ntask = (size_t)nunits * M.R;
-    for (size_t task = gid; task < ntask; task += nthr) {
+    for (size_t task = gid >> 5; task < ntask; task += nthr >> 5) {
         const int *pu = plan + (task / M.R) * ESM_SL_STRIDE;
         Ln.rep = (int)(task % M.R);
         Ln.U = 1;
@@ -730,16 +830,18 @@ __global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__
             if (t != 0) ++moved;
         }
     }
-    if (tried) atomicAdd(&stats[0], tried);
-    if (moved) atomicAdd(&stats[1], moved);
-    if (guards) atomicAdd(&stats[2], guards);
+    if (Ln.lane == 0) {
+        if (tried) atomicAdd(&stats[0], tried);
+        if (moved) atomicAdd(&stats[1], moved);
+        if (guards) atomicAdd(&stats[2], guards);
+    }
 }
 
 template <class real>
 cudaError_t launch_storage_long(const DevModel<real> &M, const int *plan, int nunits, uint32_t sweep, real *scratch,
                                 int threads, unsigned long long *stats, cudaStream_t s) {
-    size_t ntask = (size_t)nunits * M.R;
-    int blocks = (int)(((size_t)threads < ntask ? (size_t)threads : ntask) + 127) / 128;
+    size_t nthr = (size_t)nunits * M.R * 32;  // one warp per (unit, replica) task
+    int blocks = (int)(((size_t)threads < nthr ? (size_t)threads : nthr) + 127) / 128;
     k_storage_long<real><<<blocks, 128, 0, s>>>(M, plan, nunits, sweep, scratch, stats);
     return cudaGetLastError();
 }
@@ -751,7 +853,8 @@ int plateau_threads(const DevModel<real> &M) {
     int nb = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_plateau<real>, 128, 0) != cudaSuccess || nb < 1) nb = 4;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_plateau<real, false>, 128, 0) != cudaSuccess || nb < 1)
+        nb = 4;
     return nb * nsm * 128;
 }
 template <class real>
@@ -762,9 +865,13 @@ size_t plateau_scratch_reals(const DevModel<real> &M) {
 template <class real>
 cudaError_t launch_plateau(const DevModel<real> &M, const PlatMoves &mv, uint32_t sweep, real *scratch, int threads,
                            unsigned long long *stats, cudaStream_t s) {
-    size_t ntask = (size_t)mv.nb * M.R;
-    int blocks = (int)(((size_t)threads < ntask ? (size_t)threads : ntask) + 127) / 128;
-    k_plateau<real><<<blocks, 128, 0, s>>>(M, mv, sweep, scratch, stats);
+    bool coop = mv.L >= 32;  // long blocks: one warp per task
+    size_t nthr = (size_t)mv.nb * M.R * (coop ? 32 : 1);
+    int blocks = (int)(((size_t)threads < nthr ? (size_t)threads : nthr) + 127) / 128;
+    if (coop)
+        k_plateau<real, true><<<blocks, 128, 0, s>>>(M, mv, sweep, scratch, stats);
+    else
+        k_plateau<real, false><<<blocks, 128, 0, s>>>(M, mv, sweep, scratch, stats);
     return cudaGetLastError();
 }
 
