@@ -251,11 +251,17 @@ def profile_case(args):
     m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
     d = DeviceChain(m, w["R"], precision=32, seed=w["seed"])
     d.upload(initial_state(m, w["R"], seed=7))
+    grid = None
+    if args.grid:
+        d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
+    elif args.autotune:
+        grid = d.autotune_moves(sweep=0)[0]
     d.sweeps(args.warmup, 0, stats=False)
     d.set_timing(True)
     st = d.sweeps(args.steps, args.warmup)
     kt = d.timing()
-    print(json.dumps({"case": "small", "T": w["T"], "R": w["R"], "sweeps": args.steps,
+    print(json.dumps({"case": "small", "N": w["N"], "T": w["T"], "R": w["R"], "sweeps": args.steps,
+                      "grid": list(d.move_grid()[:2]),
                       "kernel_ms": {k: v[0] for k, v in kt.items()}, "launches": {k: v[1] for k, v in kt.items()},
                       "moves_tried": int(st[:20:2].sum()), "guards": int(st[-1])}), flush=True)
 
@@ -302,6 +308,8 @@ def batch_case(args):
         m = make_model(N, int(round(1.5 * N)), T, seed=1000 + i)
         d = DeviceChain(m, 16, precision=32, seed=1000 + i)
         d.upload(initial_state(m, 16, seed=7))
+        if args.grid:
+            d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
         chains.append((m, d))
     setup = time.perf_counter() - t0
     for m, d in chains:                       # warm-up: captures each context's class graphs
@@ -344,6 +352,7 @@ def main():
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
     ap.add_argument("--storage-ms", action="store_true",
                     help="operation sweeps include the storage sweeps: multiscale (probability 1/2) and long-range")
+    ap.add_argument("--autotune", action="store_true", help="--case small: the autotuner picks the line-move grid")
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
     ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage"],

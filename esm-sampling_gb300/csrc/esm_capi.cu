@@ -89,7 +89,9 @@ struct esm_ctx {
     double kappa_min = 1.0;
     int *d_sl_plan = nullptr;            // the long-range sweep's per-unit move lists
     int sms_threads = 0;
+    size_t sms_per = 0;                  // reals of global scratch per storage-kernel thread (0: local arrays)
     void *d_sms_scratch = nullptr;
+    int scratch_warps = 0;               // line-move warps the global scratch holds (0: no global scratch needed)
     unsigned long long *d_sms_stats = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // a whole class pass, per class
     // weather
@@ -458,8 +460,17 @@ int alloc_state(esm_ctx *c) {
     c->nsm = nsm;
     c->move_wpb = 1;
     c->max_warps = c->warps_cap[0];
+    // the global scratch, when the layout needs one, is first sized for the larger grids only up to
+    // 1 GB (never fewer warps than the one-warp blocks' limit): many contexts share one GPU;
+    // esm_set_move_grid grows it when a larger grid is set
     size_t per = esm::linemove_scratch_reals<real>(M);
-    if ((rc = dalloc(c, &q, per * (size_t)wmax))) return rc;
+    size_t wscr = (size_t)wmax;
+    if (per > 0) {
+        size_t fit = ((size_t)1 << 30) / (per * sizeof(real));
+        wscr = std::max((size_t)c->warps_cap[0], std::min(wscr, fit));
+        c->scratch_warps = (int)wscr;
+    }
+    if ((rc = dalloc(c, &q, per * wscr))) return rc;
     c->d_scratch = q;
     // the move descriptors of a class pass
     char *dp;
@@ -469,12 +480,10 @@ int alloc_state(esm_ctx *c) {
     if ((rc = dalloc(c, &ctr, (size_t)(M.natoms + M.nextra)))) return rc;
     c->d_item_ctr = ctr;
     if ((rc = dalloc(c, &c->d_sweep, 1))) return rc;
-    // storage multiscale sweep: resident threads of its kernel and, when the lane layout exceeds the
-    // local arrays, one global scratch column per thread
+    // storage sweeps: resident threads of their kernels; the global scratch they need when the lane
+    // layout exceeds the local arrays is allocated at their first use (sms_scratch)
     c->sms_threads = esm::plateau_threads<real>(M);
-    size_t sper = esm::plateau_scratch_reals<real>(M);
-    if ((rc = dalloc(c, &q, sper * (size_t)c->sms_threads))) return rc;
-    c->d_sms_scratch = q;
+    c->sms_per = esm::plateau_scratch_reals<real>(M);
     if ((rc = dalloc(c, &c->d_sms_stats, 3))) return rc;
     return ESM_OK;
 }
@@ -933,13 +942,30 @@ int sms_plan(const esm_ctx *c, uint32_t sweep, bool force, std::vector<esm::Plat
     return (int)out.size();
 }
 
+// the storage kernels' global scratch (layouts beyond the local arrays only), at their first use:
+// at most 256 MB, the grid capped to the threads it holds
+int sms_scratch(esm_ctx *c) {
+    if (c->sms_per == 0 || c->d_sms_scratch) return ESM_OK;
+    size_t rb = c->precision == 64 ? sizeof(double) : sizeof(float);
+    size_t fit = ((size_t)256 << 20) / (c->sms_per * rb);
+    int thr = (int)std::min((size_t)c->sms_threads, std::max((size_t)128, fit / 128 * 128));
+    char *q;
+    int rc = dalloc(c, &q, c->sms_per * rb * (size_t)thr);
+    if (rc) return rc;
+    c->d_sms_scratch = q;
+    c->sms_threads = thr;
+    return ESM_OK;
+}
+
 // the storage multiscale sweep of one operation sweep: caches rebuilt (LocalCost at the start of
 // storage_ms_sweep!, src/flowmoves.jl:261), then one launch per class pass
 int sms_sweep_any(esm_ctx *c, uint32_t sweep, bool force, int max_passes = 0) {
     std::vector<esm::PlatMoves> plan;
     if (sms_plan(c, sweep, force, plan) == 0) return ESM_OK;
     if (max_passes > 0 && (size_t)max_passes < plan.size()) plan.resize(max_passes);
-    int rc = rebuild_any(c);
+    int rc = sms_scratch(c);
+    if (rc) return rc;
+    if ((rc = rebuild_any(c))) return rc;
     if (rc) return rc;
     Span sp(c, ESM_KT_STORAGE);
     for (auto &mv : plan) {
@@ -990,6 +1016,7 @@ int sl_sweep_any(esm_ctx *c, uint32_t sweep) {
     if (rc) return rc;
     int nu = (int)plan.size() / ESM_SL_STRIDE;
     if (nu == 0) return ESM_OK;
+    if ((rc = sms_scratch(c))) return rc;
     if ((rc = rebuild_any(c))) return rc;  // LocalCost at the start (src/storage_long.jl:250)
     CK(cudaMemcpyAsync(c->d_sl_plan, plan.data(), sizeof(int) * plan.size(), cudaMemcpyHostToDevice, c->stream));
     Span sp(c, ESM_KT_STORAGE);
@@ -1427,6 +1454,19 @@ int esm_set_move_grid(esm_ctx *c, int32_t warps_per_block, int32_t warps_per_sm)
     if (w == c->max_warps && warps_per_block == c->move_wpb) return ESM_OK;
     int rc = esm_sync(c, 600.0);  // the captured class passes hold the old grid: drop them
     if (rc) return rc;
+    if (c->scratch_warps > 0 && w > c->scratch_warps) {  // the global scratch grows to the grid
+        size_t per = c->precision == 64 ? esm::linemove_scratch_reals<double>(c->Md) * sizeof(double)
+                                        : esm::linemove_scratch_reals<float>(c->Mf) * sizeof(float);
+        char *q;
+        if ((rc = dalloc(c, &q, per * (size_t)w))) return rc;
+        auto it = std::find(c->allocs.begin(), c->allocs.end(), c->d_scratch);
+        if (it != c->allocs.end()) {
+            cudaFree(*it);
+            c->allocs.erase(it);
+        }
+        c->d_scratch = q;
+        c->scratch_warps = w;
+    }
     for (auto &g : c->graph)
         if (g) {
             CK(cudaGraphExecDestroy(g));

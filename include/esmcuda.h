@@ -236,7 +236,10 @@ int esm_state_restore(esm_ctx *ctx);
    48 registers per thread) and with it the warps an SM holds (up to 24, 32 and 40); the warp count
    trades latency hiding against the cache footprint of the warps' walk scratch. esm_set_move_grid
    sets warps_per_block (1, 2, 4) and warps_per_sm (0: the resident limit of that shape; capped at
-   it) and drops the captured class graphs; the default is one-warp blocks at their limit.
+   it) and drops the captured class graphs; the default is one-warp blocks at their limit. Models
+   whose walk scratch exceeds the lanes' local arrays keep it in device memory, first sized for at
+   most 1 GB (never below the default grid) and grown (reallocated) by esm_set_move_grid when a
+   larger grid is set.
    esm_move_grid reads the current shape, warps per SM and the limits of the three shapes
    (limits_per_sm[3]). No reference counterpart (the reference threads the steps of a class on the
    host, src/local.jl:1954). */

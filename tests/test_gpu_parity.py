@@ -210,9 +210,12 @@ def test_class_pass_large_model_global_scratch():
     s = o.get_state()
     for k in ("theta", "g", "e", "z", "reg", "k"):
         setattr(st, k, s[k])
-    for limit in (20, 0):
+    for limit, grid in ((20, None), (0, None), (20, (4, 0))):
         d = DeviceChain(m, 8, precision=64, seed=5)
         d.upload(st)
+        if grid:  # four-warp blocks at their limit: the global scratch grows to the grid
+            d.set_move_grid(*grid)
+            assert d.move_grid()[0] == 4
         o = Oracle(m, 8, seed=5)
         o.set_state(st)
         sd = d.class_pass(3, 0, limit)
