@@ -330,6 +330,18 @@ def batch_case(args):
                       "sizes": {"N": [n for n, _ in specs], "T": [t for _, t in specs]}}), flush=True)
 
 
+def job_rate(pg, world, steps, seconds):
+    """Whole-job rate of `world` ranks that each ran `steps` units: world * steps over the slowest
+    rank's time (max over ranks, after which every rank holds the same value); (rate, seconds)."""
+    if pg:
+        import torch
+        t = torch.tensor([float(seconds)], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        seconds = float(t[0])
+        pg.barrier()
+    return world * steps / seconds, seconds
+
+
 def config_dict():
     w = WORKLOAD
     return {"workload": "plain replica sampler on GPU: 40 nodes, 60 lines, T=8760 hourly, 64 replicas",
@@ -414,21 +426,15 @@ def main():
     kt = d.timing()
     launches = d.launch_count() - launches0
     dev_ms = sum(v[0] for v in kt.values())
-    if pg:
-        import torch
-        t = torch.tensor([dev_ms])
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dev_ms = float(t[0])
-        pg.barrier()
-    value = world * args.steps / (dev_ms / 1000.0)
+    value, dev_s = job_rate(pg, world, args.steps, dev_ms / 1000.0)
+    dev_ms = 1000.0 * dev_s
     # end to end through the public API, host driver included
     Rset = RP.ReplicaSet(M=R, eta_w=[5e-4] * len(m.carriers))
     d.sync(600.0)
     t0 = time.perf_counter()
     h2d, d2h = e2e_loop(d, m, ctl, Rset, it0 + args.warmup + args.steps, args.steps, rng)
     d.sync(600.0)
-    e2e_wall = time.perf_counter() - t0
-    e2e = world * args.steps / e2e_wall
+    e2e, e2e_wall = job_rate(pg, world, args.steps, time.perf_counter() - t0)
     # the storage multiscale sweep on its own (one forced sweep, every class pass), device time
     d.sync(600.0)
     d.set_timing(True)
