@@ -5,6 +5,10 @@
 
 #include "../../include/esmcuda.h"
 
+// TAG_SWEEP (0, 0, 0, sweep) class order; TAG_LIST (j/2, tile, class, sweep) move list and selection;
+// TAG_LANE (2 move + h, step, replica, sweep) a line move's uniforms; TAG_LGV (j/2, group, it, 0)
+// Langevin normals; TAG_WTH (j/2, t, replica, it) weather; TAG_SMS / TAG_SML the storage multiscale
+// sweep's plan and block uniforms; TAG_SLG / TAG_SLL the long-range storage sweep's plan and uniforms
 #define ESM_TAG_SWEEP 0x53574550u
 #define ESM_TAG_LIST 0x4C495354u
 #define ESM_TAG_LANE 0x4C414E45u
@@ -18,7 +22,9 @@
 namespace esm {
 
 // ---------------------------------------------------------------------------------------------
-// Philox4x32-10 (Salmon et al., SC11); stream layout documented in include/esmcuda.h and the design doc
+// Philox4x32-10 (Salmon et al., SC11); key (seed low word, seed high word ^ tag), one call per
+// counter (w0, w1, w2, w3) gives two 53-bit uniforms; the tags and counter words of every stream
+// are listed with the ESM_TAG_* constants below
 // ---------------------------------------------------------------------------------------------
 __host__ __device__ inline void philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                                        uint32_t out[4]) {

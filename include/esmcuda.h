@@ -18,8 +18,9 @@
  *    (x*T + t)*R + r. X is N (angles), D (dispatchable units), S (storage units) or n0 (weather
  *    series). This is the layout of the reference port's DeviceState (device/src/core.jl).
  *  - One context per host thread; one CUDA stream per context.
- *  - Random numbers: counter-based Philox4x32-10 streams keyed by the context seed; the exact
- *    stream layout is part of the contract so that the CPU oracle can replay it.
+ *  - Random numbers: counter-based Philox4x32-10 streams keyed by the context seed and a tag per
+ *    stream; the exact stream layout (tags and counter words) is part of the contract, so that a
+ *    CPU restatement of the algorithm can replay every draw.
  */
 #ifndef ESMCUDA_H
 #define ESMCUDA_H
