@@ -470,7 +470,9 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": kind,
                          "kernel": "k_prep_moves + k_move (the line moves of one colour class, one span)",
-                         "note": "the exact line sampler is FP32-issue-bound; the HBM bytes are the compulsory state"},
+                         "note": ("the exact line sampler is latency-bound (per-lane walk scratch, divergent walks): "
+                                  "the HBM bytes are the compulsory state; `traffic` is the measured DRAM traffic, "
+                                  "mostly walk scratch")},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "clocks": clocks,
             "move_grid": {"warps_per_block": grid[0], "warps_per_sm": grid[1],
