@@ -165,6 +165,7 @@ def e2e_loop(d, m, ctl, R_set, it0, n, rng):
             if bursts[j]:
                 R_set.since[j], R_set.window[j], R_set.active[j] = 0, bool(window[j] > 0), False
                 R_set.gbuf[j].clear()
+                R_set.hist[j].clear()
             else:
                 R_set.since[j] += 1
         if moved.any():
@@ -178,6 +179,7 @@ def e2e_loop(d, m, ctl, R_set, it0, n, rng):
         fkm = RP.masked_mean(fk, mask)
         for j in range(d.R):
             RP.update_gate(R_set, j, [RP.masked_mean(ratio * sk[j], mask) / fkm], ctl)
+            RP.record_hist(R_set, j, ratio * sk[j], ctl)
         wts = RP.drift_weights(ctl, np.zeros(d.R), R_set.active)
         knew, _ = d.langevin_step(wts, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
         h2d += wts.nbytes + eta.nbytes + ks.nbytes

@@ -88,6 +88,7 @@ struct esm_ctx {
     std::vector<double> ulo, uhi, uhours;
     double kappa_min = 1.0;
     int *d_sl_plan = nullptr;            // the long-range sweep's per-unit move lists
+    esm_ctx *probe = nullptr;            // one-replica context of the lag probe (esm_opts.probe)
     int sms_threads = 0;
     size_t sms_per = 0;                  // reals of global scratch per storage-kernel thread (0: local arrays)
     void *d_sms_scratch = nullptr;
@@ -785,6 +786,18 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         c->d_r0 = q;
     }
     CK(cudaStreamSynchronize(c->stream));
+    if (o->probe) {  // the lag probe's one-replica context, with its own streams
+        esm_opts po = *o;
+        po.R = 1;
+        po.span = 0;
+        po.probe = 0;
+        po.seed = esm_probe_seed(o->seed);
+        int prc = esm_create(m, &po, &c->probe);
+        if (prc) {
+            std::string msg = c->probe ? esm_last_error(c->probe) : "";
+            return fail(c, prc, "probe context: %s", msg.c_str());
+        }
+    }
     return ESM_OK;
 }
 
@@ -800,6 +813,7 @@ int esm_destroy(esm_ctx *c) {
         if (g) cudaGraphExecDestroy(g);
     for (void *p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->probe) esm_destroy(c->probe);
     delete c->snap;
     delete c;
     return ESM_OK;
@@ -1441,6 +1455,62 @@ int esm_state_restore(esm_ctx *c) {
     if ((rc = rebuild_any(c))) return rc;
     CK(cudaStreamSynchronize(c->stream));
     c->has_scores = false;
+    return ESM_OK;
+}
+
+namespace {
+template <class T>
+__global__ void k_gather_replica(const T *src, T *dst, size_t n, int R, int j) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i * R + j];
+}
+template <class T>
+int gather_replica(esm_ctx *c, const void *src, void *dst, size_t n, int j) {
+    if (n == 0) return ESM_OK;
+    k_gather_replica<T><<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>((const T *)src, (T *)dst, n, c->R, j);
+    CK(cudaGetLastError());
+    return ESM_OK;
+}
+template <class real>
+int probe_copy(esm_ctx *c, int j) {  // replica j of c into the probe context (its single replica)
+    esm_ctx *p = c->probe;
+    size_t T = (size_t)c->T;
+    int rc;
+    if ((rc = gather_replica<real>(c, c->theta, p->theta, c->N * T, j))) return rc;
+    if ((rc = gather_replica<real>(c, c->g, p->g, c->D * T, j))) return rc;
+    if ((rc = gather_replica<real>(c, c->e, p->e, c->S * T, j))) return rc;
+    if ((rc = gather_replica<real>(c, c->z, p->z, c->n0 * T, j))) return rc;
+    if ((rc = gather_replica<int32_t>(c, c->d_reg, p->d_reg, T, j))) return rc;
+    CK(cudaMemcpyAsync(p->d_k, c->d_k, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream));
+    return esm_sync(c, 600.0);
+}
+}  // namespace
+
+int esm_lag_probe(esm_ctx *c, int32_t j, int32_t nsweeps, int32_t tail, int64_t sweep0, double *sk_mean,
+                  double *fk) {
+    if (!c) return ESM_EINVAL;
+    if (!c->probe) return fail(c, ESM_ESTATE, "no probe context (esm_opts.probe = 0)");
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    if (j < 0 || j >= c->R || nsweeps < 1 || tail < 1 || tail > nsweeps)
+        return fail(c, ESM_EINVAL, "bad probe arguments");
+    int rc = esm_sync(c, 600.0);
+    if (rc) return rc;
+    rc = c->precision == 64 ? probe_copy<double>(c, j) : probe_copy<float>(c, j);
+    if (rc) return rc;
+    esm_ctx *p = c->probe;
+    if ((rc = set_kc_any(p, p->d_k))) return fail(c, rc, "probe: %s", p->err.c_str());
+    p->has_state = true;
+    p->has_scores = false;
+    std::vector<double> sk(c->K), f(c->K);
+    if (sk_mean) std::fill(sk_mean, sk_mean + c->K, 0.0);
+    for (int q = 0; q < nsweeps; ++q) {
+        if ((rc = esm_operation_sweeps(p, 1, sweep0 + q, nullptr))) return fail(c, rc, "probe: %s", p->err.c_str());
+        if (q < nsweeps - tail) continue;
+        if ((rc = esm_capacity_scores(p, sk.data(), f.data(), nullptr))) return fail(c, rc, "probe: %s", p->err.c_str());
+        if (sk_mean)
+            for (int i = 0; i < c->K; ++i) sk_mean[i] += sk[i] / tail;
+    }
+    if (fk) std::copy(f.begin(), f.end(), fk);
     return ESM_OK;
 }
 

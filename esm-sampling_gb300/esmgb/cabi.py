@@ -48,6 +48,7 @@ class EsmOpts(C.Structure):
         ("R", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64), ("extra", C.c_double),
         ("maxnats", C.c_double), ("kappa_min", C.c_double), ("max_points", C.c_int32), ("span", C.c_int32),
         ("family_rates", C.c_double * NFAM), ("storage_ms", C.c_int32), ("storage_long", C.c_int32),
+        ("probe", C.c_int32),
     ]
 
 
@@ -114,6 +115,11 @@ class ModelBuffers:
         self.natoms = int(fap[-1])
 
 
+def probe_seed(seed):
+    """esm_probe_seed: the seed of the lag probe's streams."""
+    return int(seed) ^ 0x50524F4245000000
+
+
 def storage_groups(m: SynthModel):
     """The cell-class aggregates of the storage multiscale sweep (src/flowmoves.jl:270-274): the
     storage units grouped by (country cell of their node, carrier), keys in sorted order, units in
@@ -128,10 +134,11 @@ def storage_groups(m: SynthModel):
 
 
 def make_opts(R, precision=32, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-              rates=FAMILY_RATES, storage_ms=0, storage_long=0) -> EsmOpts:
+              rates=FAMILY_RATES, storage_ms=0, storage_long=0, probe=0) -> EsmOpts:
     o = EsmOpts()
     o.R, o.precision, o.seed, o.extra, o.maxnats, o.kappa_min = R, precision, seed, extra, maxnats, kappa_min
     o.max_points, o.span, o.storage_ms, o.storage_long = max_points, span, int(storage_ms), int(storage_long)
+    o.probe = int(probe)
     for i, r in enumerate(rates):
         o.family_rates[i] = r
     return o

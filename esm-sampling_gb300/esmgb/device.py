@@ -23,7 +23,7 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
            "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
-           "esm_autotune_moves", "esm_storage_ms", "esm_storage_long")
+           "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -75,6 +75,7 @@ def load(build_if_missing=True):
     L.esm_set_move_grid.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     L.esm_storage_ms.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
     L.esm_storage_long.argtypes = [C.c_void_p, C.c_int64, P_i64]
+    L.esm_lag_probe.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int64, P_f64, P_f64]
     L.esm_move_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
     L.esm_autotune_moves.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
     L.esm_launch_count.restype = C.c_int64
@@ -96,13 +97,13 @@ class DeviceChain:
 
     def __init__(self, model: SynthModel, R: int, precision: int = 32, seed: int = 1, extra: float = 4.0,
                  maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 0, span: int = 0,
-                 storage_ms: int = 0, storage_long: int = 0):
+                 storage_ms: int = 0, storage_long: int = 0, probe: int = 0):
         self.L = load()
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
         self.opts: EsmOpts = make_opts(R, precision, seed, extra, maxnats, kappa_min, max_points, span,
-                                       storage_ms=storage_ms, storage_long=storage_long)
+                                       storage_ms=storage_ms, storage_long=storage_long, probe=probe)
         h = C.c_void_p()
         rc = self.L.esm_create(C.byref(self.buf.struct), C.byref(self.opts), C.byref(h))
         self.h = h
@@ -181,6 +182,14 @@ class DeviceChain:
         st = np.zeros(3, np.int64)
         self._check(self.L.esm_storage_long(self.h, sweep, _p(st, P_i64)), "esm_storage_long")
         return st
+
+    def lag_probe(self, j, nsweeps=30, tail=10, sweep0=0):
+        """esm_lag_probe: (mean capacity score of the last `tail` of `nsweeps` operation sweeps of a
+        frozen copy of replica j, the last prior term fk); the chain is unchanged."""
+        sk = np.zeros(self.m.Kunits)
+        fk = np.zeros(self.m.Kunits)
+        self._check(self.L.esm_lag_probe(self.h, j, nsweeps, tail, sweep0, _p(sk), _p(fk)), "esm_lag_probe")
+        return sk, fk
 
     def scores(self):
         m, R = self.m, self.R

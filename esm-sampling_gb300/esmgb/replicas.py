@@ -190,3 +190,34 @@ def interior_nodes(k, hi, lo=50.0):
 def masked_mean(v, mask):
     v = np.asarray(v)
     return float(v[mask].mean()) if mask.any() else math.nan
+
+
+def record_hist(R: ReplicaSet, j: int, rs, ctl: ReplicaCtl):
+    """``src/replicas.jl:690-693``: an active replica's score record r s joins its in-flight window
+    of the last ``probe_win`` records."""
+    if R.active[j]:
+        R.hist[j].append(np.array(rs, float))
+        if len(R.hist[j]) > ctl.probe_win:
+            R.hist[j].pop(0)
+
+
+def probe_candidate(R: ReplicaSet, ctl: ReplicaCtl):
+    """``src/replicas.jl:717`` probe_candidate (0-based): among the active replicas with a full
+    in-flight window (``probe_win`` score records), the one longest after its burst; None if none."""
+    cand = [j for j in range(R.M) if R.active[j] and len(R.hist[j]) >= ctl.probe_win]
+    if not cand:
+        return None
+    return max(cand, key=lambda j: (R.since[j], -j))
+
+
+def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, sweep0: int = 0):
+    """``src/replicas.jl:733`` lag_probe: the device runs ``probe_len`` operation sweeps of a frozen
+    copy of replica j (esm_lag_probe; the chain is unchanged) and returns the mean capacity score of
+    the last ``probe_tail``; the gap of the in-flight scores (the mean of ``hist``, replica j's
+    records of r s, r = beta_k / beta_v, as record_hist keeps them) against it is formed on the
+    interior nodes, per k field: gap = (<r s_in> - <r s_eq>) / <fk>."""
+    sk_eq, fk = dev.lag_probe(j, ctl.probe_len, ctl.probe_tail, sweep0)
+    inflight = np.mean(np.asarray(hist, float), axis=0)
+    mask = interior_nodes(k, hi)
+    rs_eq, rs_in, fkm = masked_mean(ratio * sk_eq, mask), masked_mean(inflight, mask), masked_mean(fk, mask)
+    return {"gap": [(rs_in - rs_eq) / fkm], "rs_eq": [rs_eq], "rs_in": [rs_in], "fk": [fkm]}

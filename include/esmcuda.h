@@ -133,7 +133,12 @@ typedef struct esm_opts {
                                   0: the local sweep only */
     int32_t storage_long;      /* 1: then the long-range storage sweep (storage_long_sweep!,
                                   src/storage_long.jl:245; probability 1, the default of src/run.jl:27) */
+    int32_t probe;             /* 1: create the one-replica context of esm_lag_probe (its streams are
+                                  keyed by esm_probe_seed(seed)) */
 } esm_opts;
+
+/* The seed of the lag probe's streams (the reference's separate probe stream, src/replicas.jl:873). */
+static inline uint64_t esm_probe_seed(uint64_t seed) { return seed ^ 0x50524F4245000000ull; }
 
 /* The automatic point cap: 192, or 4 points per unit of the largest state-of-charge atom when that
    is more (measured guard rates: 0 at 40 nodes with 192; 0.06 % at 256 nodes with 1024). */
@@ -255,6 +260,15 @@ int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_p
    best[2], the candidate pairs cand[2*ESM_TUNE_MAX], their times in ms ms[ESM_TUNE_MAX], their count. */
 #define ESM_TUNE_MAX 16
 int esm_autotune_moves(esm_ctx *ctx, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand);
+
+/* Lag probe (lag_probe, src/replicas.jl:733): a copy of replica j, at the chain's capacities and
+   with its weather frozen, runs nsweeps operation sweeps (sweep indices sweep0 ...; the probe
+   context's streams) and sk_mean [K] receives the mean capacity score of the last `tail` sweeps, fk
+   [K] (may be NULL) the prior term of the last; the chain is unchanged. The host forms the gap
+   against the replica's in-flight scores and adapts the step (adapt_step!, :758). Needs
+   esm_opts.probe = 1. */
+int esm_lag_probe(esm_ctx *ctx, int32_t j, int32_t nsweeps, int32_t tail, int64_t sweep0, double *sk_mean,
+                  double *fk);
 
 /* Fraction of (step, replica) pairs in each (regime, season): occ [nreg*4], regime-major, the
    season of a step as season (src/weather.jl:50). The regime summary fed to the surrogate. */

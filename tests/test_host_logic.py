@@ -69,3 +69,35 @@ def test_convergence_diagnostics():
     assert CV.rhat_rank([rng.standard_normal(1000) * (2.0 if k == 0 else 1.0) for k in range(4)]) > 1.01
     rw = [np.cumsum(rng.standard_normal(1000)) for _ in range(4)]
     assert CV.rhat_rank(rw) > 1.01 or CV.ess_bulk(rw) < 400
+
+
+def test_probe_candidate_hist_and_gap():
+    """probe_candidate / record_hist / lag_probe of src/replicas.jl:690-750 on the host, with a
+    fake device whose probe returns fixed equilibrium scores."""
+    ctl = RP.ReplicaCtl(M=4, probe_win=3, probe_len=5, probe_tail=2)
+    R = RP.ReplicaSet(M=4, eta_w=[1e-3])
+    R.active = [True, True, False, True]
+    R.since = [5, 9, 12, 9]
+    for q in range(4):
+        for j in range(4):
+            RP.record_hist(R, j, [float(q)] * 3, ctl)
+    assert [len(h) for h in R.hist] == [3, 3, 0, 3]   # the inactive replica keeps no window
+    assert R.hist[0][0][0] == 1.0                      # the oldest record left the window
+    assert RP.probe_candidate(R, ctl) == 1             # longest since its burst; first on ties
+    R.hist[1] = R.hist[1][:2]
+    assert RP.probe_candidate(R, ctl) == 3
+    R.active = [False] * 4
+    assert RP.probe_candidate(R, ctl) is None
+
+    class FakeDev:
+        def lag_probe(self, j, n, tail, sweep0):
+            assert (j, n, tail, sweep0) == (3, 5, 2, 40)
+            return np.array([1.0, 2.0, 4.0]), np.array([0.5, 0.5, 9.0])
+
+    k = np.array([100.0, 200.0, 10.0])                # the third unit is below 50 MW: not interior
+    hi = np.full(3, 20000.0)
+    hist = [np.array([3.0, 5.0, 7.0]), np.array([5.0, 7.0, 9.0])]
+    pr = RP.lag_probe(FakeDev(), 3, hist, ctl, 2.0, k, hi, 40)
+    # rs_in = mean(4, 6) = 5, rs_eq = 2 * mean(1, 2) = 3, fk = 0.5
+    assert pr["gap"][0] == pytest.approx((5.0 - 3.0) / 0.5)
+    assert pr["rs_in"][0] == pytest.approx(5.0) and pr["rs_eq"][0] == pytest.approx(3.0)
