@@ -265,7 +265,7 @@ def profile_case(args):
     print(json.dumps({"case": "small", "N": w["N"], "T": w["T"], "R": w["R"], "sweeps": args.steps,
                       "grid": list(d.move_grid()[:2]),
                       "kernel_ms": {k: v[0] for k, v in kt.items()}, "launches": {k: v[1] for k, v in kt.items()},
-                      "moves_tried": int(st[:20:2].sum()), "guards": int(st[-1])}), flush=True)
+                      "moves_tried": int(st[:-1:2].sum()), "guards": int(st[-1])}), flush=True)
 
 
 def storage_case(args):

@@ -408,8 +408,11 @@ int build_model(esm_ctx *c, const esm_model *m, const esm_opts *o) {
     for (int q = 0; q < ncell; ++q) maxcell = std::max(maxcell, m->cell_ptr[q + 1] - m->cell_ptr[q]);
     int maxunits = 1;
     for (int n = 0; n < N; ++n) maxunits = std::max(maxunits, m->units_ptr[n + 1] - m->units_ptr[n]);
-    int maxleak = 1;
+    // kinks of one move: the leak nodes of an xlocc pair, the two steps of a tsoc move, a tpot
+    // node and the far ends of its lines
+    int maxleak = 2;
     for (int p = 0; p < npair; ++p) maxleak = std::max(maxleak, m->xlk_ptr[p + 1] - m->xlk_ptr[p]);
+    for (int n = 0; n < N; ++n) maxleak = std::max(maxleak, nlp[n + 1] - nlp[n] + 1);
     M.maxe = std::max(std::max(maxatom, maxcell), 4) + 4;
     M.maxl = L;
     M.maxn = N;

@@ -39,7 +39,8 @@ struct Carve {
 template <class real>
 struct Desc {
     int *moves;
-    int *hdr;  // [0] ng, [1] nse, [2] nl, [3] nk, [4] nku, [5] nns, [6] nga, [7] nna, [8] nth, [9] valid, [10] fam
+    int *hdr;  // [0] ng, [1] nse, [2] nl, [3] nk, [4] nku, [5] nns, [6] nga, [7] nna, [8] nth, [9] valid, [10] fam,
+               // [11] nku0 (the kinked units of step tau; those of step tau - 1 follow)
     int *gi, *gpos;
     real *ga;
     int *si, *spos, *sposa;
@@ -52,6 +53,8 @@ struct Desc {
     real *kg;
     int *ku, *kk, *kupos;
     real *kda;  // direct coefficient of a kinked unit that the move also moves directly (else 0)
+    int *ksd;   // step of a kink: 0 tau, 1 tau - 1
+    int *kqs;   // storage unit whose requirement adjustment (soc_qadj) enters the kink, or -1
     int *nds, *nda;
     int *gia, *gposa;
     real *gaa;
@@ -85,6 +88,8 @@ __host__ __device__ inline Desc<real> carve_desc(char *base, const DevModel<real
     d.kk = c.take<int>(M.maxku);
     d.kupos = c.take<int>(M.maxku);
     d.kda = c.take<real>(M.maxku);
+    d.ksd = c.take<int>(M.maxk);
+    d.kqs = c.take<int>(M.maxk);
     d.nds = c.take<int>(M.N);
     d.nda = c.take<int>(M.N);
     d.gia = c.take<int>(4);
@@ -125,6 +130,8 @@ size_t desc_bytes(const DevModel<real> &M, int nmoves) {
     c.take<int>(M.maxku);
     c.take<int>(M.maxku);
     c.take<real>(M.maxku);
+    c.take<int>(M.maxk);
+    c.take<int>(M.maxk);
     c.take<int>(M.N);
     c.take<int>(M.N);
     c.take<int>(4);
@@ -242,7 +249,7 @@ struct Lane {
     __device__ __noinline__ real eval(real t) const {
         const int *hdr = d.hdr;
         int ng = hdr[0], nse = hdr[1], nl = hdr[2], nk = hdr[3], nku = hdr[4], nns = hdr[5], nga = hdr[6],
-            nna = hdr[7];
+            nna = hdr[7], nku0 = hdr[11];
         real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
         real D = 0, A = 0;
         // kinks (src/local.jl:605 update_kinks!)
@@ -254,21 +261,21 @@ struct Lane {
         for (int q = 0; q < nns; ++q) S(LL.drs, q) = 0;
         for (int q = 0; q < ng; ++q) {
             int j = d.gi[q];
-            real k = M.kc_d[j], A = M.d_avail[j];
+            real k = M.kc_d[j], av = M.d_avail[j];
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, tau)], t * d.ga[q], &dyc, &dex);
-            real dp = A * k * dyc;
+            real dp = av * k * dyc;
             D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.drs, d.gpos[q]) -= dp;
         }
-        for (int q = 0; q < nku; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
+        for (int q = 0; q < nku0; ++q) {  // kinked entries (prorata!, src/local.jl:1782)
             real ak = S(LL.kua, q), a = d.kda[q];
             if (ak == 0 && a == 0) continue;
             int j = d.ku[q];
-            real k = M.kc_d[j], A = M.d_avail[j];
+            real k = M.kc_d[j], av = M.d_avail[j];
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, tau)], t * a + ak * S(LL.kph, d.kk[q]), &dyc, &dex);
-            real dp = A * k * dyc;
+            real dp = av * k * dyc;
             D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.drs, d.kupos[q]) -= dp;
         }
@@ -294,12 +301,23 @@ struct Lane {
         for (int q = 0; q < nna; ++q) S(LL.dra, q) = 0;
         for (int q = 0; q < nga; ++q) {
             int j = d.gia[q];
-            real k = M.kc_d[j], A = M.d_avail[j];
+            real k = M.kc_d[j], av = M.d_avail[j];
             real dyc, dex;
             clamp_diff<real>(M.g[ix(j, taum)], t * d.gaa[q], &dyc, &dex);
-            real dp = A * k * dyc;
+            real dp = av * k * dyc;
             D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
             S(LL.dra, d.gposa[q]) -= dp;
+        }
+        for (int q = nku0; q < nku; ++q) {  // kinked entries at tau - 1 (prep_tsoc!, src/local.jl:1849)
+            real ak = S(LL.kua, q), a = d.kda[q];
+            if (ak == 0 && a == 0) continue;
+            int j = d.ku[q];
+            real k = M.kc_d[j], av = M.d_avail[j];
+            real dyc, dex;
+            clamp_diff<real>(M.g[ix(j, taum)], t * a + ak * S(LL.kph, d.kk[q]), &dyc, &dex);
+            real dp = av * k * dyc;
+            D += nzacc(dt * M.d_mc[j] * dp + cv * dt * (k + k0) * dex, A);
+            S(LL.dra, d.kupos[q]) -= dp;
         }
         for (int q = 0; q < nse; ++q) {
             int j = d.si[q];
@@ -405,7 +423,8 @@ struct Lane {
     // next primary breakpoint beyond tp in walking direction (finalize!, src/local.jl:656, scanned
     // instead of sorted: the same sequence); returns false if none
     __device__ __noinline__ bool next_bp(real tp, real sgn, real *out) const {
-        int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nk = d.hdr[3], nku = d.hdr[4], nga = d.hdr[6];
+        int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nk = d.hdr[3], nku = d.hdr[4], nga = d.hdr[6],
+            nku0 = d.hdr[11];
         bool have = false;
         real best = 0;
         auto consider = [&](real x) {
@@ -436,7 +455,7 @@ struct Lane {
             if (ak == 0 && a == 0) continue;
             int kq = d.kk[q];
             real Q = S(LL.kq, kq), gk = d.kg[kq];
-            real y0 = M.g[ix(d.ku[q], tau)];
+            real y0 = M.g[ix(d.ku[q], q < nku0 ? tau : taum)];
             real offs[4] = {real(0), real(0), -ak * Q, ak * Q};
             real sls[4] = {a + ak * gk, a, a, a + ak * gk};
             for (int h = 0; h < 4; ++h) {
@@ -919,13 +938,13 @@ struct Lane {
     __device__ __noinline__ void commit(real t) const {
         eval(t);
         int ng = d.hdr[0], nse = d.hdr[1], nl = d.hdr[2], nku = d.hdr[4], nns = d.hdr[5], nga = d.hdr[6],
-            nna = d.hdr[7], nth = d.hdr[8];
+            nna = d.hdr[7], nth = d.hdr[8], nku0 = d.hdr[11];
         for (int q = 0; q < nga; ++q) M.g[ix(d.gia[q], taum)] += t * d.gaa[q];
         for (int q = 0; q < nna; ++q) M.r[ix(d.nda[q], taum)] += S(LL.dra, q);
         for (int q = 0; q < ng; ++q) M.g[ix(d.gi[q], tau)] += t * d.ga[q];
         for (int q = 0; q < nku; ++q) {
             real ak = S(LL.kua, q), a = d.kda[q];
-            if (ak != 0 || a != 0) M.g[ix(d.ku[q], tau)] += t * a + ak * S(LL.kph, d.kk[q]);
+            if (ak != 0 || a != 0) M.g[ix(d.ku[q], q < nku0 ? tau : taum)] += t * a + ak * S(LL.kph, d.kk[q]);
         }
         for (int q = 0; q < nse; ++q) M.e[ix(d.si[q], tau)] += t * d.sa[q];
         for (int q = 0; q < nth; ++q) M.theta[ix(d.thn[q], tau)] += t * d.tha[q];
@@ -1016,6 +1035,7 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
     __syncwarp();
     int fam = mv >= 0 ? ESM_NFAM : -mv - 1;
     int ng = 0, nse = 0, nth = 0, nk = 0, nku = 0, nga = 0;
+    int nku0 = -1;  // kinked units of step tau (-1: all of them)
     real kmin = M.kmin;
     auto nun = [&](int n) { return M.up[n + 1] - M.up[n]; };
     bool ok = true;
@@ -1146,6 +1166,8 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
                         if (w0) {
                             d.kn[nk] = ln;
                             d.kg[nk] = gq;
+                            d.ksd[nk] = 0;
+                            d.kqs[nk] = -1;
                         }
                         for (int p = M.up[ln]; p < M.up[ln + 1]; ++p) {
                             int j = M.ua[p];
@@ -1289,8 +1311,103 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
                 ng = 1;
                 break;
             }
+            case ESM_FAM_TPOT: {  // prep_tpot! (src/local.jl:1741): the angle of node n rises by t
+                int n = st.pick(N);
+                if (M.theta_nnz[n] == 0) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.thn[0] = n;
+                    d.tha[0] = 1;
+                }
+                nth = 1;
+                // requirement change per unit t at the ends of n's lines (r[a] += f_e, r[b] -= f_e
+                // for a line a -> b), node by node in ascending order, each node's terms summed in
+                // line order; the dispatch there follows pro rata
+                int last = -1;
+                for (;;) {
+                    int nx = INT_MAX;
+                    for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) {
+                        int e = M.nl[p], a = M.bus0[e], b = M.bus1[e];
+                        if (a > last && a < nx) nx = a;
+                        if (b > last && b < nx) nx = b;
+                    }
+                    if (nx == INT_MAX) break;
+                    last = nx;
+                    real gm = 0;
+                    for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) {
+                        int e = M.nl[p], a = M.bus0[e], b = M.bus1[e];
+                        real df = M.lb[e] * real((a == n) - (b == n));
+                        if (a == nx) gm += df;
+                        if (b == nx) gm -= df;
+                    }
+                    if (gm == 0) continue;
+                    if (w0) {
+                        d.kn[nk] = nx;
+                        d.kg[nk] = gm;
+                        d.ksd[nk] = 0;
+                        d.kqs[nk] = -1;
+                    }
+                    for (int p = M.up[nx]; p < M.up[nx + 1]; ++p) {
+                        int j = M.ua[p];
+                        if (!(fabs(kappa_d(M, j)) >= kmin)) continue;
+                        if (w0) {
+                            d.ku[nku] = j;
+                            d.kk[nku] = nk;
+                        }
+                        ++nku;
+                    }
+                    ++nk;
+                }
+                break;
+            }
+            case ESM_FAM_TSOC: {  // prep_tsoc! (src/local.jl:1849): energy moved from step tau - 1 to tau
+                int n = st.pick(N);
+                int ns = M.sp[n + 1] - M.sp[n];
+                if (ns == 0) {
+                    ok = false;
+                    break;
+                }
+                int sj = M.sa[M.sp[n] + st.pick(ns)];
+                real ks = M.kc_s[sj] * M.s_hours[sj] / M.dt;
+                if (ks < kmin) {
+                    ok = false;
+                    break;
+                }
+                if (w0) {
+                    d.si[0] = sj;
+                    d.sa[0] = 1;
+                    // kink 0: node n at tau - 1 (+ks), kink 1: node n at tau (-ks), both with the
+                    // unit's requirement adjustment (soc_qadj)
+                    d.kn[0] = n;
+                    d.kg[0] = ks;
+                    d.ksd[0] = 1;
+                    d.kqs[0] = sj;
+                    d.kn[1] = n;
+                    d.kg[1] = -ks;
+                    d.ksd[1] = 0;
+                    d.kqs[1] = sj;
+                }
+                nse = 1;
+                nk = 2;
+                for (int side = 0; side < 2; ++side) {  // the kinked units of step tau first
+                    for (int p = M.up[n]; p < M.up[n + 1]; ++p) {
+                        int j = M.ua[p];
+                        if (!(fabs(kappa_d(M, j)) >= kmin)) continue;
+                        if (w0) {
+                            d.ku[nku] = j;
+                            d.kk[nku] = side == 0 ? 1 : 0;
+                        }
+                        ++nku;
+                    }
+                    if (side == 0) nku0 = nku;
+                }
+                break;
+            }
         }
     }
+    if (nku0 < 0) nku0 = nku;
     __syncwarp();
     if (!ok) return -1;
     // ---- finalize! (src/local.jl:656): zero tiny coefficients, lines, touched nodes
@@ -1320,20 +1437,28 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
             }
         nth = c;
         // a unit moved directly and pro rata is one term (add_kentry! adds to the unit's entry,
-        // src/local.jl:583): its direct coefficient moves into the kinked entry
+        // src/local.jl:583): its direct coefficient at the same step moves into the kinked entry
         for (int q = 0; q < nku; ++q) {
             d.kda[q] = 0;
-            for (int p = 0; p < ng; ++p)
-                if (d.gi[p] == d.ku[q] && d.ga[p] != 0) {
-                    d.kda[q] = d.ga[p];
-                    d.ga[p] = 0;
-                }
+            if (q < nku0) {
+                for (int p = 0; p < ng; ++p)
+                    if (d.gi[p] == d.ku[q] && d.ga[p] != 0) {
+                        d.kda[q] = d.ga[p];
+                        d.ga[p] = 0;
+                    }
+            } else {
+                for (int p = 0; p < nga; ++p)
+                    if (d.gia[p] == d.ku[q] && d.gaa[p] != 0) {
+                        d.kda[q] = d.gaa[p];
+                        d.gaa[p] = 0;
+                    }
+            }
         }
         // node lists: ws entries (gens, storage, kinked units), then line ends; wa entries, linked storage
         int nns = 0, nna = 0;
         for (int q = 0; q < ng; ++q) add_node(d, 0, M.d_bus[d.gi[q]], &nns, &d.gpos[q]);
         for (int q = 0; q < nse; ++q) add_node(d, 0, M.s_bus[d.si[q]], &nns, &d.spos[q]);
-        for (int q = 0; q < nku; ++q) add_node(d, 0, M.d_bus[d.ku[q]], &nns, &d.kupos[q]);
+        for (int q = 0; q < nku0; ++q) add_node(d, 0, M.d_bus[d.ku[q]], &nns, &d.kupos[q]);
         int nl = 0;
         for (int q = 0; q < nth; ++q) d.dth[d.thn[q]] = d.tha[q];
         for (int q = 0; q < nth; ++q) {
@@ -1359,6 +1484,7 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
             for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) d.lmark[M.nl[p]] = 0;
         }
         for (int q = 0; q < nga; ++q) add_node(d, 1, M.d_bus[d.gia[q]], &nna, &d.gposa[q]);
+        for (int q = nku0; q < nku; ++q) add_node(d, 1, M.d_bus[d.ku[q]], &nna, &d.kupos[q]);
         for (int q = 0; q < nse; ++q) add_node(d, 1, M.s_bus[d.si[q]], &nna, &d.sposa[q]);
         for (int q = 0; q < nns; ++q) d.nmarks[d.nds[q]] = 0;
         for (int q = 0; q < nna; ++q) d.nmarka[d.nda[q]] = 0;
@@ -1373,34 +1499,59 @@ __device__ __noinline__ int prep_move(const DevModel<real> &M, Desc<real> &d, St
         h[8] = nth;
         h[9] = (ng + nse + nth + nku) > 0;
         h[10] = fam;
+        h[11] = nku0;
     }
     __syncwarp();
     if (!d.hdr[9]) return -1;
     return fam;
 }
 
-// per-lane part of the kinks (prorata!, src/local.jl:1782): Q, e, P per leak node and the
-// kinked coefficients sigma/kappa; a lane without dispatch at a node has no kink there
+// soc_qadj (src/local.jl:1826) of storage unit j over the step from state ye to ye1: nominal minus
+// actual injection, k h (ye1 - ye) / dt - k (p+ - p-), the power that of soc_power (the clamped
+// state-of-charge difference less the standing loss, charged through eta_in or discharged
+// through eta_out up to the unit's rating)
+template <class real>
+__device__ inline real soc_qadj_unit(const DevModel<real> &M, int j, real ye, real ye1) {
+    real ec = clampr<real>(ye, 0, 1), ec1 = clampr<real>(ye1, 0, 1);
+    real dd = M.s_hours[j] * (ec1 - ec) / M.dt - M.s_qt[j];
+    real pc = 0, mcx = 0;
+    if (dd >= 0)
+        pc = M.s_etain[j] > 0 ? dd / M.s_etain[j] : real(0);
+    else
+        mcx = fmin(-dd * M.s_etaout[j], real(1));
+    return M.kc_s[j] * M.s_hours[j] * (ye1 - ye) / M.dt - M.kc_s[j] * (pc - mcx);
+}
+
+// per-lane part of the kinks (prorata!, src/local.jl:1782): Q, e, P per kink node (at its step,
+// tau or tau - 1, with the storage adjustment where the move sets one) and the kinked
+// coefficients sigma/kappa; a lane without dispatch at a node has no kink there
 template <class real>
 __device__ __noinline__ void lane_kinks(const Lane<real> &Ln) {
     const DevModel<real> &M = Ln.M;
     const Desc<real> &d = Ln.d;
-    int nk = d.hdr[3], nku = d.hdr[4];
+    int nk = d.hdr[3], nku = d.hdr[4], nku0 = d.hdr[11];
     for (int q = 0; q < nk; ++q) {
         int m = d.kn[q];
+        int step = d.ksd[q] ? Ln.taum : Ln.tau;
         real Pm = 0, Qs = 0;
         int nu = 0;
         for (int p = M.up[m]; p < M.up[m + 1]; ++p) {
             int j = M.ua[p];
             real kap = kappa_d(M, j);
             if (!(fabs(kap) >= M.kmin)) continue;
-            real om = M.g[Ln.ix(j, Ln.tau)];
+            real om = M.g[Ln.ix(j, step)];
             Pm += kap * om;
             Qs += kap * clampr<real>(om, 0, 1);
             nu += 1;
         }
         bool valid = nu > 0 && !(fabs(Pm) < real(1e-6));
-        real Q = M.r[Ln.ix(m, Ln.tau)] + Qs + real(0);
+        real qadj = 0;
+        int sj = d.kqs[q];
+        if (sj >= 0 && M.s_bus[sj] == m) {
+            int s1 = d.ksd[q] ? Ln.tau : Ln.tau1;
+            qadj = soc_qadj_unit(M, sj, M.e[Ln.ix(sj, step)], M.e[Ln.ix(sj, s1)]);
+        }
+        real Q = M.r[Ln.ix(m, step)] + Qs + qadj;
         Ln.S(Ln.LL.kq, q) = valid ? Q : real(0);
         Ln.S(Ln.LL.kp, q) = valid ? Pm : real(1);
         Ln.S(Ln.LL.ke, q) = valid ? Pm - fmax(Q, real(0)) : real(0);
@@ -1414,7 +1565,7 @@ __device__ __noinline__ void lane_kinks(const Lane<real> &Ln) {
         if (Ln.S(Ln.LL.kv, kq) != 0) {
             int j = d.ku[q];
             real kap = kappa_d(M, j);
-            real sigma = kap * M.g[Ln.ix(j, Ln.tau)] / Ln.S(Ln.LL.kp, kq);
+            real sigma = kap * M.g[Ln.ix(j, q < nku0 ? Ln.tau : Ln.taum)] / Ln.S(Ln.LL.kp, kq);
             if (sigma != 0) ak = sigma / kap;
         }
         Ln.S(Ln.LL.kua, q) = ak;
@@ -1530,7 +1681,8 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
         bool guard;
         real t = Ln.sample_line((real)uc, (real)uo, &guard);
         if (guard) ++guards;
-        if (fi == ESM_FAM_XLOCC && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
+        bool compensated = fi == ESM_FAM_XLOCC || fi == ESM_FAM_TPOT || fi == ESM_FAM_TSOC;
+        if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
             int nk = d.hdr[3];
             bool any = false;
             real lj = 0;

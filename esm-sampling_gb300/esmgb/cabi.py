@@ -14,7 +14,7 @@ from .model import FAMILY_RATES, SynthModel
 
 P_i32 = C.POINTER(C.c_int32)
 P_f64 = C.POINTER(C.c_double)
-NFAM = 9
+NFAM = 11
 
 
 class EsmModel(C.Structure):

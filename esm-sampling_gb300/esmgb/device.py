@@ -9,13 +9,13 @@ import os
 
 import numpy as np
 
-from .cabi import EsmOpts, ModelBuffers, make_opts
+from .cabi import NFAM, EsmOpts, ModelBuffers, make_opts
 from .model import SynthModel
 
 P_f64 = C.POINTER(C.c_double)
 P_i32 = C.POINTER(C.c_int32)
 P_i64 = C.POINTER(C.c_int64)
-NSTAT = 2 * (9 + 1) + 1
+NSTAT = 2 * (NFAM + 1) + 1
 
 # the symbols declared in include/esmcuda.h
 EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
@@ -97,13 +97,14 @@ class DeviceChain:
 
     def __init__(self, model: SynthModel, R: int, precision: int = 32, seed: int = 1, extra: float = 4.0,
                  maxnats: float = 40.0, kappa_min: float = 1.0, max_points: int = 0, span: int = 0,
-                 storage_ms: int = 0, storage_long: int = 0, probe: int = 0):
+                 storage_ms: int = 0, storage_long: int = 0, probe: int = 0, rates=None):
         self.L = load()
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
+        kw = {} if rates is None else {"rates": rates}
         self.opts: EsmOpts = make_opts(R, precision, seed, extra, maxnats, kappa_min, max_points, span,
-                                       storage_ms=storage_ms, storage_long=storage_long, probe=probe)
+                                       storage_ms=storage_ms, storage_long=storage_long, probe=probe, **kw)
         h = C.c_void_p()
         rc = self.L.esm_create(C.byref(self.buf.struct), C.byref(self.opts), C.byref(h))
         self.h = h

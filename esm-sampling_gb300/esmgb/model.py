@@ -36,9 +36,10 @@ KIND_REN, KIND_DISP, KIND_STOR = 0, 1, 2
 # v-field roles (src/local.jl:36)
 ROLE_THETA, ROLE_GEN, ROLE_SE = 1, 3, 6
 
-# the plain local families and their rates (src/local.jl:1912 plain_families)
-FAMILIES = ("unit", "pair", "xpair", "xlocc", "xloc", "potential", "cellpair", "cell", "spair")
-FAMILY_RATES = (0.3, 0.25, 0.03, 0.08, 0.04, 0.1, 0.1, 0.1, 0.3)
+# the plain local families and their rates (src/local.jl:1912 plain_families), then the compensated
+# transport families tpot and tsoc of the flow design (src/flowmoves.jl:333), off in the plain sweep
+FAMILIES = ("unit", "pair", "xpair", "xlocc", "xloc", "potential", "cellpair", "cell", "spair", "tpot", "tsoc")
+FAMILY_RATES = (0.3, 0.25, 0.03, 0.08, 0.04, 0.1, 0.1, 0.1, 0.3, 0.0, 0.0)
 
 # Langevin offsets kappa_s per carrier (src/replicas.jl:522 LANGEVIN_KAPPA)
 LANGEVIN_KAPPA = {"onwind": 500.0, "solar": 1000.0, "offwind": 200.0, "gas": 300.0, "OCGT": 300.0,

@@ -45,9 +45,14 @@ enum {
 enum { ESM_UNIT_REN = 0, ESM_UNIT_DISP = 1, ESM_UNIT_STOR = 2 };
 /* v-field roles (src/local.jl:36) */
 enum { ESM_ROLE_THETA = 1, ESM_ROLE_GEN = 3, ESM_ROLE_SE = 6 };
-/* the plain local families (src/local.jl:1912 plain_families), in this order */
+/* the plain local families (src/local.jl:1912 plain_families), in this order, then the two
+   compensated transport families of the flow design that need no flow basis (flow_families,
+   src/flowmoves.jl:333, rate 0.1 each there; 0 in the plain sweep): TPOT (prep_tpot!,
+   src/local.jl:1741, one node angle with the dispatch at the ends of its lines following pro
+   rata) and TSOC (prep_tsoc!, :1849, one unit's state of charge with the dispatch at its node
+   following pro rata at tau - 1 and tau) */
 enum { ESM_FAM_UNIT = 0, ESM_FAM_PAIR, ESM_FAM_XPAIR, ESM_FAM_XLOCC, ESM_FAM_XLOC, ESM_FAM_POTENTIAL,
-       ESM_FAM_CELLPAIR, ESM_FAM_CELL, ESM_FAM_SPAIR, ESM_NFAM };
+       ESM_FAM_CELLPAIR, ESM_FAM_CELL, ESM_FAM_SPAIR, ESM_FAM_TPOT, ESM_FAM_TSOC, ESM_NFAM };
 
 /*
  * Static model: network, units, prices, weather prior and the move tables.

@@ -752,7 +752,10 @@ static bool prorata(const Ctx &c, WS &w, int rep, int mnode, double g, vector<Ki
     return true;
 }
 
-// prep_random!, prep_xloc!, prep_spair! (src/local.jl:1608, :1672, :1708)
+static double soc_qadj(const Ctx &c, const vector<int> &us, int mnode, int tau, int rep);
+
+// prep_random!, prep_xloc!, prep_spair!, prep_tpot!, prep_tsoc! (src/local.jl:1608, :1672, :1708,
+// :1741, :1849)
 static bool prep_family(const Ctx &c, TileStream &ts, int fam, WS &ws, WS &wa, int rep, vector<Kink> *jac) {
     const Model &m = c.m;
     int N = m.N;
@@ -875,6 +878,43 @@ static bool prep_family(const Ctx &c, TileStream &ts, int fam, WS &ws, WS &wa, i
             ws.add_entry(EK_GEN, u2, -ks / k2);
             return true;
         }
+        case ESM_FAM_TPOT: {  // prep_tpot! (src/local.jl:1741): the angle of node n rises by t
+            int n = ts.pick(N);
+            if (m.theta_nnz[n] == 0) return false;
+            jac->clear();
+            ws.add_entry(EK_THETA, n, 1.0);
+            // requirement change per unit t: r[a] += f_e, r[b] -= f_e for each line a -> b of n
+            vector<double> g(N, 0.0);
+            vector<int> gn;
+            for (int p = m.nlp[n]; p < m.nlp[n + 1]; ++p) {
+                int e = m.nl[p], a = m.bus0[e], b = m.bus1[e];
+                double df = m.lb[e] * (double)((a == n) - (b == n));
+                g[a] += df;
+                g[b] -= df;
+                gn.push_back(a);
+                gn.push_back(b);
+            }
+            std::sort(gn.begin(), gn.end());
+            gn.erase(std::unique(gn.begin(), gn.end()), gn.end());
+            for (int mm : gn)
+                if (g[mm] != 0.0) prorata(c, ws, rep, mm, g[mm], jac);
+            return true;
+        }
+        case ESM_FAM_TSOC: {  // prep_tsoc! (src/local.jl:1849): energy moved from step tau-1 to tau
+            int n = ts.pick(N);
+            int ns = m.sp[n + 1] - m.sp[n];
+            if (ns == 0) return false;
+            int sj = m.sa[m.sp[n] + ts.pick(ns)];
+            int su = m.stor[sj];
+            double ks = kcl(c, su) * m.uhours[su] / m.dt;
+            if (ks < kmin) return false;
+            jac->clear();
+            ws.add_entry(EK_SE, sj, 1.0);
+            vector<int> us{sj};
+            prorata(c, wa, rep, n, ks, jac, soc_qadj(c, us, n, wa.tau, rep));
+            prorata(c, ws, rep, n, -ks, jac, soc_qadj(c, us, n, ws.tau, rep));
+            return true;
+        }
     }
     return false;
 }
@@ -917,7 +957,8 @@ static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int t
         bool guard = false;
         double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
         if (guard) stats[2 * (ESM_NFAM + 1)] += 1;
-        if (mr.kind == ESM_FAM_XLOCC && t != 0.0 && !jac.empty()) {
+        bool compensated = mr.kind == ESM_FAM_XLOCC || mr.kind == ESM_FAM_TPOT || mr.kind == ESM_FAM_TSOC;
+        if (compensated && t != 0.0 && !jac.empty()) {
             double lj = 0.0;  // logjac (src/local.jl:1871)
             for (auto &k : jac) lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
             if (uj >= exp(std::min(0.0, lj))) t = 0.0;

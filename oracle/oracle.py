@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "_build", "liboracle_esm.so")
 P_f64 = C.POINTER(C.c_double)
 P_i32 = C.POINTER(C.c_int32)
 P_i64 = C.POINTER(C.c_int64)
-NSTAT = 2 * (9 + 1) + 1
+NSTAT = 2 * (11 + 1) + 1  # ESM_NFAM = 11
 
 
 def build():
@@ -102,15 +102,16 @@ class Oracle:
     """FP64 CPU restatement of the replica hot path for one chain of R replicas."""
 
     def __init__(self, model, R, seed=1, extra=4.0, maxnats=40.0, kappa_min=1.0, max_points=0, span=0,
-                 threads=None, storage_ms=0, storage_long=0):
+                 threads=None, storage_ms=0, storage_long=0, rates=None):
         import sys
         sys.path.insert(0, os.path.join(os.path.dirname(HERE), "esm-sampling_gb300"))
         from esmgb.cabi import ModelBuffers, make_opts
         self.m = model
         self.R = R
         self.buf = ModelBuffers(model)
+        kw = {} if rates is None else {"rates": rates}
         self.opts = make_opts(R, 64, seed, extra, maxnats, kappa_min, max_points, span, storage_ms=storage_ms,
-                              storage_long=storage_long)
+                              storage_long=storage_long, **kw)
         self.threads = threads or os.cpu_count() or 1
         self.h = lib().orc_create(C.byref(self.buf.struct), C.byref(self.opts))
 

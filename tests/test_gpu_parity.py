@@ -94,7 +94,7 @@ def test_class_pass_fp64(base):
     o.rebuild()
     sd = d.class_pass(3, 0)
     so = o.class_pass(3, 0)
-    assert np.array_equal(sd[:20:2], so[:20:2])           # the same moves were tried
+    assert np.array_equal(sd[:-1:2], so[:-1:2])           # the same moves were tried
     assert sd[-1] == so[-1] == 0                          # no guard events
     frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
     print(f"FP64 class pass: flipped tasks {frac:.4f}, worst other {worst:.2e}")
@@ -116,7 +116,7 @@ def test_class_pass_fp64_grids(base, wpb, wps):
     o.rebuild()
     sd = d.class_pass(3, 0)
     so = o.class_pass(3, 0)
-    assert np.array_equal(sd[:20:2], so[:20:2])
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
     assert sd[-1] == so[-1] == 0
     frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
     assert frac <= 0.02
@@ -157,7 +157,7 @@ def test_moves_fp32(equilibrated, limit):
     o.rebuild()
     sd = d.class_pass(3, 1, limit)
     so = o.class_pass(3, 1, limit)
-    assert np.array_equal(sd[:20:2], so[:20:2])
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
     frac, worst = task_flips(d.download(), o.get_state(), m, 2e-3, 4e-3)
     print(f"FP32 first {limit} moves: flipped tasks {frac:.4f}, worst other {worst:.2e}")
     assert frac <= 0.02
@@ -190,7 +190,7 @@ def test_sweeps_fp64_odd_T_small_R():
     o.set_state(st)
     sd = d.sweeps(1, 10)
     so = o.sweeps(1, 10)
-    assert np.array_equal(sd[:20:2], so[:20:2])
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
     frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
     print(f"odd T: flipped {frac:.4f}, worst {worst:.2e}")
     assert frac <= 0.03
@@ -220,7 +220,7 @@ def test_class_pass_large_model_global_scratch():
         o.set_state(st)
         sd = d.class_pass(3, 0, limit)
         so = o.class_pass(3, 0, limit)
-        assert np.array_equal(sd[:20:2], so[:20:2])
+        assert np.array_equal(sd[:-1:2], so[:-1:2])
         assert sd[-1] == so[-1] == 0                      # no guard events
         frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
         print(f"128 nodes, FP64, first {limit or 'all'} moves: flipped tasks {frac:.4f}, worst other {worst:.2e}")

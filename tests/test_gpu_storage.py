@@ -83,7 +83,7 @@ def test_operation_sweeps_with_storage(state):
     o.set_state(st)
     assert any(bool(o.storage_ms_plan(s, force=False)) for s in range(3))
     sd, so = d.sweeps(3, 0), o.sweeps(3, 0)
-    assert np.array_equal(sd[:20:2], so[:20:2])
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
     frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
     print(f"3 operation sweeps with storage: entries differing {frac:.4f}, worst other {worst:.2e}")
     assert worst <= 1e-8 and frac <= 0.5

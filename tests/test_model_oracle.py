@@ -57,7 +57,7 @@ def test_sweep_caches_equal_rebuild_and_determinism(small):
     o.set_state(st)
     stats = o.sweeps(2, 0)
     assert stats[-1] == 0                       # no guard events
-    assert stats[:20:2].sum() > 0
+    assert stats[:-1:2].sum() > 0
     r1, F1 = o.caches()
     o.rebuild()
     r2, F2 = o.caches()
@@ -108,3 +108,125 @@ def _with_k(base, k):
         setattr(s, key, v)
     s.k = k
     return s
+
+
+def _rates(**on):
+    from esmgb.model import FAMILIES
+    return tuple(float(on.get(f, 0.0)) for f in FAMILIES)
+
+
+def _deficit_state(st):
+    """Low renewables (weather anomaly -3) and every dispatchable unit at half output: the nodes'
+    requirement is positive and the dispatch can follow it inside the box."""
+    import copy
+    s = copy.deepcopy(st)
+    s.z[:] = -3.0
+    s.g[:] = 0.5
+    return s
+
+
+def _first_move_of(o, fam, cls=0):
+    """A sweep whose class-`cls` move list starts with a draw of family `fam`."""
+    for sw in range(400):
+        k, _, _ = o.move_list(sw, cls, 0)
+        if k[0] == fam:
+            return sw
+    raise AssertionError("no such sweep")
+
+
+@pytest.mark.parametrize("fam", ["tpot", "tsoc"])
+def test_transport_families_caches_and_counts(small, fam):
+    """Sweeps of the compensated transport families only (with the atoms): moves are tried and
+    taken, the Jacobian test rejects some, and the caches still equal a rebuild."""
+    from esmgb.model import FAMILIES
+    m, st = small
+    o = Oracle(m, 4, seed=5, rates=_rates(**{fam: 1.0}))
+    o.set_state(st)
+    stats = o.sweeps(2, 0)
+    f = FAMILIES.index(fam)
+    assert stats[2 * f] > 0 and stats[2 * f + 1] > 0
+    assert stats[:2 * f:2].sum() == 0           # no other family was drawn
+    assert stats[-1] == 0
+    r1, F1 = o.caches()
+    o.rebuild()
+    r2, F2 = o.caches()
+    assert np.abs(r1 - r2).max() < 1e-8 * (1 + np.abs(r2).max())
+    assert np.abs(F1 - F2).max() < 1e-8 * (1 + np.abs(F2).max())
+
+
+def test_tpot_compensation_keeps_the_residuals(small):
+    """prep_tpot! (src/local.jl:1741): the angle of node n rises by t, the flows of its lines change
+    by b (+-t) and the dispatch at every end node follows the requirement change g t pro rata, so a
+    node's residual changes by at most |g t| (a unit or the node leaving the box) and by nothing
+    where the compensation stays inside; with the opposite sign it would change by 2 g t."""
+    from esmgb.model import FAMILIES
+    m, st = small
+    o = Oracle(m, 4, seed=5, rates=_rates(tpot=1.0))
+    sw = _first_move_of(o, FAMILIES.index("tpot"))
+    o.set_state(_deficit_state(st))
+    o.rebuild()
+    r0, _ = o.caches()
+    s0 = o.get_state()
+    o.class_pass(sw, 0, limit=1)
+    r1, _ = o.caches()
+    dth = o.get_state()["theta"] - s0["theta"]
+    nodes = np.unique(np.nonzero(dth)[0])
+    assert len(nodes) == 1                      # one node for every task of the class
+    n = int(nodes[0])
+    g = np.zeros(m.N)
+    for e in range(m.L):
+        a, b = int(m.bus0[e]), int(m.bus1[e])
+        if n in (a, b):
+            df = m.line_b[e] * ((a == n) - (b == n))
+            g[a] += df
+            g[b] -= df
+    ends = np.flatnonzero(g != 0)
+    moved = np.argwhere(dth[n] != 0)            # (step, replica) of the moved tasks
+    assert len(moved) > 0
+    exact = 0
+    for tau, rep in moved:
+        t = dth[n, tau, rep]
+        dr = r1[:, tau, rep] - r0[:, tau, rep]
+        scale = np.abs(g * t).max()
+        assert (np.abs(dr[ends]) <= np.abs(g[ends] * t) * (1 + 1e-9) + 1e-9 * scale).all()
+        others = np.setdiff1d(np.arange(m.N), ends)
+        assert np.abs(dr[others]).max(initial=0) <= 1e-9 * scale
+        exact += np.abs(dr).max() <= 1e-9 * scale
+    print(f"tpot node {n}: {len(moved)} moved tasks, residuals unchanged in {exact}")
+    assert exact >= 0.2 * len(moved)            # measured 27 of 80
+
+
+def test_tsoc_compensation_direction(small):
+    """prep_tsoc! (src/local.jl:1849): the state of charge of one unit at tau rises by t; the
+    dispatch at its node follows +kappa_s t at tau - 1 and -kappa_s t at tau (with soc_qadj), so
+    the node's residuals change only by the efficiency bend of the storage power (a fraction
+    |1/eta_in - 1| or |eta_out - 1| of kappa_s t), not by the whole kappa_s t (or twice it with the
+    opposite sign)."""
+    from esmgb.model import FAMILIES
+    m, st = small
+    o = Oracle(m, 4, seed=5, rates=_rates(tsoc=1.0))
+    sw = _first_move_of(o, FAMILIES.index("tsoc"))
+    o.set_state(_deficit_state(st))
+    o.rebuild()
+    r0, _ = o.caches()
+    s0 = o.get_state()
+    o.class_pass(sw, 0, limit=1)
+    r1, _ = o.caches()
+    de = o.get_state()["e"] - s0["e"]
+    units = np.unique(np.nonzero(de)[0])
+    assert len(units) == 1
+    sj = int(units[0])
+    u = int(m.stor[sj])
+    n = int(m.unit_bus[u])
+    kc = np.clip(s0["k"][u], m.unit_lo[u], m.unit_hi[u])
+    ks = kc * m.unit_hours[u] / m.dt
+    moved = np.argwhere(de[sj] != 0)
+    assert len(moved) > 0
+    ratios = []
+    for tau, rep in moved:
+        t = de[sj, tau, rep]
+        taum = (tau - 1) % m.T
+        ratios.append(max(abs(r1[n, tau, rep] - r0[n, tau, rep]), abs(r1[n, taum, rep] - r0[n, taum, rep])) /
+                      (ks * abs(t)))
+    print(f"tsoc unit {sj} at node {n}: {len(moved)} moved tasks, median residual ratio {np.median(ratios):.3f}")
+    assert np.median(ratios) < 0.6
