@@ -137,7 +137,8 @@ def _first_move_of(o, fam, cls=0):
 @pytest.mark.parametrize("fam", ["tpot", "tsoc"])
 def test_transport_families_caches_and_counts(small, fam):
     """Sweeps of the compensated transport families only (with the atoms): moves are tried and
-    taken, the Jacobian test rejects some, and the caches still equal a rebuild."""
+    taken (the Jacobian test, with its small log-Jacobians, rejects few) and the caches still equal
+    a rebuild."""
     from esmgb.model import FAMILIES
     m, st = small
     o = Oracle(m, 4, seed=5, rates=_rates(**{fam: 1.0}))
