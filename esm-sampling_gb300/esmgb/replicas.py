@@ -210,13 +210,21 @@ def probe_candidate(R: ReplicaSet, ctl: ReplicaCtl):
     return max(cand, key=lambda j: (R.since[j], -j))
 
 
-def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, sweep0: int = 0):
-    """``src/replicas.jl:733`` lag_probe: the device runs ``probe_len`` operation sweeps of a frozen
-    copy of replica j (esm_lag_probe; the chain is unchanged) and returns the mean capacity score of
-    the last ``probe_tail``; the gap of the in-flight scores (the mean of ``hist``, replica j's
-    records of r s, r = beta_k / beta_v, as record_hist keeps them) against it is formed on the
-    interior nodes, per k field: gap = (<r s_in> - <r s_eq>) / <fk>."""
-    sk_eq, fk = dev.lag_probe(j, ctl.probe_len, ctl.probe_tail, sweep0)
+def probe_sweep0(it: int, ctl: ReplicaCtl) -> int:
+    """The first sweep index of the probe at step ``it``: every probe draws from its own sweep
+    indices of the probe streams (the reference's probe stream ``prngs[c]`` advances from probe to
+    probe, src/replicas.jl:923)."""
+    return it * ctl.probe_len
+
+
+def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, it: int):
+    """``src/replicas.jl:733`` lag_probe at step ``it``: the device runs ``probe_len`` operation
+    sweeps of a frozen copy of replica j (esm_lag_probe, sweep indices from probe_sweep0; the chain
+    is unchanged) and returns the mean capacity score of the last ``probe_tail``; the gap of the
+    in-flight scores (the mean of ``hist``, replica j's records of r s, r = beta_k / beta_v, as
+    record_hist keeps them) against it is formed on the interior nodes, per k field:
+    gap = (<r s_in> - <r s_eq>) / <fk>."""
+    sk_eq, fk = dev.lag_probe(j, ctl.probe_len, ctl.probe_tail, probe_sweep0(it, ctl))
     inflight = np.mean(np.asarray(hist, float), axis=0)
     mask = interior_nodes(k, hi)
     rs_eq, rs_in, fkm = masked_mean(ratio * sk_eq, mask), masked_mean(inflight, mask), masked_mean(fk, mask)

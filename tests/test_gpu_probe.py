@@ -97,7 +97,7 @@ def test_probe_gap_and_errors(state):
     ratio = m.beta_k / m.beta_v
     hist = [ratio * sk[J], ratio * sk[J]]
     k = d.download_k()
-    pr = RP.lag_probe(d, J, hist, ctl, ratio, k, m.unit_hi, SW0)
+    pr = RP.lag_probe(d, J, hist, ctl, ratio, k, m.unit_hi, it=20)
     assert np.isfinite(pr["gap"][0])
     bare = DeviceChain(m, 32, precision=32, seed=5)
     bare.upload(st)

@@ -91,7 +91,7 @@ def test_probe_candidate_hist_and_gap():
 
     class FakeDev:
         def lag_probe(self, j, n, tail, sweep0):
-            assert (j, n, tail, sweep0) == (3, 5, 2, 40)
+            assert (j, n, tail, sweep0) == (3, 5, 2, 40 * 5)
             return np.array([1.0, 2.0, 4.0]), np.array([0.5, 0.5, 9.0])
 
     k = np.array([100.0, 200.0, 10.0])                # the third unit is below 50 MW: not interior
