@@ -27,3 +27,20 @@ def test_library_exports_all_symbols():
     lib = ctypes.CDLL(path)
     for name in declared_symbols():
         assert hasattr(lib, name), name
+
+
+def test_header_constants_match_the_binding():
+    """The family enum (order and count), the probe seed and the stat layout of the header agree
+    with the Python side."""
+    from esmgb import cabi
+    from esmgb.model import FAMILIES, FAMILY_RATES
+    src = open(os.path.join(ROOT, "include", "esmcuda.h")).read()
+    enum = re.search(r"enum \{ (ESM_FAM_UNIT = 0,[^}]*)\}", src).group(1)
+    names = [x.strip().split("=")[0].strip() for x in enum.split(",") if x.strip()]
+    assert names[-1] == "ESM_NFAM"
+    assert [n[len("ESM_FAM_"):].lower() for n in names[:-1]] == list(FAMILIES)
+    assert cabi.NFAM == len(FAMILIES) == len(FAMILY_RATES)
+    from oracle import oracle as O
+    assert DV.NSTAT == O.NSTAT == 2 * (cabi.NFAM + 1) + 1
+    xor = int(re.search(r"esm_probe_seed\(uint64_t seed\) \{ return seed \^ (0x[0-9A-Fa-f]+)ull; \}", src).group(1), 16)
+    assert cabi.probe_seed(12345) == 12345 ^ xor
