@@ -229,3 +229,31 @@ def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, it: int):
     mask = interior_nodes(k, hi)
     rs_eq, rs_in, fkm = masked_mean(ratio * sk_eq, mask), masked_mean(inflight, mask), masked_mean(fk, mask)
     return {"gap": [(rs_in - rs_eq) / fkm], "rs_eq": [rs_eq], "rs_in": [rs_in], "fk": [fkm]}
+
+
+def init_replicas(dev, s0, ctl: ReplicaCtl, nsweeps: int, rng, it: int = 0, sweep0: int = 0) -> ReplicaSet:
+    """``src/replicas.jl:785`` init_replicas on a chain `dev` (upload / weather_step / sweeps of the
+    C ABI): its R replicas start at the capacities and operation of `s0` (its first replica), each
+    with a fresh exact weather draw, the compensated initialisation of the dispatch and `nsweeps`
+    operation sweeps at fixed k.
+
+    The draw is made in two parts: the regime paths from the prior chain on the host
+    (sample_weather_batch, the recursion of sample_weather), then the anomalies from the prior given
+    those paths by the device's weather step at pCN angle pi/2 (the rotation keeps a weight of
+    cos(pi/2) ~ 6e-17 of the old innovations; replica j's normals come from its stream of step
+    `it`). The uploaded anomalies are those of s0, so the weather step's compensate_weather!
+    measures the residual change against the residual of s0, as the reference's r0. Returns the
+    chain's ReplicaSet."""
+    from .model import sample_weather_batch
+    m, R = dev.m, dev.R
+    get = (lambda k: s0[k]) if isinstance(s0, dict) else (lambda k: getattr(s0, k))
+    st = {k: np.repeat(np.asarray(get(k), float)[..., :1], R, axis=-1) for k in ("theta", "g", "e", "z")}
+    st["reg"], _ = sample_weather_batch(m, R, rng)
+    st["k"] = np.asarray(get("k"), float)
+    dev.upload(st)
+    dev.weather_step(np.ones(R, np.int32), np.full(R, math.pi / 2), np.zeros(R, np.int32), np.ones(R, np.int32),
+                     it=it)
+    if nsweeps > 0:
+        dev.sweeps(nsweeps, sweep0)
+    return ReplicaSet(M=R, eta_w=list(ctl.eta_w))
+
