@@ -110,25 +110,10 @@ def setup_chain(precision=32, storage_ms=0):
 
 
 def schedule(ctl, it, R, rng):
-    """Weather bursts of the step (weather_schedule / replica_weather!, src/replicas.jl:571-606)."""
-    from esmgb.replicas import weather_schedule, window_bounds
-    moved = np.zeros(R, np.int32)
-    theta = np.zeros(R)
-    window = np.zeros(R, np.int32)
-    wstart = np.ones(R, np.int32)
-    bursts = np.zeros(R, bool)
-    for j in range(R):
-        th, burst = weather_schedule(ctl, it, j + 1)
-        regime = (burst or ctl.burst_every == 0) and ctl.window > 0
-        win = regime and rng.random() < ctl.window_prob
-        theta[j] = th
-        bursts[j] = burst
-        if th > 0 or win:
-            moved[j] = 1
-        if win:
-            window[j] = ctl.window
-            wstart[j] = window_bounds(WORKLOAD["T"], ctl.window, rng.random())[0]
-    return moved, theta, window, wstart, bursts
+    """Weather bursts of the step (replica_schedule: weather_schedule / replica_weather!,
+    src/replicas.jl:571-606)."""
+    from esmgb.replicas import replica_schedule
+    return replica_schedule(ctl, it, R, WORKLOAD["T"], rng)
 
 
 def carrier_params(m):
@@ -153,37 +138,16 @@ def device_loop(d, m, ctl, it0, n, rng, pre):
 
 
 def e2e_loop(d, m, ctl, R_set, it0, n, rng):
-    """The host-driven replica loop (replica_step!, src/replicas.jl:676-704) through the C ABI."""
+    """The host-driven replica loop through the library's public call, replica_step (replica_step!,
+    src/replicas.jl:676-704, over the C ABI); returns the bytes copied per step each way."""
     from esmgb import replicas as RP
-    eta, ks = carrier_params(m)
+    _, ks = carrier_params(m)
     ratio = m.beta_k / m.beta_v
     h2d = d2h = 0
     for q in range(n):
-        it = it0 + q
-        moved, theta, window, wstart, bursts = schedule(ctl, it, d.R, rng)
-        for j in range(d.R):
-            if bursts[j]:
-                R_set.since[j], R_set.window[j], R_set.active[j] = 0, bool(window[j] > 0), False
-                R_set.gbuf[j].clear()
-                R_set.hist[j].clear()
-            else:
-                R_set.since[j] += 1
-        if moved.any():
-            d.weather_step(moved, theta, window, wstart, it=it)
-            h2d += moved.nbytes + theta.nbytes + window.nbytes + wstart.nbytes
-        d.sweeps(1, sweep0=it, stats=False)
-        sk, fk, parts = d.scores()
-        d2h += sk.nbytes + fk.nbytes + parts.nbytes
-        k = d.download_k() if hasattr(d, "download_k") else None
-        mask = RP.interior_nodes(k if k is not None else m.k0, m.unit_hi)
-        fkm = RP.masked_mean(fk, mask)
-        for j in range(d.R):
-            RP.update_gate(R_set, j, [RP.masked_mean(ratio * sk[j], mask) / fkm], ctl)
-            RP.record_hist(R_set, j, ratio * sk[j], ctl)
-        wts = RP.drift_weights(ctl, np.zeros(d.R), R_set.active)
-        knew, _ = d.langevin_step(wts, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
-        h2d += wts.nbytes + eta.nbytes + ks.nbytes
-        d2h += knew.nbytes
+        rec = RP.replica_step(d, R_set, ctl, it0 + q, rng, ks, ratio, m.unit_hi, m.unit_group)
+        h2d += rec["h2d"]
+        d2h += rec["d2h"]
     return h2d / n, d2h / n
 
 

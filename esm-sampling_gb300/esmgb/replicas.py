@@ -192,6 +192,14 @@ def masked_mean(v, mask):
     return float(v[mask].mean()) if mask.any() else math.nan
 
 
+def masked_means(v, mask, groups, nfields):
+    """``src/replicas.jl:477`` masked_means: per k field (a capacity group of the flat unit vector,
+    ``groups`` [K]) the mean of v over its masked units, NaN where none."""
+    v = np.asarray(v)
+    groups = np.asarray(groups)
+    return [masked_mean(v, mask & (groups == f)) for f in range(nfields)]
+
+
 def record_hist(R: ReplicaSet, j: int, rs, ctl: ReplicaCtl):
     """``src/replicas.jl:690-693``: an active replica's score record r s joins its in-flight window
     of the last ``probe_win`` records."""
@@ -217,18 +225,24 @@ def probe_sweep0(it: int, ctl: ReplicaCtl) -> int:
     return it * ctl.probe_len
 
 
-def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, it: int):
+def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, it: int, groups=None, nfields=1):
     """``src/replicas.jl:733`` lag_probe at step ``it``: the device runs ``probe_len`` operation
     sweeps of a frozen copy of replica j (esm_lag_probe, sweep indices from probe_sweep0; the chain
     is unchanged) and returns the mean capacity score of the last ``probe_tail``; the gap of the
     in-flight scores (the mean of ``hist``, replica j's records of r s, r = beta_k / beta_v, as
-    record_hist keeps them) against it is formed on the interior nodes, per k field:
+    record_hist keeps them) against it is formed on the interior nodes, per k field (the capacity
+    groups ``groups`` of the units; one field over all units without them):
     gap = (<r s_in> - <r s_eq>) / <fk>."""
     sk_eq, fk = dev.lag_probe(j, ctl.probe_len, ctl.probe_tail, probe_sweep0(it, ctl))
     inflight = np.mean(np.asarray(hist, float), axis=0)
     mask = interior_nodes(k, hi)
-    rs_eq, rs_in, fkm = masked_mean(ratio * sk_eq, mask), masked_mean(inflight, mask), masked_mean(fk, mask)
-    return {"gap": [(rs_in - rs_eq) / fkm], "rs_eq": [rs_eq], "rs_in": [rs_in], "fk": [fkm]}
+    if groups is None:
+        groups, nfields = np.zeros(len(mask), int), 1
+    rs_eq = masked_means(ratio * sk_eq, mask, groups, nfields)
+    rs_in = masked_means(inflight, mask, groups, nfields)
+    fkm = masked_means(fk, mask, groups, nfields)
+    gap = [(a - b) / c for a, b, c in zip(rs_in, rs_eq, fkm)]
+    return {"gap": gap, "rs_eq": rs_eq, "rs_in": rs_in, "fk": fkm}
 
 
 def init_replicas(dev, s0, ctl: ReplicaCtl, nsweeps: int, rng, it: int = 0, sweep0: int = 0) -> ReplicaSet:
@@ -256,4 +270,73 @@ def init_replicas(dev, s0, ctl: ReplicaCtl, nsweeps: int, rng, it: int = 0, swee
     if nsweeps > 0:
         dev.sweeps(nsweeps, sweep0)
     return ReplicaSet(M=R, eta_w=list(ctl.eta_w))
+
+
+def replica_schedule(ctl: ReplicaCtl, it: int, M: int, T: int, rng):
+    """The weather draws of every replica at step ``it`` (replica_weather!, src/replicas.jl:586-606:
+    weather_schedule, the window coin and its start): (moved, angle, window, window start (1-based),
+    burst) per replica, as the arrays esm_weather_step takes."""
+    moved = np.zeros(M, np.int32)
+    theta = np.zeros(M)
+    window = np.zeros(M, np.int32)
+    wstart = np.ones(M, np.int32)
+    bursts = np.zeros(M, bool)
+    for j in range(M):
+        th, burst = weather_schedule(ctl, it, j + 1)
+        regime = (burst or ctl.burst_every == 0) and ctl.window > 0
+        win = regime and rng.random() < ctl.window_prob
+        theta[j] = th
+        bursts[j] = burst
+        if th > 0 or win:
+            moved[j] = 1
+        if win:
+            window[j] = ctl.window
+            wstart[j] = window_bounds(T, ctl.window, rng.random())[0]
+    return moved, theta, window, wstart, bursts
+
+
+def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, ratio: float, hi, groups,
+                 Phis=None):
+    """``src/replicas.jl:676`` replica_step! for the chain `dev` (the C ABI's calls): the weather
+    step of the replicas the schedule moves (with the gate reset at a burst), ``ctl.inner``
+    operation sweeps (sweep indices it·inner …), the capacity scores, per replica its gate and
+    in-flight record, the drift weights and one Langevin step of the shared capacities with
+    dispatch following (step ``R.eta_w`` per k field, offsets ``kappa_s`` per field). ``ratio`` is
+    beta_k / beta_v, ``hi`` the capacity box, ``groups`` the k field of each unit. Returns the
+    step's record: moved, scores, prior terms, weights, the capacities before and after, the clip
+    count, the masked field means of r s-bar and fk, and the bytes copied each way."""
+    M = dev.R
+    nf = len(R.eta_w)
+    moved, theta, window, wstart, bursts = replica_schedule(ctl, it, M, dev.m.T, rng)
+    h2d = d2h = 0
+    for j in range(M):
+        if bursts[j]:
+            R.since[j], R.window[j], R.active[j] = 0, bool(window[j] > 0), False
+            R.gbuf[j].clear()
+            R.hist[j].clear()
+        else:
+            R.since[j] += 1
+    if moved.any():
+        dev.weather_step(moved, theta, window, wstart, it=it)
+        h2d += moved.nbytes + theta.nbytes + window.nbytes + wstart.nbytes
+    dev.sweeps(ctl.inner, it * ctl.inner, stats=False)
+    sk, fk, parts = dev.scores()
+    kraw = dev.download_k()
+    d2h += sk.nbytes + fk.nbytes + parts.nbytes + kraw.nbytes
+    mask = interior_nodes(kraw, hi)
+    fkm = masked_means(fk, mask, groups, nf)
+    for j in range(M):
+        rs = masked_means(ratio * sk[j], mask, groups, nf)
+        update_gate(R, j, [a / b for a, b in zip(rs, fkm)], ctl)
+        record_hist(R, j, ratio * sk[j], ctl)
+    wts = drift_weights(ctl, np.zeros(M) if Phis is None else Phis, R.active)
+    eta = np.asarray(R.eta_w, float)
+    ks = np.asarray(kappa_s, float)
+    knew, nclip = dev.langevin_step(wts, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
+    h2d += wts.nbytes + eta.nbytes + ks.nbytes
+    d2h += knew.nbytes
+    sbar = np.asarray(wts) @ sk
+    return {"it": it, "moved": moved.astype(bool), "sk": sk, "fk": fk, "parts": parts, "wts": wts, "kraw": kraw,
+            "knew": knew, "nclip": nclip, "rs": masked_means(ratio * sbar, mask, groups, nf), "fkm": fkm,
+            "h2d": h2d, "d2h": d2h}
 
