@@ -192,6 +192,11 @@ def masked_mean(v, mask):
     return float(v[mask].mean()) if mask.any() else math.nan
 
 
+def _div(a, b):
+    """a / b with the IEEE result where b is 0 (the reference's Float64 division), not an error."""
+    return float(np.float64(a) / np.float64(b)) if b != 0 else (math.nan if a == 0 or a != a else math.copysign(math.inf, a))
+
+
 def masked_means(v, mask, groups, nfields):
     """``src/replicas.jl:477`` masked_means: per k field (a capacity group of the flat unit vector,
     ``groups`` [K]) the mean of v over its masked units, NaN where none."""
@@ -241,7 +246,7 @@ def lag_probe(dev, j: int, hist, ctl: ReplicaCtl, ratio: float, k, hi, it: int, 
     rs_eq = masked_means(ratio * sk_eq, mask, groups, nfields)
     rs_in = masked_means(inflight, mask, groups, nfields)
     fkm = masked_means(fk, mask, groups, nfields)
-    gap = [(a - b) / c for a, b, c in zip(rs_in, rs_eq, fkm)]
+    gap = [_div(a - b, c) for a, b, c in zip(rs_in, rs_eq, fkm)]
     return {"gap": gap, "rs_eq": rs_eq, "rs_in": rs_in, "fk": fkm}
 
 
@@ -327,7 +332,7 @@ def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, rat
     fkm = masked_means(fk, mask, groups, nf)
     for j in range(M):
         rs = masked_means(ratio * sk[j], mask, groups, nf)
-        update_gate(R, j, [a / b for a, b in zip(rs, fkm)], ctl)
+        update_gate(R, j, [_div(a, b) for a, b in zip(rs, fkm)], ctl)
         record_hist(R, j, ratio * sk[j], ctl)
     wts = drift_weights(ctl, np.zeros(M) if Phis is None else Phis, R.active)
     eta = np.asarray(R.eta_w, float)
