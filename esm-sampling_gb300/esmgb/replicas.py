@@ -345,3 +345,52 @@ def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, rat
             "knew": knew, "nclip": nclip, "rs": masked_means(ratio * sbar, mask, groups, nf), "fkm": fkm,
             "h2d": h2d, "d2h": d2h}
 
+
+LANGEVIN_ETA = 5e-4   # the initial Langevin step of every k field (langevin_eta, src/run.jl:105)
+
+
+def run_replicas(dev, s0, ctl: ReplicaCtl, nwarm: int, nprod: int, rng, *, kappa_s, ratio: float, hi, groups,
+                 seed: int, init_sweeps: int = 2, snapshot_path=None, snapshot_every: int = 0):
+    """``src/replicas.jl:841`` run_replicas for one chain on `dev` (the C ABI's calls; no
+    configuration system, logs or output files): resume from ``snapshot_path`` when it holds a
+    snapshot of this chain (read_replica_snapshot with its checks), else init_replicas from `s0`;
+    then the steps up to nwarm + nprod (replica_step); every ``probe_every`` steps the lag probe of
+    probe_candidate (the chain must be created with the probe context) with the step adaptation
+    during the warm-up (adapt_step, ``:921-926``); a snapshot every ``snapshot_every`` steps before
+    the last (boundary!). Returns (ReplicaSet, step records, probe records), the records as
+    dictionaries of per-step vectors, as the snapshot's trace and probe groups keep them."""
+    from . import snapshot as SN
+    groups = np.asarray(groups)
+    nf = int(groups.max()) + 1
+    eta_w = list(ctl.eta_w) if ctl.eta_w else [LANGEVIN_ETA] * nf
+    snap = SN.read_replica_snapshot(snapshot_path, seed=seed, shapes=dev.shapes()) if snapshot_path else None
+    if snap is not None:
+        R = ReplicaSet(M=dev.R, eta_w=eta_w)
+        SN.resume_chain(snap["sets"][0], dev, R)
+        it0, trace, probes = snap["it"], snap["sets"][0]["trace"], snap["sets"][0]["probe"]
+        restarts = snap["restarts"] + 1
+    else:
+        R = init_replicas(dev, s0, ctl, init_sweeps, rng)
+        R.eta_w = eta_w
+        it0, trace, probes, restarts = 0, {}, {}, 0
+    for it in range(it0 + 1, nwarm + nprod + 1):
+        rec = replica_step(dev, R, ctl, it, rng, kappa_s, ratio, hi, groups)
+        for key, val in (("it", [it]), ("ktot", [float(np.sum(rec["knew"][groups == f])) for f in range(nf)]),
+                         ("rs", rec["rs"]), ("fk", rec["fkm"]), ("active", [float(sum(R.active))]),
+                         ("nclip", [rec["nclip"]])):
+            trace.setdefault(key, []).append(np.asarray(val, float))
+        if ctl.probe_every > 0 and it % ctl.probe_every == 0:
+            j = probe_candidate(R, ctl)
+            if j is not None:
+                pr = lag_probe(dev, j, R.hist[j], ctl, ratio, rec["knew"], hi, it, groups, nf)
+                eta0 = list(R.eta_w)
+                adapted = ctl.adapt and it <= nwarm and adapt_step(R, pr["gap"], ctl)
+                for key, val in (("it", [it, j]), ("gap", pr["gap"]), ("eta_before", eta0),
+                                 ("eta_after", list(R.eta_w)), ("adapted", [float(adapted)])):
+                    probes.setdefault(key, []).append(np.asarray(val, float))
+        if snapshot_path and snapshot_every > 0 and it % snapshot_every == 0 and it < nwarm + nprod:
+            SN.write_replica_snapshot(snapshot_path, [{"chain": dev, "set": R, "trace": trace, "probe": probes}],
+                                      it=it, seed=seed, phase="warmup" if it < nwarm else "production",
+                                      where=f"step {it}", restarts=restarts)
+    return R, trace, probes
+
