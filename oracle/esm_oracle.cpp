@@ -2008,6 +2008,41 @@ int orc_move_list(void *p, int64_t sweep, int cls, int tile, int *kinds, int *fi
     return (int)moves.size();
 }
 
+// One move of family `fam` at 0-based step tau of replica rep, its selection drawn from a fresh
+// stream (seed, tile 0, cls, sweep), moved by t (commit != 0) or only prepared: returns 1 if the
+// selection made a move, the log-Jacobian at t (logjac, src/local.jl:1871) in *lj and the first
+// kink's requirement and slope in kq[0], kq[1] (0 and 0 without kinks). The check of the
+// reference's reversibility test (test/test_local.jl:309-345) calls it twice.
+int orc_move_at(void *p, int fam, int tau, int rep, int cls, int64_t sweep, double t, int commit_it, double *lj,
+                double *kq) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    WS ws, wa;
+    ws.init(m);
+    wa.init(m);
+    ws.tau = tau;
+    wa.tau = (tau - 1 + m.T) % m.T;
+    vector<Kink> jac;
+    TileStream ts{c.o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
+    *lj = 0.0;
+    kq[0] = kq[1] = 0.0;
+    if (!prep_family(c, ts, fam, ws, wa, rep, &jac)) return 0;
+    finalize_ws(c, ws, rep);
+    if (ws.ent.empty()) return 0;
+    finalize_ws(c, wa, rep);
+    link_soc(m, wa, ws);
+    for (auto &k : jac) *lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
+    if (!jac.empty()) {
+        kq[0] = jac[0].Q;
+        kq[1] = jac[0].g;
+    }
+    if (commit_it) {
+        Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
+        commit(c, mv, t);
+    }
+    return 1;
+}
+
 void orc_class_order(void *p, int64_t sweep, int *order, int *ncls) {
     class_order(*(Ctx *)p, (uint32_t)sweep, order, ncls);
 }
