@@ -332,8 +332,13 @@ def _logit(p):
     return math.log(p / (1.0 - p))
 
 
-def make_model(N=40, L=60, T=1460, n_off=None, seed=1234, countries=None, init="uniform") -> SynthModel:
-    """Seeded synthetic model of the benchmark configurations (see the module docstring)."""
+def make_model(N=40, L=60, T=1460, n_off=None, seed=1234, countries=None, init="uniform",
+               dispatch=("OCGT",)) -> SynthModel:
+    """Seeded synthetic model of the benchmark configurations (see the module docstring).
+    ``dispatch`` names the dispatchable carriers, one unit of each at every node: the benchmark
+    configurations have OCGT alone; a second one (e.g. ("OCGT", "CCGT")) gives nodes with several
+    dispatchable units, where the pair and cell-pair selections and the Jacobian terms of the
+    compensated moves come into play."""
     assert 8760 % T == 0, "T must divide 8760 (src/layout.jl:37)"
     dt = 8760.0 / T
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -347,16 +352,18 @@ def make_model(N=40, L=60, T=1460, n_off=None, seed=1234, countries=None, init="
     comp = _components(N, bus0, bus1)
     off_nodes = np.sort(np.argsort(coords[:, 1], kind="stable")[:n_off]).astype(np.int32)
 
-    carriers = ["onwind", "offwind", "solar", "OCGT", "battery", "H2"]
-    capex = {"onwind": 1.10e5, "offwind": 1.90e5, "solar": 0.45e5, "OCGT": 0.47e5, "battery": 0.85e5, "H2": 1.20e5}
+    carriers = ["onwind", "offwind", "solar", *dispatch, "battery", "H2"]
+    capex = {"onwind": 1.10e5, "offwind": 1.90e5, "solar": 0.45e5, "OCGT": 0.47e5, "CCGT": 0.90e5, "battery": 0.85e5,
+             "H2": 1.20e5}
     kind, group, bus, series = [], [], [], []
-    nodes_of = {"onwind": np.arange(N), "offwind": off_nodes, "solar": np.arange(N), "OCGT": np.arange(N),
-                "battery": np.arange(N), "H2": np.arange(N)}
+    nodes_of = {"onwind": np.arange(N), "offwind": off_nodes, "solar": np.arange(N), "battery": np.arange(N),
+                "H2": np.arange(N)}
+    nodes_of.update({c: np.arange(N) for c in dispatch})
     # weather series: load (N), onwind (N), offwind (n_off), solar (N)  (src/energy.jl:307 wnames order)
     ser_base = {"onwind": N, "offwind": 2 * N, "solar": 2 * N + n_off}
     for gi, c in enumerate(carriers):
         for j, n in enumerate(nodes_of[c]):
-            kind.append(KIND_REN if c in ser_base else (KIND_DISP if c == "OCGT" else KIND_STOR))
+            kind.append(KIND_REN if c in ser_base else (KIND_DISP if c in dispatch else KIND_STOR))
             group.append(gi)
             bus.append(int(n))
             series.append(ser_base[c] + j if c in ser_base else -1)

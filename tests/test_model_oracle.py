@@ -233,8 +233,38 @@ def test_tsoc_compensation_direction(small):
     assert np.median(ratios) < 0.6
 
 
+@pytest.fixture(scope="module")
+def two_dispatch():
+    """Two dispatchable units at every node (OCGT and CCGT): the pair and cell-pair selections and
+    the Jacobian terms (|S| - 1 = 1) of the compensated moves come into play."""
+    m = make_model(12, 18, 40, seed=4, dispatch=("OCGT", "CCGT"))
+    return m, initial_state(m, 4, seed=2)
+
+
+def test_two_dispatch_model_sweeps(two_dispatch):
+    """Sweeps with every family (the plain rates and tpot, tsoc at 0.1) on the two-unit model: every
+    family is tried and moves, the Jacobian test rejects some compensated moves, and the caches
+    equal a rebuild."""
+    from esmgb.model import FAMILIES, FAMILY_RATES
+    m, st = two_dispatch
+    o = Oracle(m, 4, seed=5, rates=tuple(FAMILY_RATES[:9]) + (0.1, 0.1))
+    o.set_state(st)
+    stats = o.sweeps(2, 0)
+    tried, moved = stats[0:2 * len(FAMILIES):2], stats[1:2 * len(FAMILIES):2]
+    assert (tried > 0).all() and (moved > 0).all(), dict(zip(FAMILIES, tried))
+    comp = [FAMILIES.index(f) for f in ("xlocc", "tpot", "tsoc")]
+    assert (tried[comp] - moved[comp]).sum() > 0           # Jacobian rejections
+    assert stats[-1] == 0
+    r1, F1 = o.caches()
+    o.rebuild()
+    r2, F2 = o.caches()
+    assert np.abs(r1 - r2).max() < 1e-8 * (1 + np.abs(r2).max())
+    assert np.abs(F1 - F2).max() < 1e-8 * (1 + np.abs(F2).max())
+
+
+@pytest.mark.parametrize("model", ["one", "two"])
 @pytest.mark.parametrize("state", ["perturbed", "deficit"])
-def test_compensated_moves_are_reversible(small, state):
+def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
     """test/test_local.jl:285-345 restated for the compensated transport families (tpot, whose
     docstring, src/local.jl:1730, states the same invariance, and tsoc): a move by t, then the same
     move prepared at the new state and moved by -t, returns to the start (the shares and the
@@ -244,7 +274,7 @@ def test_compensated_moves_are_reversible(small, state):
     general: a unit moved directly and pro rata changes its own share along the line.)"""
     from esmgb.model import FAMILIES
     import copy
-    m, st = small
+    m, st = small if model == "one" else two_dispatch
     rng = np.random.Generator(np.random.PCG64(17))
     if state == "deficit":
         st = _deficit_state(st)
@@ -258,7 +288,7 @@ def test_compensated_moves_are_reversible(small, state):
     o.set_state(st)
     o.rebuild()
     fams = [FAMILIES.index(f) for f in ("tpot", "tsoc")]
-    worst = worstj = 0.0
+    worst = worstj = ljmax = 0.0
     ncross = nmoves = 0
     for trial in range(120):
         fam = fams[(trial // 2) % 2]
@@ -274,9 +304,12 @@ def test_compensated_moves_are_reversible(small, state):
         for k in ("theta", "g", "e"):
             worst = max(worst, np.abs(s1[k] - s0[k]).max() / (1 + np.abs(s0[k]).max()))
         worstj = max(worstj, abs(lj + lj2))
+        ljmax = max(ljmax, abs(lj))
         ncross += abs(t) > abs(Q / g)
         nmoves += 1
-    print(f"{state}: {nmoves} moves, {ncross} across the kink, worst {worst:.2e}, worst log-Jacobian sum {worstj:.2e}")
+    print(f"{model} {state}: {nmoves} moves, {ncross} across the kink, worst {worst:.2e}, largest |log-Jacobian| "
+          f"{ljmax:.2e}, worst sum {worstj:.2e}")
     assert nmoves > 30 and ncross > 5
+    assert (ljmax > 1e-3) == (model == "two")      # the Jacobian terms vanish with one unit per node
     assert worst < 1e-9
     assert worstj < 1e-8
