@@ -2011,10 +2011,11 @@ int orc_move_list(void *p, int64_t sweep, int cls, int tile, int *kinds, int *fi
 // One move of family `fam` at 0-based step tau of replica rep, its selection drawn from a fresh
 // stream (seed, tile 0, cls, sweep), moved by t (commit != 0) or only prepared: returns 1 if the
 // selection made a move, the log-Jacobian at t (logjac, src/local.jl:1871) in *lj and the first
-// kink's requirement and slope in kq[0], kq[1] (0 and 0 without kinks). The check of the
-// reference's reversibility test (test/test_local.jl:309-345) calls it twice.
+// kink's requirement and slope in kq[0], kq[1] (0 and 0 without kinks), and the cost change the
+// move evaluates at t (mv_eval!) in *dc. The checks of the reference's reversibility and
+// exactness tests (test/test_local.jl:285-345, test/test_moves.jl) call it.
 int orc_move_at(void *p, int fam, int tau, int rep, int cls, int64_t sweep, double t, int commit_it, double *lj,
-                double *kq) {
+                double *kq, double *dc) {
     Ctx &c = *(Ctx *)p;
     const Model &m = c.m;
     WS ws, wa;
@@ -2025,6 +2026,7 @@ int orc_move_at(void *p, int fam, int tau, int rep, int cls, int64_t sweep, doub
     vector<Kink> jac;
     TileStream ts{c.o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
     *lj = 0.0;
+    *dc = 0.0;
     kq[0] = kq[1] = 0.0;
     if (!prep_family(c, ts, fam, ws, wa, rep, &jac)) return 0;
     finalize_ws(c, ws, rep);
@@ -2036,10 +2038,9 @@ int orc_move_at(void *p, int fam, int tau, int rep, int cls, int64_t sweep, doub
         kq[0] = jac[0].Q;
         kq[1] = jac[0].g;
     }
-    if (commit_it) {
-        Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
-        commit(c, mv, t);
-    }
+    Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
+    *dc = mv.eval(t);
+    if (commit_it) commit(c, mv, t);
     return 1;
 }
 

@@ -51,7 +51,7 @@ def lib():
         L.orc_get_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
         L.orc_rebuild.argtypes = [C.c_void_p, C.c_int]
         L.orc_move_at.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_double, C.c_int,
-                                  P_f64, P_f64]
+                                  P_f64, P_f64, P_f64]
         L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
         L.orc_set_caches.argtypes = [C.c_void_p, P_f64, P_f64]
         L.orc_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, P_i64, C.c_int]
@@ -198,13 +198,16 @@ class Oracle:
         n = lib().orc_move_list(self.h, sweep, cls, tile, _p(k, P_i32), _p(f, P_i32), _p(a, P_i32), maxn)
         return k[:n], f[:n], a[:n]
 
-    def move_at(self, fam, tau, rep, cls, sweep, t, commit=True):
+    def move_at(self, fam, tau, rep, cls, sweep, t, commit=True, with_cost=False):
         """One move of family `fam` at step tau of replica rep (selection from the stream (cls,
-        sweep)), moved by t when `commit`: (made, log-Jacobian at t, (Q, g) of its first kink)."""
+        sweep)), moved by t when `commit`: (made, log-Jacobian at t, (Q, g) of its first kink)
+        and, with `with_cost`, the cost change the move evaluates at t."""
         lj = np.zeros(1)
         kq = np.zeros(2)
-        ok = lib().orc_move_at(self.h, fam, tau, rep, cls, sweep, t, int(commit), _p(lj), _p(kq))
-        return bool(ok), float(lj[0]), (float(kq[0]), float(kq[1]))
+        dc = np.zeros(1)
+        ok = lib().orc_move_at(self.h, fam, tau, rep, cls, sweep, t, int(commit), _p(lj), _p(kq), _p(dc))
+        out = (bool(ok), float(lj[0]), (float(kq[0]), float(kq[1])))
+        return out + (float(dc[0]),) if with_cost else out
 
     def class_order(self, sweep):
         o = np.zeros(3, np.int32)

@@ -313,3 +313,41 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
     assert (ljmax > 1e-3) == (model == "two")      # the Jacobian terms vanish with one unit per node
     assert worst < 1e-9
     assert worstj < 1e-8
+
+
+@pytest.mark.parametrize("model", ["one", "two"])
+def test_every_family_cost_change_is_exact(small, two_dispatch, model):
+    """test/test_moves.jl (draw consistency): the cost change a move evaluates for its t equals
+    the change of the global operational cost (energy_cost, src/energy.jl:551) after the commit,
+    for every family, at sites of random step, replica and selection, with t over five decades."""
+    import copy
+    from esmgb.model import FAMILIES
+    m, st = small if model == "one" else two_dispatch
+    rng = np.random.Generator(np.random.PCG64(23))
+    st = copy.deepcopy(st)
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    o = Oracle(m, 4, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    made = {f: 0 for f in FAMILIES}
+    worst = 0.0
+    for trial in range(330):
+        fam = trial % len(FAMILIES)
+        tau, rep = int(rng.integers(0, m.T)), int(rng.integers(0, 4))
+        t = float(rng.choice([-1.0, 1.0]) * 10.0 ** rng.uniform(-3.0, 2.5))
+        c0 = o.scores()[2][rep, 1]
+        ok, _, _, dc = o.move_at(fam, tau, rep, 2, trial, t, with_cost=True)
+        if not ok:
+            continue
+        c1 = o.scores()[2][rep, 1]
+        err = abs((c1 - c0) - dc)
+        assert err <= 1e-11 * abs(c0) + 1e-9 * abs(dc), (FAMILIES[fam], t, c1 - c0, dc)
+        worst = max(worst, err / (abs(c0) + abs(dc)))
+        made[FAMILIES[fam]] += 1
+    print(model, made, f"worst {worst:.1e}")
+    blocked = {"pair", "cellpair"} if model == "one" else set()
+    assert all(v > 0 for f, v in made.items() if f not in blocked)
+    r1, F1 = o.caches()
+    o.rebuild()
+    r2, _ = o.caches()
+    assert np.abs(r1 - r2).max() < 1e-8 * (1 + np.abs(r2).max())
