@@ -2044,6 +2044,55 @@ int orc_move_at(void *p, int fam, int tau, int rep, int cls, int64_t sweep, doub
     return 1;
 }
 
+// The walk of the same move (both directions, merged in ascending order with t = 0): points in
+// pts and potentials beta * DeltaC in cs, at most maxn; returns their number, 0 if the selection
+// made no move, -1 at the point cap. For the reference's walk-linearity check (test/test_moves.jl
+// 1a: the potential is linear between consecutive points).
+int orc_move_walk(void *p, int fam, int tau, int rep, int cls, int64_t sweep, double *pts, double *cs, int maxn) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    WS ws, wa;
+    ws.init(m);
+    wa.init(m);
+    ws.tau = tau;
+    wa.tau = (tau - 1 + m.T) % m.T;
+    vector<Kink> jac;
+    TileStream ts{c.o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
+    if (!prep_family(c, ts, fam, ws, wa, rep, &jac)) return 0;
+    finalize_ws(c, ws, rep);
+    if (ws.ent.empty()) return 0;
+    finalize_ws(c, wa, rep);
+    link_soc(m, wa, ws);
+    Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
+    vector<double> right, left;
+    for (const WS *w : mv.w)
+        for (double x : w->bps) {
+            if (!std::isfinite(x)) continue;
+            if (x > 0.0)
+                right.push_back(x);
+            else if (x < 0.0)
+                left.push_back(x);
+        }
+    mv.eval(0.0);
+    vector<double> sec0 = mv.sec;
+    Walk Wr, Wl;
+    Wr.cap = Wl.cap = c.o.max_points > 0 ? c.o.max_points : 4096;
+    if (!walk(Wr, mv, right, 1.0, c.o.maxnats, sec0) || Wr.full) return -1;
+    if (!walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) || Wl.full) return -1;
+    int n = 0;
+    auto put = [&](double x, double cx) {
+        if (n < maxn) {
+            pts[n] = x;
+            cs[n] = cx;
+        }
+        ++n;
+    };
+    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) put(Wl.pts[j], Wl.cs[j]);
+    put(0.0, 0.0);
+    for (size_t j = 0; j < Wr.pts.size(); ++j) put(Wr.pts[j], Wr.cs[j]);
+    return n;
+}
+
 void orc_class_order(void *p, int64_t sweep, int *order, int *ncls) {
     class_order(*(Ctx *)p, (uint32_t)sweep, order, ncls);
 }

@@ -50,6 +50,7 @@ def lib():
         L.orc_set_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
         L.orc_get_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
         L.orc_rebuild.argtypes = [C.c_void_p, C.c_int]
+        L.orc_move_walk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, P_f64, P_f64, C.c_int]
         L.orc_move_at.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_double, C.c_int,
                                   P_f64, P_f64, P_f64]
         L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
@@ -208,6 +209,17 @@ class Oracle:
         ok = lib().orc_move_at(self.h, fam, tau, rep, cls, sweep, t, int(commit), _p(lj), _p(kq), _p(dc))
         out = (bool(ok), float(lj[0]), (float(kq[0]), float(kq[1])))
         return out + (float(dc[0]),) if with_cost else out
+
+    def move_walk(self, fam, tau, rep, cls, sweep, maxn=8192):
+        """The walk of that move: (points, potentials beta DeltaC), ascending, with t = 0; None if
+        the selection made no move or the walk reached the point cap."""
+        pts = np.zeros(maxn)
+        cs = np.zeros(maxn)
+        n = lib().orc_move_walk(self.h, fam, tau, rep, cls, sweep, _p(pts), _p(cs), maxn)
+        if n <= 0:
+            return None
+        n = min(n, maxn)
+        return pts[:n].copy(), cs[:n].copy()
 
     def class_order(self, sweep):
         o = np.zeros(3, np.int32)

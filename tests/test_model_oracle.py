@@ -351,3 +351,40 @@ def test_every_family_cost_change_is_exact(small, two_dispatch, model):
     o.rebuild()
     r2, _ = o.caches()
     assert np.abs(r1 - r2).max() < 1e-8 * (1 + np.abs(r2).max())
+
+
+@pytest.mark.parametrize("model", ["one", "two"])
+def test_every_family_potential_is_linear_between_walk_points(small, two_dispatch, model):
+    """test/test_moves.jl 1a: between consecutive points of a move's walk the potential beta
+    DeltaC(t) is linear (checked at 1/4, 1/2, 3/4 of every segment, bound 1e-6 nats as there), so
+    the walk misses no kink or root of the line's piecewise-linear cost."""
+    import copy
+    from esmgb.model import FAMILIES
+    m, st = small if model == "one" else two_dispatch
+    rng = np.random.Generator(np.random.PCG64(29))
+    st = copy.deepcopy(st)
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    o = Oracle(m, 4, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    beta = m.beta_v
+    worst, nseg = 0.0, {f: 0 for f in FAMILIES}
+    for trial in range(110):
+        fam = trial % len(FAMILIES)
+        tau, rep = int(rng.integers(0, m.T)), int(rng.integers(0, 4))
+        w = o.move_walk(fam, tau, rep, 3, trial)
+        if w is None:
+            continue
+        pts, cs = w
+        for j in range(len(pts) - 1):
+            if not pts[j + 1] > pts[j]:
+                continue
+            nseg[FAMILIES[fam]] += 1
+            for a in (0.25, 0.5, 0.75):
+                t = pts[j] + a * (pts[j + 1] - pts[j])
+                _, _, _, dc = o.move_at(fam, tau, rep, 3, trial, t, commit=False, with_cost=True)
+                worst = max(worst, abs(beta * dc - ((1 - a) * cs[j] + a * cs[j + 1])))
+    print(model, nseg, f"worst {worst:.2e} nats")
+    blocked = {"pair", "cellpair"} if model == "one" else set()
+    assert all(v > 0 for f, v in nseg.items() if f not in blocked)
+    assert worst < 1e-6
