@@ -265,13 +265,13 @@ def test_two_dispatch_model_sweeps(two_dispatch):
 @pytest.mark.parametrize("model", ["one", "two"])
 @pytest.mark.parametrize("state", ["perturbed", "deficit"])
 def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
-    """test/test_local.jl:285-345 restated for the compensated transport families (tpot, whose
-    docstring, src/local.jl:1730, states the same invariance, and tsoc): a move by t, then the same
+    """test/test_local.jl:285-345 and test/test_moves.jl (2, reversibility) restated for every
+    family, the compensated ones (xlocc, tpot, tsoc) with their kinks: a move by t, then the same
     move prepared at the new state and moved by -t, returns to the start (the shares and the
     excess are coordinates of the curve; soc_qadj makes the requirement of tsoc's compensation
     follow the nominal storage injection), and the two log-Jacobians cancel. t is drawn as there:
-    on the scale of the first kink, or twice its distance (beyond it). (xlocc is not invariant in
-    general: a unit moved directly and pro rata changes its own share along the line.)"""
+    on the scale of the first kink, or twice its distance (beyond it); for the families without
+    kinks (or with a kink beyond 1e5) over five decades."""
     from esmgb.model import FAMILIES
     import copy
     m, st = small if model == "one" else two_dispatch
@@ -287,17 +287,22 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
     o = Oracle(m, 4, seed=5)
     o.set_state(st)
     o.rebuild()
-    fams = [FAMILIES.index(f) for f in ("tpot", "tsoc")]
+    comp = [FAMILIES.index(f) for f in ("xlocc", "tpot", "tsoc")]
     worst = worstj = ljmax = 0.0
-    ncross = nmoves = 0
-    for trial in range(120):
-        fam = fams[(trial // 2) % 2]
+    ncross = nmoves = nplain = 0
+    for trial in range(360):
+        fam = trial % len(FAMILIES)
         tau, rep = int(rng.integers(0, m.T)), int(rng.integers(0, 4))
         ok, _, (Q, g) = o.move_at(fam, tau, rep, 1, trial, 0.0, commit=False)
-        if not ok or g == 0.0:
+        if not ok:
             continue
         s0 = o.get_state()
-        t = 0.3 * rng.standard_normal() * abs(Q / g) if trial % 2 else -2.0 * Q / g
+        if fam in comp and g != 0.0 and abs(Q / g) < 1e5:   # (a leak of round-off size puts the kink far away)
+            t = 0.3 * rng.standard_normal() * abs(Q / g) if (trial // len(FAMILIES)) % 2 else -2.0 * Q / g
+        else:
+            t = float(rng.choice([-1.0, 1.0]) * 10.0 ** rng.uniform(-3.0, 2.5))
+            g, Q = 0.0, 0.0
+            nplain += 1
         _, lj, _ = o.move_at(fam, tau, rep, 1, trial, t)
         _, lj2, _ = o.move_at(fam, tau, rep, 1, trial, -t)
         s1 = o.get_state()
@@ -305,11 +310,12 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
             worst = max(worst, np.abs(s1[k] - s0[k]).max() / (1 + np.abs(s0[k]).max()))
         worstj = max(worstj, abs(lj + lj2))
         ljmax = max(ljmax, abs(lj))
-        ncross += abs(t) > abs(Q / g)
-        nmoves += 1
-    print(f"{model} {state}: {nmoves} moves, {ncross} across the kink, worst {worst:.2e}, largest |log-Jacobian| "
-          f"{ljmax:.2e}, worst sum {worstj:.2e}")
-    assert nmoves > 30 and ncross > 5
+        if g != 0.0:
+            ncross += abs(t) > abs(Q / g)
+            nmoves += 1
+    print(f"{model} {state}: {nmoves} compensated moves, {ncross} across the kink, {nplain} others, worst "
+          f"{worst:.2e}, largest |log-Jacobian| {ljmax:.2e}, worst sum {worstj:.2e}")
+    assert nmoves > 60 and ncross > 10 and nplain > 150
     assert (ljmax > 1e-3) == (model == "two")      # the Jacobian terms vanish with one unit per node
     assert worst < 1e-9
     assert worstj < 1e-8
