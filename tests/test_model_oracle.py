@@ -271,7 +271,8 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
     excess are coordinates of the curve; soc_qadj makes the requirement of tsoc's compensation
     follow the nominal storage injection), and the two log-Jacobians cancel. t is drawn as there:
     on the scale of the first kink, or twice its distance (beyond it); for the families without
-    kinks (or with a kink beyond 1e5) over five decades."""
+    kinks (or with a kink beyond 1e5) over five decades. The line density of the move prepared at
+    the moved state is the forward one shifted by t (bound 1e-6 as there)."""
     from esmgb.model import FAMILIES
     import copy
     m, st = small if model == "one" else two_dispatch
@@ -288,7 +289,7 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
     o.set_state(st)
     o.rebuild()
     comp = [FAMILIES.index(f) for f in ("xlocc", "tpot", "tsoc")]
-    worst = worstj = ljmax = 0.0
+    worst = worstj = ljmax = worstd = 0.0
     ncross = nmoves = nplain = 0
     for trial in range(360):
         fam = trial % len(FAMILIES)
@@ -303,7 +304,17 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
             t = float(rng.choice([-1.0, 1.0]) * 10.0 ** rng.uniform(-3.0, 2.5))
             g, Q = 0.0, 0.0
             nplain += 1
+        def dens(x):  # the line log-density (up to its constant) of the move prepared now, at x
+            _, ljx, _, dcx = o.move_at(fam, tau, rep, 1, trial, x, commit=False, with_cost=True)
+            return -m.beta_v * dcx + ljx, abs(m.beta_v * dcx)
+        us = (-t, -0.37 * t, 0.61 * t, 1.5 * t)
+        f0, m0 = dens(t)
+        fwd = [dens(t + u) for u in us]
         _, lj, _ = o.move_at(fam, tau, rep, 1, trial, t)
+        fr0 = dens(0.0)[0]
+        for u, (fu, mu) in zip(us, fwd):   # the reverse density is the forward one shifted
+            wdens = abs((dens(u)[0] - fr0) - (fu - f0)) / (1 + 1e-9 * (mu + m0))
+            worstd = max(worstd, wdens)
         _, lj2, _ = o.move_at(fam, tau, rep, 1, trial, -t)
         s1 = o.get_state()
         for k in ("theta", "g", "e"):
@@ -314,7 +325,8 @@ def test_compensated_moves_are_reversible(small, two_dispatch, model, state):
             ncross += abs(t) > abs(Q / g)
             nmoves += 1
     print(f"{model} {state}: {nmoves} compensated moves, {ncross} across the kink, {nplain} others, worst "
-          f"{worst:.2e}, largest |log-Jacobian| {ljmax:.2e}, worst sum {worstj:.2e}")
+          f"{worst:.2e}, largest |log-Jacobian| {ljmax:.2e}, worst sum {worstj:.2e}, reverse density {worstd:.2e}")
+    assert worstd < 1e-6
     assert nmoves > 60 and ncross > 10 and nplain > 150
     assert (ljmax > 1e-3) == (model == "two")      # the Jacobian terms vanish with one unit per node
     assert worst < 1e-9
