@@ -2093,6 +2093,73 @@ int orc_move_walk(void *p, int fam, int tau, int rep, int cls, int64_t sweep, do
     return n;
 }
 
+// One storage block move of replica rep: the plateau of the storage units us[0..nus) over the
+// instants b0+1 .. b0+L (cyclic; prep_storage_ms! / prep_slong!) or, with L = T and one unit, its
+// level move; moved by t when commit_it. Outputs as orc_move_at, and with pts/cs (maxn > 0) its
+// walk as orc_move_walk (the return is then the number of points, -1 at the point cap). For the
+// reference's storage-move checks (test/test_local.jl:227-345).
+int orc_block_at(void *p, const int *us, int nus, int b0, int L, int rep, double t, int commit_it, double *lj,
+                 double *kq, double *dc, double *pts, double *cs, int maxn) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    int T = m.T;
+    bool level = L == T;
+    int n = level ? T : L + 1;
+    vector<WS> wss(n);
+    for (auto &w : wss) w.init(m);
+    vector<Kink> jac;
+    vector<int> uv(us, us + nus);
+    *lj = 0.0;
+    *dc = 0.0;
+    kq[0] = kq[1] = 0.0;
+    if (level) {
+        if (nus != 1) return 0;
+        prep_level(c, wss, uv[0], rep);
+    } else if (!prep_plateau(c, wss, b0, L, uv, rep, &jac)) {
+        return 0;
+    }
+    Mover mv{&c, {}, rep, m.beta_v, {}};
+    mv.cyclic = level;
+    for (auto &w : wss) mv.w.push_back(&w);
+    for (auto &k : jac) *lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
+    if (!jac.empty()) {
+        kq[0] = jac[0].Q;
+        kq[1] = jac[0].g;
+    }
+    if (maxn > 0) {
+        vector<double> right, left;
+        for (const WS *w : mv.w)
+            for (double x : w->bps) {
+                if (!std::isfinite(x)) continue;
+                if (x > 0.0)
+                    right.push_back(x);
+                else if (x < 0.0)
+                    left.push_back(x);
+            }
+        mv.eval(0.0);
+        vector<double> sec0 = mv.sec;
+        Walk Wr, Wl;
+        Wr.cap = Wl.cap = c.o.max_points > 0 ? c.o.max_points : 4096;
+        if (!walk(Wr, mv, right, 1.0, c.o.maxnats, sec0) || Wr.full) return -1;
+        if (!walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) || Wl.full) return -1;
+        int k = 0;
+        auto put = [&](double x, double cx) {
+            if (k < maxn) {
+                pts[k] = x;
+                cs[k] = cx;
+            }
+            ++k;
+        };
+        for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) put(Wl.pts[j], Wl.cs[j]);
+        put(0.0, 0.0);
+        for (size_t j = 0; j < Wr.pts.size(); ++j) put(Wr.pts[j], Wr.cs[j]);
+        return k;
+    }
+    *dc = mv.eval(t);
+    if (commit_it) commit(c, mv, t);
+    return 1;
+}
+
 void orc_class_order(void *p, int64_t sweep, int *order, int *ncls) {
     class_order(*(Ctx *)p, (uint32_t)sweep, order, ncls);
 }

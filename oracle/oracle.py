@@ -51,6 +51,8 @@ def lib():
         L.orc_get_state.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64]
         L.orc_rebuild.argtypes = [C.c_void_p, C.c_int]
         L.orc_move_walk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, P_f64, P_f64, C.c_int]
+        L.orc_block_at.argtypes = [C.c_void_p, P_i32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, P_f64,
+                                   P_f64, P_f64, P_f64, P_f64, C.c_int]
         L.orc_move_at.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_double, C.c_int,
                                   P_f64, P_f64, P_f64]
         L.orc_get_caches.argtypes = [C.c_void_p, P_f64, P_f64]
@@ -216,6 +218,29 @@ class Oracle:
         pts = np.zeros(maxn)
         cs = np.zeros(maxn)
         n = lib().orc_move_walk(self.h, fam, tau, rep, cls, sweep, _p(pts), _p(cs), maxn)
+        if n <= 0:
+            return None
+        n = min(n, maxn)
+        return pts[:n].copy(), cs[:n].copy()
+
+    def block_at(self, units, b0, L, rep, t, commit=True):
+        """One storage block move of replica rep (the plateau of `units` over the instants b0+1 ..
+        b0+L, cyclic; L = T: the level move of one unit), moved by t when `commit`: (made,
+        log-Jacobian at t, (Q, g) of its first kink, the cost change it evaluates at t)."""
+        us = np.ascontiguousarray(units, dtype=np.int32)
+        lj, kq, dc = np.zeros(1), np.zeros(2), np.zeros(1)
+        ok = lib().orc_block_at(self.h, _p(us, P_i32), len(us), b0, L, rep, t, int(commit), _p(lj), _p(kq), _p(dc),
+                                None, None, 0)
+        return bool(ok), float(lj[0]), (float(kq[0]), float(kq[1])), float(dc[0])
+
+    def block_walk(self, units, b0, L, rep, maxn=8192):
+        """The walk of that block move: (points, potentials beta DeltaC), ascending, with t = 0;
+        None if there is no move or the walk reached the point cap."""
+        us = np.ascontiguousarray(units, dtype=np.int32)
+        lj, kq, dc = np.zeros(1), np.zeros(2), np.zeros(1)
+        pts, cs = np.zeros(maxn), np.zeros(maxn)
+        n = lib().orc_block_at(self.h, _p(us, P_i32), len(us), b0, L, rep, 0.0, 0, _p(lj), _p(kq), _p(dc), _p(pts),
+                               _p(cs), maxn)
         if n <= 0:
             return None
         n = min(n, maxn)

@@ -66,3 +66,86 @@ def test_long_range_plan_and_caches():
     s1 = o.get_state()
     moved = np.abs(s1["e"] - s0["e"]).max(axis=(1, 2)) > 0
     assert set(np.flatnonzero(moved)) <= set(units)  # only the long-duration units move
+
+
+def _blocks(m, rng, ntrial):
+    """Storage block moves as the sweeps draw them: multiscale plateaus of one unit or of a cell-class
+    aggregate over L in {1, 2, 8} inside the year, long-range plateaus of one long-duration unit that
+    wrap the year end, and level moves (L = T)."""
+    from esmgb.cabi import storage_groups
+    sgp, sgu = storage_groups(m)
+    longu = [j for j, u in enumerate(m.stor) if m.unit_hours[u] >= 24]
+    for trial in range(ntrial):
+        kind = trial % 4
+        if kind == 0:
+            us, L = [int(rng.integers(0, m.S))], int(rng.choice([1, 2, 8]))
+            b0 = int(rng.integers(0, m.T - L))
+        elif kind == 1:
+            g = int(rng.integers(0, len(sgp) - 1))
+            us, L = [int(x) for x in sgu[sgp[g]:sgp[g + 1]]], int(rng.choice([1, 2, 8]))
+            b0 = int(rng.integers(0, m.T - L))
+        elif kind == 2:
+            us, L = [int(rng.choice(longu))], int(rng.integers(m.T // 2, m.T - 1))
+            b0 = int(rng.integers(m.T // 2, m.T))
+        else:
+            us, L, b0 = [int(rng.choice(longu))], m.T, 0
+        yield trial, kind, us, b0, L
+
+
+def test_block_moves_exact_reversible_linear():
+    """The reference's storage-move checks (test/test_local.jl:227-345, test/test_moves.jl §1-2) on
+    the oracle's plateau, long-range and level moves: the cost change a move evaluates equals the
+    global change after the commit; the move prepared again at the moved state and moved by -t
+    returns to the start with the log-Jacobians cancelling (t on the scale of the first kink, or
+    beyond it); the potential is linear between walk points (1e-6 nats)."""
+    import copy
+    m = make_model(12, 18, 40, seed=4, dispatch=("OCGT", "CCGT"))
+    rng = np.random.Generator(np.random.PCG64(41))
+    st = initial_state(m, 4, seed=2)
+    st = copy.deepcopy(st)
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    st.e = rng.uniform(0.05, 0.95, st.e.shape)
+    o = Oracle(m, 4, seed=9)
+    o.set_state(st)
+    o.rebuild()
+    beta = m.beta_v
+    worst_c = worst_r = worst_j = worst_l = 0.0
+    counts = [0, 0, 0, 0]
+    ncross = 0
+    for trial, kind, us, b0, L in _blocks(m, rng, 160):
+        rep = int(rng.integers(0, 4))
+        ok, _, (Q, g), _ = o.block_at(us, b0, L, rep, 0.0, commit=False)
+        if not ok:
+            continue
+        counts[kind] += 1
+        # walk linearity
+        w = o.block_walk(us, b0, L, rep)
+        if w is not None:
+            pts, cs = w
+            for j in range(len(pts) - 1):
+                if pts[j + 1] > pts[j]:
+                    for a in (0.25, 0.5, 0.75):
+                        x = pts[j] + a * (pts[j + 1] - pts[j])
+                        dc = o.block_at(us, b0, L, rep, x, commit=False)[3]
+                        worst_l = max(worst_l, abs(beta * dc - ((1 - a) * cs[j] + a * cs[j + 1])))
+        # exactness and reversibility
+        if g != 0.0 and abs(Q / g) < 1e5:
+            t = 0.3 * rng.standard_normal() * abs(Q / g) if trial % 8 < 4 else -2.0 * Q / g
+            ncross += abs(t) > abs(Q / g)
+        else:
+            t = 0.02 * rng.standard_normal()
+        s0 = o.get_state()
+        c0 = o.scores()[2][rep, 1]
+        _, lj, _, dc = o.block_at(us, b0, L, rep, t)
+        c1 = o.scores()[2][rep, 1]
+        worst_c = max(worst_c, abs((c1 - c0) - dc) / (1e-12 * abs(c0) + 1e-9 * (1 + abs(dc))))
+        _, lj2, _, _ = o.block_at(us, b0, L, rep, -t)
+        s1 = o.get_state()
+        worst_r = max(worst_r, max(np.abs(s1[k] - s0[k]).max() / (1 + np.abs(s0[k]).max()) for k in ("g", "e")))
+        worst_j = max(worst_j, abs(lj + lj2))
+    print(f"block moves {counts} (plateau, aggregate, long, level), {ncross} across a kink: cost {worst_c:.2e} "
+          f"(of the bound), return {worst_r:.2e}, log-Jacobian sum {worst_j:.2e}, linearity {worst_l:.2e} nats")
+    assert min(counts) > 10 and ncross > 5
+    assert worst_c <= 1.0
+    assert worst_r < 1e-9 and worst_j < 1e-8
+    assert worst_l < 1e-6
