@@ -406,3 +406,64 @@ def test_every_family_potential_is_linear_between_walk_points(small, two_dispatc
     blocked = {"pair", "cellpair"} if model == "one" else set()
     assert all(v > 0 for f, v in nseg.items() if f not in blocked)
     assert worst < 1e-6
+
+
+def _prorata_coords(m, st, r, kmin=1.0):
+    """Shares sigma [D, T, R] and excess e [N, T, R] of the dispatchable units at every node and
+    step (prorata_coords of test/test_kop.jl); NaN where a node has no unit or |P| < 1e-6."""
+    k = st["k"]
+    g = st["g"]
+    kap = np.array([m.unit_avail[u] * np.clip(k[u], m.unit_lo[u], m.unit_hi[u]) for u in m.disp])
+    use = np.abs(kap) >= kmin
+    bus = m.unit_bus[m.disp]
+    sig = np.full(g.shape, np.nan)
+    e = np.full(r.shape, np.nan)
+    for n in range(m.N):
+        js = np.flatnonzero((bus == n) & use)
+        if len(js) == 0:
+            continue
+        p = kap[js, None, None] * g[js]
+        P = p.sum(0)
+        Q = r[n] + (kap[js, None, None] * np.clip(g[js], 0.0, 1.0)).sum(0)
+        ok = np.abs(P) >= 1e-6
+        e[n] = np.where(ok, P - np.maximum(Q, 0.0), np.nan)
+        sig[js] = np.where(ok, p / np.where(ok, P, 1.0), np.nan)
+    return sig, e
+
+
+def test_following_keeps_prorata_coordinates(two_dispatch):
+    """follow_capacities! (src/replicas.jl:448) in the oracle's Langevin step, as test/test_kop.jl
+    checks it: the dispatchable units keep their output (utilisation scaled by c(k0)/c(k1)), the
+    renewable and storage units move along their kop curves at fixed utilisation with the node's
+    dispatch following share-preservingly, so the shares and the excess of every node's
+    dispatchable units are unchanged (bounds 1e-9 and 1e-6 as there), the storage states and the
+    weather are untouched, and the capacities become the Langevin step's."""
+    import copy
+    m, st = two_dispatch
+    rng = np.random.Generator(np.random.PCG64(43))
+    st = copy.deepcopy(st)
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    o = Oracle(m, 4, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    s0 = o.get_state()
+    r0, _ = o.caches()
+    sig0, e0 = _prorata_coords(m, s0, r0)
+    o.scores()
+    G = len(m.carriers)
+    knew, _ = o.langevin_step(np.full(4, 0.25), np.full(G, 2e-3), np.full(G, 300.0), 1.0, 10.0, True,
+                              rng.standard_normal(m.Kunits), 7)
+    s1 = o.get_state()
+    r1, _ = o.caches()
+    np.testing.assert_array_equal(s1["k"], knew)
+    assert np.abs(knew - s0["k"]).max() > 1.0                  # the capacities moved
+    sig1, e1 = _prorata_coords(m, s1, r1)
+    both = ~np.isnan(sig0) & ~np.isnan(sig1)
+    esig = np.abs(sig1 - sig0)[both].max()
+    bothe = ~np.isnan(e0) & ~np.isnan(e1)
+    ee = (np.abs(e1 - e0) / (1 + np.abs(e0)))[bothe].max()
+    print(f"following: shares {esig:.2e} over {both.sum()}, excess {ee:.2e} over {bothe.sum()}")
+    assert both.mean() > 0.9 and esig < 1e-9 and ee < 1e-6
+    # the storage states and the renewable utilisations (weather) are unchanged: fixed utilisations
+    np.testing.assert_array_equal(s1["e"], s0["e"])
+    np.testing.assert_array_equal(s1["z"], s0["z"])
