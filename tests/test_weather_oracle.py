@@ -82,3 +82,53 @@ def test_regime_window_against_enumeration(tiny):
         p = pw / tot
         sd = math.sqrt(p * (1 - p) / n)
         assert abs(counts.get(path, 0) / n - p) < 5 * sd + 1e-3
+
+
+def test_compensation_follows_headroom_and_output():
+    """compensate_weather! (src/replicas.jl:207) in the oracle's weather step, on a model with two
+    dispatchable units per node: at every node and step the residual change `need` of the weather
+    move is taken up by the dispatchable units, an increase in proportion to their headroom (up to
+    it), a decrease in proportion to their output; the rest stays on the residual."""
+    import copy
+    from esmgb.model import initial_state, make_model
+    from oracle.oracle import Oracle
+    m = make_model(12, 18, 40, seed=4, dispatch=("OCGT", "CCGT"))
+    R = 3
+    st = initial_state(m, R, seed=2)
+    rng = np.random.Generator(np.random.PCG64(3))
+    st.g = np.clip(st.g + 0.1 * rng.standard_normal(st.g.shape), 0.0, 1.0)
+    o = Oracle(m, R, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    s0 = o.get_state()
+    r0, _ = o.caches()
+    o.weather_step(np.ones(R, np.int32), np.full(R, 0.6), np.zeros(R, np.int32), np.ones(R, np.int32), it=2)
+    s1 = o.get_state()
+    raw = Oracle(m, R, seed=5)
+    raw.set_state(dict(s1, g=s0["g"]))
+    raw.rebuild()
+    need_all = raw.caches()[0] - r0
+    k = s0["k"]
+    kap = np.array([m.unit_avail[u] * np.clip(k[u], m.unit_lo[u], m.unit_hi[u]) for u in m.disp])
+    bus = m.unit_bus[m.disp]
+    worst, nchk = 0.0, 0
+    for n in range(m.N):
+        js = np.flatnonzero(bus == n)
+        for t in range(m.T):
+            for rep in range(R):
+                need = need_all[n, t, rep]
+                if abs(need) < 1e-6:
+                    continue
+                p = kap[js] * np.clip(s0["g"][js, t, rep], 0.0, 1.0)
+                wq = np.maximum(kap[js] - p, 0.0) if need > 0 else p
+                tot = wq.sum()
+                dy = s1["g"][js, t, rep] - s0["g"][js, t, rep]
+                if tot <= 1e-9:
+                    assert np.abs(dy).max() == 0.0
+                    continue
+                a = min(need, tot) / tot if need > 0 else max(need, -tot) / tot
+                want = a * wq / kap[js]
+                worst = max(worst, np.abs(dy - want).max())
+                nchk += 1
+    print(f"compensation: {nchk} (node, step, replica) entries, worst {worst:.2e}")
+    assert nchk > 100 and worst < 1e-12
