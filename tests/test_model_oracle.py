@@ -467,3 +467,35 @@ def test_following_keeps_prorata_coordinates(two_dispatch):
     # the storage states and the renewable utilisations (weather) are unchanged: fixed utilisations
     np.testing.assert_array_equal(s1["e"], s0["e"])
     np.testing.assert_array_equal(s1["z"], s0["z"])
+
+
+def test_following_of_dispatchable_capacities_keeps_output(two_dispatch):
+    """test/test_replicas.jl "dispatch-following maps": when only the dispatchable capacities move
+    (the Langevin step with zero step for every other field), their output c(k) omega is kept at
+    every step (rtol 1e-9, atol 1e-6) and the residual with it (1e-6); the other capacities and the
+    storage states are untouched."""
+    import copy
+    m, st = two_dispatch
+    rng = np.random.Generator(np.random.PCG64(47))
+    st = copy.deepcopy(st)
+    st.g = st.g + 0.05 * rng.standard_normal(st.g.shape)
+    o = Oracle(m, 4, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    s0 = o.get_state()
+    r0, _ = o.caches()
+    o.scores()
+    G = len(m.carriers)
+    dispg = sorted({int(m.unit_group[u]) for u in m.disp})
+    eta = np.array([2e-3 if gi in dispg else 0.0 for gi in range(G)])
+    knew, _ = o.langevin_step(np.full(4, 0.25), eta, np.full(G, 300.0), 1.0, 10.0, True, rng.standard_normal(m.Kunits), 3)
+    s1 = o.get_state()
+    r1, _ = o.caches()
+    moved = np.abs(knew - s0["k"]) > 0
+    assert moved[m.disp].any() and not moved[np.setdiff1d(np.arange(m.Kunits), m.disp)].any()
+    for j, u in enumerate(m.disp):
+        kc0 = np.clip(s0["k"][u], m.unit_lo[u], m.unit_hi[u])
+        kc1 = np.clip(s1["k"][u], m.unit_lo[u], m.unit_hi[u])
+        np.testing.assert_allclose(kc1 * s1["g"][j], kc0 * s0["g"][j], rtol=1e-9, atol=1e-6)
+    assert np.abs(r1 - r0).max() < 1e-6
+    np.testing.assert_array_equal(s1["e"], s0["e"])
