@@ -329,11 +329,14 @@ def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, rat
     kraw = dev.download_k()
     d2h += sk.nbytes + fk.nbytes + parts.nbytes + kraw.nbytes
     mask = interior_nodes(kraw, hi)
-    fkm = masked_means(fk, mask, groups, nf)
+    groups = np.asarray(groups)
+    fmask = [mask & (groups == f) for f in range(nf)]
+    fkm = [float(fk[fm].mean()) if fm.any() else math.nan for fm in fmask]
+    rsk = ratio * sk
+    rs_all = np.stack([rsk[:, fm].mean(axis=1) if fm.any() else np.full(M, math.nan) for fm in fmask], axis=1)
     for j in range(M):
-        rs = masked_means(ratio * sk[j], mask, groups, nf)
-        update_gate(R, j, [_div(a, b) for a, b in zip(rs, fkm)], ctl)
-        record_hist(R, j, ratio * sk[j], ctl)
+        update_gate(R, j, [_div(a, b) for a, b in zip(rs_all[j].tolist(), fkm)], ctl)
+        record_hist(R, j, rsk[j], ctl)
     wts = drift_weights(ctl, np.zeros(M) if Phis is None else Phis, R.active)
     eta = np.asarray(R.eta_w, float)
     ks = np.asarray(kappa_s, float)
