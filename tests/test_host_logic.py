@@ -9,46 +9,64 @@ from esmgb import replicas as RP
 from esmgb import convergence as CV
 
 
+def _golden():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")) as f:
+        return json.load(f)
+
+
 def test_schedule_gate_weights_adaptation():
-    ctl = RP.ReplicaCtl(M=4, burst_every=8, phi=0.3, gate_min=2, gate_max=5, gate_win=4, gate_tol=0.1,
-                        eta_w=[1e-3, 1e-3], kappa_s=[100.0, 100.0], probe_avg=2)
+    """The known answers of test/test_replicas.jl:17-56 (tests/golden/known_answers.json)."""
+    G = _golden()
+    ws = G["weather_schedule"]
+    ctl = RP.ReplicaCtl(M=ws["ctl"]["M"], burst_every=ws["ctl"]["burst_every"], phi=ws["ctl"]["phi"],
+                        gate_min=G["gate"]["ctl"]["gate_min"], gate_max=5, gate_win=G["gate"]["ctl"]["gate_win"],
+                        gate_tol=G["gate"]["ctl"]["gate_tol"], eta_w=list(G["adapt_step"]["eta0"]),
+                        kappa_s=[100.0, 100.0], probe_avg=G["adapt_step"]["ctl"]["probe_avg"])
     assert [[it for it in range(1, 17) if RP.weather_schedule(ctl, it, j)[1]] for j in range(1, 5)] == \
-        [[8, 16], [6, 14], [4, 12], [2, 10]]
-    assert RP.weather_schedule(ctl, 8, 1) == (0.3, True) and RP.weather_schedule(ctl, 7, 1) == (0.0, False)
-    ctl.theta = 0.1
+        ws["burst_steps_1_to_16"]
+    assert RP.weather_schedule(ctl, 8, 1) == (ws["angle_at_8_replica_1"], True)
+    assert RP.weather_schedule(ctl, 7, 1) == (ws["angle_at_7_replica_1"], False)
+    ctl.theta = 0.1                      # a continuous angle composed with the burst (:23-24)
     assert math.isclose(RP.weather_schedule(ctl, 8, 1)[0], math.acos(math.cos(0.1) * math.cos(0.3)))
     assert RP.weather_schedule(ctl, 7, 1)[0] == 0.1
     ctl.theta = 0.0
-    p = [0.2, 0.0, 0.5, 0.3]
-    assert [RP.categorical(p, u) for u in (0.0, 0.1, 0.2, 0.2000001, 0.7, 0.70001, 1.0)] == [1, 1, 1, 3, 3, 4, 4]
-    assert RP.relaxation_indicator([[1.0, 2.0]], 4) == math.inf
-    assert math.isclose(RP.relaxation_indicator([[1.0, 2.0], [1.0, 2.0], [1.5, 2.0], [1.5, 2.2]], 4), 0.5)
+    c = G["categorical"]
+    assert [RP.categorical(c["p"], u) for u in c["u"]] == c["want"]
+    ri = G["relaxation_indicator"]
+    assert RP.relaxation_indicator(ri["gbuf"][:1], ri["win"]) == math.inf
+    assert math.isclose(RP.relaxation_indicator(ri["gbuf"], ri["win"]), ri["want"])
     R = RP.ReplicaSet(M=1, eta_w=ctl.eta_w, since=[0], window=[False], active=[False])
-    ctl.gate_max = 10
+    gr = G["gate"]["relaxing"]
+    ctl.gate_max = gr["gate_max"]
     acts = []
-    for g in ([5.0, 1.0], [2.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0], [1.0, 1.0]):
+    for g in gr["g"]:
         acts.append(RP.update_gate(R, 0, g, ctl))
         R.since[0] += 1
-    assert acts == [False, False, False, False, False, True, True]
-    ctl.gate_max = 5
+    assert acts == gr["want"]
+    gn = G["gate"]["never_relaxed"]
+    ctl.gate_max = gn["gate_max"]
     R.since[0] = 0
     R.active[0] = False
     R.gbuf[0].clear()
     acts = []
     for it in range(1, 8):
-        acts.append(RP.update_gate(R, 0, [float(it), 0.0], ctl))
+        acts.append(RP.update_gate(R, 0, [float(it) * gn["g_first"][0], gn["g_first"][1]], ctl))
         R.since[0] += 1
-    assert acts == [False, False, False, False, False, True, True]
-    Phis = [0.7, -1.3, 0.2, 2.1]
-    act = [True, False, True, True]
-    assert list(RP.tilt_weights(0.0, Phis, act)) == list(RP.uniform_weights(act)) == [1 / 3, 0.0, 1 / 3, 1 / 3]
-    w = RP.tilt_weights(2.0, Phis, act)
-    assert math.isclose(w.sum(), 1) and w[1] == 0 and math.isclose(w[3] / w[0], math.exp(2 * (2.1 - 0.7)))
-    assert list(RP.uniform_weights([False] * 4)) == [0.25] * 4
-    R.eta_w = [1e-3, 1e-3]
-    assert not RP.adapt_step(R, [0.5, 0.01], ctl)
-    assert RP.adapt_step(R, [-0.1, 0.03], ctl)
-    np.testing.assert_allclose(R.eta_w, [0.7e-3, 1.2e-3]) and not R.gaps
+    assert acts == gn["want"]
+    w8 = G["weights"]
+    assert list(RP.tilt_weights(0.0, w8["Phi"], w8["active"])) == list(RP.uniform_weights(w8["active"])) == \
+        w8["uniform"]
+    w = RP.tilt_weights(w8["lam"], w8["Phi"], w8["active"])
+    assert math.isclose(w.sum(), 1) and w[1] == 0
+    assert math.isclose(w[3] / w[0], math.exp(w8["lam"] * (w8["Phi"][3] - w8["Phi"][0])))
+    assert list(RP.uniform_weights([False] * 4)) == w8["none_active"]
+    ad = G["adapt_step"]
+    R.eta_w = list(ad["eta0"])
+    assert [RP.adapt_step(R, g, ctl) for g in ad["gaps"]] == ad["want_adapted"]
+    np.testing.assert_allclose(R.eta_w, ad["want_eta"])
+    assert not R.gaps
 
 
 def test_convergence_diagnostics():
