@@ -267,8 +267,10 @@ int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_p
 int esm_autotune_moves(esm_ctx *ctx, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand);
 
 /* Lag probe (lag_probe, src/replicas.jl:733): a copy of replica j, at the chain's capacities and
-   with its weather frozen, runs nsweeps operation sweeps (sweep indices sweep0 ...; the probe
-   context's streams) and sk_mean [K] receives the mean capacity score of the last `tail` sweeps, fk
+   with its weather frozen, runs nsweeps operation sweeps (sweep indices sweep0 ... sweep0 +
+   nsweeps - 1 of the probe context's streams: give every probe its own range, e.g. sweep0 = step *
+   nsweeps, as the reference's probe stream advances from probe to probe) and sk_mean [K]
+   receives the mean capacity score of the last `tail` sweeps, fk
    [K] (may be NULL) the prior term of the last; the chain is unchanged. The host forms the gap
    against the replica's in-flight scores and adapts the step (adapt_step!, :758). Needs
    esm_opts.probe = 1. */
