@@ -75,3 +75,30 @@ def test_init_replicas_sweeps():
     st = o.get_state()
     assert not np.array_equal(st["theta"], np.repeat(s0.theta, 4, axis=-1))   # the sweeps moved the angles
     assert math.isclose(float(np.abs(st["k"] - s0.k).max()), 0.0)              # at fixed k
+
+
+def test_init_replicas_anomalies_are_prior_draws():
+    """The anomalies init_replicas leaves are a draw from the prior given the new regime paths: their
+    VAR innovations (src/replicas.jl:29-112, the diagonal VAR of the model) are independent standard
+    normals (mean within 4 standard errors of 0, variance within 5 % of 1, lag-one correlation
+    within 4 standard errors of 0)."""
+    m = make_model(12, 18, 120, seed=3)
+    s0 = initial_state(m, 1, seed=5)
+    R = 16
+    o = Oracle(m, R, seed=7)
+    RP.init_replicas(OracleChain(o), s0, RP.ReplicaCtl(M=R), 0, np.random.Generator(np.random.PCG64(2)), it=1)
+    st = o.get_state()
+    z, reg = st["z"], st["reg"]
+    T = m.T
+    e = np.empty_like(z)
+    e[:, 0, :] = z[:, 0, :] / m.sig0[:, None]
+    for t in range(1, T):
+        k = reg[t]                                           # [R]
+        cs, sn = math.cos(2 * math.pi * (t + 1) / T), math.sin(2 * math.pi * (t + 1) / T)
+        mean = (m.phi[k].T * z[:, t - 1, :] + m.mu[k, :, 0].T + cs * m.mu[k, :, 1].T + sn * m.mu[k, :, 2].T)
+        e[:, t, :] = (z[:, t, :] - mean) / m.sig[k].T
+    x = e.ravel()
+    n = x.size
+    lag = (e[:, 1:, :] * e[:, :-1, :]).mean()
+    print(f"innovations: n {n}, mean {x.mean():.4f}, var {x.var():.4f}, lag-one {lag:.4f}")
+    assert abs(x.mean()) < 4 / math.sqrt(n) and abs(x.var() - 1) < 0.05 and abs(lag) < 4 / math.sqrt(n)
