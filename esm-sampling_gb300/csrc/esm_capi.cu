@@ -52,6 +52,10 @@ struct esm_ctx {
     bool has_state = false, has_scores = false;
     int move_wpb = 1;           // k_move block shape: warps per block (1, 2 or 4)
     int max_warps = 0;          // k_move warps launched per move: the resident limit or a tuned count
+    // the cooperative walk of the separable moves (k_move_sep): moves with at least sep_min units
+    // (0: off), its grid and where its per-warp walk buffers live
+    int sep_min = ESM_SEP_MIN_DEFAULT, sep_max_warps = 0, sep_in_smem = 1;
+    char *d_sep_slab = nullptr;
     int warps_cap[3] = {0, 0, 0};  // the resident limit per block shape (1, 2, 4 warps per block)
     int nsm = 0;
     esm::DevModel<float> Mf;
@@ -476,6 +480,22 @@ int alloc_state(esm_ctx *c) {
     }
     if ((rc = dalloc(c, &q, per * wscr))) return rc;
     c->d_scratch = q;
+    // the cooperative walk: resident warps of k_move_sep and, when two walk regions and the
+    // descriptor do not fit a block's shared memory, one global region per warp (at most 1 GB)
+    {
+        int in_smem = 1;
+        int wps = esm::sep_warps_per_sm<real>(M, &in_smem);
+        size_t reg = esm::sep_region_bytes<real>(M);
+        size_t sw = (size_t)nsm * wps;
+        if (!in_smem) sw = std::max<size_t>(64, std::min(sw, ((size_t)1 << 30) / reg));
+        c->sep_max_warps = (int)(sw & ~(size_t)1);
+        c->sep_in_smem = in_smem;
+        if (!in_smem) {
+            char *sl;
+            if ((rc = dalloc(c, &sl, reg * (size_t)c->sep_max_warps))) return rc;
+            c->d_sep_slab = sl;
+        }
+    }
     // the move descriptors of a class pass
     char *dp;
     if ((rc = dalloc(c, &dp, esm::linemove_smem_per_warp<real>(M) * (size_t)(M.natoms + M.nextra)))) return rc;
@@ -586,13 +606,14 @@ __global__ void k_set_word(uint32_t *p, uint32_t v) { *p = v; }
 
 int class_pass_launch(esm_ctx *c, int cls, int limit) {
     int ns = c->class_len[cls];
+    esm::SepLaunch sep{c->sep_min, c->sep_max_warps, c->sep_in_smem, c->d_sep_slab};
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, c->d_sweep, cls, limit, (double *)c->d_scratch,
-                                          c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr,
+                                          c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, sep,
                                           c->stream));
     else
         CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, c->d_sweep, cls, limit, (float *)c->d_scratch,
-                                         c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr,
+                                         c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, sep,
                                          c->stream));
     return ESM_OK;
 }
@@ -1547,6 +1568,29 @@ int esm_set_move_grid(esm_ctx *c, int32_t warps_per_block, int32_t warps_per_sm)
         }
     c->move_wpb = warps_per_block;
     c->max_warps = w;
+    return ESM_OK;
+}
+
+int esm_set_sep_walk(esm_ctx *c, int32_t min_units) {
+    if (!c) return ESM_EINVAL;
+    if (min_units < 0) return fail(c, ESM_EINVAL, "min_units must be >= 0");
+    if (min_units == c->sep_min) return ESM_OK;
+    int rc = esm_sync(c, 600.0);  // the captured class passes hold the old choice: drop them
+    if (rc) return rc;
+    for (auto &g : c->graph)
+        if (g) {
+            CK(cudaGraphExecDestroy(g));
+            g = nullptr;
+        }
+    c->sep_min = min_units;
+    if (c->probe) return esm_set_sep_walk(c->probe, min_units);
+    return ESM_OK;
+}
+
+int esm_sep_walk(const esm_ctx *c, int32_t *min_units, int32_t *warps) {
+    if (!c) return ESM_EINVAL;
+    if (min_units) *min_units = c->sep_min;
+    if (warps) *warps = c->sep_max_warps;
     return ESM_OK;
 }
 

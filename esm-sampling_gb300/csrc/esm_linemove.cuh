@@ -10,12 +10,25 @@ template <class real>
 size_t linemove_scratch_reals(const DevModel<real> &M);  // per warp
 template <class real>
 size_t linemove_smem_per_warp(const DevModel<real> &M);  // bytes of one move descriptor
+// the cooperative walk of the separable moves: moves whose units are storage units at distinct nodes
+// and nothing else, with at least min_units units (0: none, k_move walks every move), run in
+// k_move_sep on max_warps warps, their walk buffers in shared memory (in_smem) or in per-warp slabs
+// of `slab` (sep_region_bytes each)
+struct SepLaunch {
+    int min_units, max_warps, in_smem;
+    char *slab;
+};
+template <class real>
+size_t sep_region_bytes(const DevModel<real> &M);
+template <class real>
+int sep_warps_per_sm(const DevModel<real> &M, int *in_smem);
 // one colour class: the descriptors of its moves into descs ((natoms + nextra) descriptors), then
-// one launch per move; the sweep index is read on the device from *sweep (graph-capturable)
+// per move one k_move launch (and one k_move_sep launch; the kernel that does not take the move
+// returns at once); the sweep index is read on the device from *sweep (graph-capturable)
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
                               int limit, real *scratch, int wpb, int max_warps, unsigned long long *stats,
-                              char *descs, unsigned int *counters, cudaStream_t s);
+                              char *descs, unsigned int *counters, const SepLaunch &sep, cudaStream_t s);
 // resident k_move warps per SM with blocks of wpb (1, 2 or 4) warps
 template <class real>
 int linemove_blocks_per_sm(const DevModel<real> &M, int wpb);

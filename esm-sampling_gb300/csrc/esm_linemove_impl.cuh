@@ -1572,6 +1572,12 @@ __device__ __noinline__ void lane_kinks(const Lane<real> &Ln) {
     }
 }
 
+}  // namespace esm
+
+#include "esm_sepwalk.cuh"
+
+namespace esm {
+
 // ---------------------------------------------------------------------------------------------
 // the kernel: one colour class of one sweep
 // ---------------------------------------------------------------------------------------------
@@ -1629,7 +1635,7 @@ template <class real, int WPB>
 __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
     k_move(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps, int ntile, int wpt,
            const uint32_t *sweep_p, int mi, const char *descs, size_t stride, real *scratch,
-           unsigned long long *stats, unsigned int *next_item) {
+           unsigned long long *stats, unsigned int *next_item, int sepmin) {
     extern __shared__ __align__(16) char smem[];
     __shared__ Desc<real> sd;
     __shared__ LaneLayout sLL;
@@ -1651,6 +1657,7 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
     const LaneLayout &LL = sLL;
     int fi = d.hdr[12];
     if (fi < 0) return;  // not a valid move: nothing to do (grid-uniform)
+    if (sep_move<real>(d, sepmin)) return;  // k_move_sep walks it (grid-uniform)
     // per-lane scratch: a local array (cached in L1, written back) when the layout fits it, else
     // the lane's column of this warp's slab in global memory
     real local[ESM_LANE_LOCAL];
@@ -1754,10 +1761,31 @@ int linemove_blocks_per_sm(const DevModel<real> &M, int wpb) {
     return nb * wpb;
 }
 
+// The cooperative walk of the separable moves (k_move_sep, two-warp blocks): its per-warp region,
+// and whether two regions and the descriptor fit in a block's shared memory (else global slabs).
+template <class real>
+size_t sep_region_bytes(const DevModel<real> &M) {
+    return (size_t)sep_layout<real>(M.maxstu, M.maxpts).total;
+}
+
+template <class real>
+int sep_warps_per_sm(const DevModel<real> &M, int *in_smem) {
+    size_t stride = linemove_smem_per_warp(M);
+    size_t per = sep_region_bytes(M);
+    size_t smem = stride + 2 * per;
+    *in_smem = smem <= 200 * 1024;
+    if (!*in_smem) smem = stride;
+    cudaFuncSetAttribute(k_move_sep<real, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    int nb = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move_sep<real, 2>, 64, smem);
+    if (e != cudaSuccess || nb < 1) nb = 1;
+    return 2 * nb;
+}
+
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
                               int limit, real *scratch, int wpb, int max_warps, unsigned long long *stats,
-                              char *descs, unsigned int *counters, cudaStream_t s) {
+                              char *descs, unsigned int *counters, const SepLaunch &sep, cudaStream_t s) {
     int nmoves = M.natoms + M.nextra;
     int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
     size_t stride = linemove_smem_per_warp(M);
@@ -1770,17 +1798,27 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
     int items = ntile * wpt;
     int warps = items < max_warps ? items : max_warps;
     int blocks = (warps + wpb - 1) / wpb;
+    int sepmin = sep.min_units;
+    int ntask = nsteps * M.R;
+    int swarps = ntask < sep.max_warps ? ntask : sep.max_warps;
+    int sblocks = (swarps + 1) / 2;
+    size_t ssmem = stride + (sep.in_smem ? 2 * sep_region_bytes(M) : 0);
     for (int mi = 0; mi < nrun; ++mi) {
         if (wpb == 4)
             k_move<real, 4><<<blocks, 128, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
-                                                       stats, counters + mi);
+                                                       stats, counters + mi, sepmin);
         else if (wpb == 2)
             k_move<real, 2><<<blocks, 64, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
-                                                      stats, counters + mi);
+                                                      stats, counters + mi, sepmin);
         else
             k_move<real, 1><<<blocks, 32, stride, s>>>(M, steps, nsteps, ntile, wpt, sweep, mi, descs, stride, scratch,
-                                                      stats, counters + mi);
+                                                      stats, counters + mi, sepmin);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (sepmin > 0 && sblocks > 0) {
+            k_move_sep<real, 2><<<sblocks, 64, ssmem, s>>>(M, steps, nsteps, sweep, mi, descs, stride, sepmin,
+                                                          sep.in_smem, sep.slab, stats, counters + mi);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
     }
     return cudaSuccess;
 }

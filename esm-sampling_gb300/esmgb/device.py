@@ -23,7 +23,8 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
            "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
-           "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe")
+           "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe", "esm_set_sep_walk",
+           "esm_sep_walk")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -77,6 +78,8 @@ def load(build_if_missing=True):
     L.esm_storage_long.argtypes = [C.c_void_p, C.c_int64, P_i64]
     L.esm_lag_probe.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int64, P_f64, P_f64]
     L.esm_move_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
+    L.esm_set_sep_walk.argtypes = [C.c_void_p, C.c_int32]
+    L.esm_sep_walk.argtypes = [C.c_void_p, P_i32, P_i32]
     L.esm_autotune_moves.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
     L.esm_launch_count.restype = C.c_int64
     L.esm_launch_count.argtypes = [C.c_void_p]
@@ -252,6 +255,16 @@ class DeviceChain:
     def set_move_grid(self, warps_per_block=1, warps_per_sm=0):
         """Line-move grid: blocks of 1, 2 or 4 warps, resident warps per SM (0: that shape's limit)."""
         self._check(self.L.esm_set_move_grid(self.h, int(warps_per_block), int(warps_per_sm)), "esm_set_move_grid")
+
+    def set_sep_walk(self, min_units):
+        """The cooperative walk for separable moves of at least min_units units (0: off)."""
+        self._check(self.L.esm_set_sep_walk(self.h, int(min_units)), "esm_set_sep_walk")
+
+    def sep_walk(self):
+        """(min_units, warps of the cooperative walk kernel)."""
+        a, b = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        self._check(self.L.esm_sep_walk(self.h, _p(a, P_i32), _p(b, P_i32)), "esm_sep_walk")
+        return int(a[0]), int(b[0])
 
     def move_grid(self):
         """(warps per block, warps per SM, limits per SM of the 1-, 2- and 4-warp shapes)."""

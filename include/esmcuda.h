@@ -257,6 +257,18 @@ int esm_state_restore(esm_ctx *ctx);
 int esm_set_move_grid(esm_ctx *ctx, int32_t warps_per_block, int32_t warps_per_sm);
 int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limits_per_sm);
 
+/* The cooperative walk of the separable moves. A move whose terms are storage units at distinct
+   nodes and nothing else (the state-of-charge atoms, walk!, src/local.jl:1294, on a potential that
+   is a sum of per-unit functions) with at least min_units units runs one (step, replica) task per
+   warp: the lanes generate the units' breakpoints, a window's breakpoints are sorted in shared memory
+   and the potential follows from warp scans. Smaller and other moves keep one task per lane (k_move).
+   min_units 0 switches it off. Same draws and the same points as the per-lane walk, up to the
+   order of floating-point sums. esm_set_sep_walk drops the captured class graphs; esm_sep_walk
+   reads the setting and the kernel's warps. No reference counterpart. */
+#define ESM_SEP_MIN_DEFAULT 0
+int esm_set_sep_walk(esm_ctx *ctx, int32_t min_units);
+int esm_sep_walk(const esm_ctx *ctx, int32_t *min_units, int32_t *warps);
+
 /* Autotuner of the line-move grid: for each candidate (warps_per_block, warps_per_sm) -- the three
    block shapes at their resident limits and at 8, 16, 24, 32, 40 warps per SM below them -- one
    colour class of sweep `sweep` is run and timed (CUDA events on the context's stream) from the

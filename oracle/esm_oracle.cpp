@@ -465,6 +465,7 @@ struct Walk {
     vector<double> pts, cs;
     int cap;
     bool full = false;
+    int nprim = 0, nray = 0;  // primary breakpoints and ray steps visited (diagnostics)
     void push(double x, double cx) {
         if ((int)pts.size() >= cap) {
             full = true;
@@ -515,7 +516,9 @@ static int walk(Walk &W, Mover &mv, vector<double> &bp, double sgn, double maxna
         if (idx < bp.size()) {
             t = bp[idx++];
             if (t == tp) continue;
+            W.nprim += 1;
         } else {
+            W.nray += 1;
             double cprev = W.cs.empty() ? 0.0 : W.cs.back();
             double hp = 1e-6 * std::max(1.0, fabs(tp));
             double sl = (mv.beta * mv.eval(tp + sgn * hp) + 0.0 - cprev - 0.0) / hp;
@@ -2079,6 +2082,65 @@ int orc_move_walk(void *p, int fam, int tau, int rep, int cls, int64_t sweep, do
     Wr.cap = Wl.cap = c.o.max_points > 0 ? c.o.max_points : 4096;
     if (!walk(Wr, mv, right, 1.0, c.o.maxnats, sec0) || Wr.full) return -1;
     if (!walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) || Wl.full) return -1;
+    int n = 0;
+    auto put = [&](double x, double cx) {
+        if (n < maxn) {
+            pts[n] = x;
+            cs[n] = cx;
+        }
+        ++n;
+    };
+    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) put(Wl.pts[j], Wl.cs[j]);
+    put(0.0, 0.0);
+    for (size_t j = 0; j < Wr.pts.size(); ++j) put(Wr.pts[j], Wr.cs[j]);
+    return n;
+}
+
+// The walk of atom `atom` (index into the model's atoms) at 0-based step tau of replica rep on the
+// current state, without committing: the points (ascending, with t = 0) and their potentials into
+// pts, cs (up to maxn), and in info[0..3] the points of the right and left walks and the primary
+// breakpoints and ray steps the two walks visited. Returns the number of points, -1 when a walk
+// reached the point cap or ran out of ray steps. A diagnostic of the walk lengths.
+int orc_atom_walk(void *p, int atom, int tau, int rep, double *pts, double *cs, int maxn, int *info) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    WS ws, wa;
+    ws.init(m);
+    wa.init(m);
+    ws.tau = tau;
+    wa.tau = (tau - 1 + m.T) % m.T;
+    int f = 0;
+    while (f + 1 < (int)m.fap.size() - 1 && m.fap[f + 1] <= atom) ++f;
+    int role = m.frole[f];
+    int kind = role == ESM_ROLE_THETA ? EK_THETA : (role == ESM_ROLE_GEN ? EK_GEN : EK_SE);
+    for (int q = m.ap[atom]; q < m.ap[atom + 1]; ++q) ws.add_entry(kind, m.ai[q], m.av[q]);
+    finalize_ws(c, ws, rep);
+    if (ws.ent.empty()) return 0;
+    finalize_ws(c, wa, rep);
+    link_soc(m, wa, ws);
+    Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
+    vector<double> right, left;
+    for (const WS *w : mv.w)
+        for (double x : w->bps) {
+            if (!std::isfinite(x)) continue;
+            if (x > 0.0)
+                right.push_back(x);
+            else if (x < 0.0)
+                left.push_back(x);
+        }
+    mv.eval(0.0);
+    vector<double> sec0 = mv.sec;
+    Walk Wr, Wl;
+    Wr.cap = Wl.cap = c.o.max_points > 0 ? c.o.max_points : 4096;
+    int okr = walk(Wr, mv, right, 1.0, c.o.maxnats, sec0);
+    int okl = walk(Wl, mv, left, -1.0, c.o.maxnats, sec0);
+    if (info) {
+        info[0] = (int)Wr.pts.size();
+        info[1] = (int)Wl.pts.size();
+        info[2] = Wr.nprim + Wl.nprim;
+        info[3] = Wr.nray + Wl.nray;
+    }
+    if (!okr || !okl || Wr.full || Wl.full) return -1;
     int n = 0;
     auto put = [&](double x, double cx) {
         if (n < maxn) {

@@ -101,6 +101,49 @@ def test_class_pass_fp64(base):
     assert frac <= 0.02
 
 
+@pytest.mark.parametrize("sep", [0, 2, 41])
+def test_class_pass_fp64_walk_modes(base, sep):
+    """The same class pass with the separable moves walked one task per lane (sep 0 and 41: no
+    move has 41 units) or one task per warp (sep 2: every separable move): the same moves tried,
+    no guard events, and the oracle's result on all but the flipped tasks."""
+    m, st = base
+    d = DeviceChain(m, 32, precision=64, seed=5)
+    d.upload(st)
+    d.set_sep_walk(sep)
+    assert d.sep_walk()[0] == sep
+    d.rebuild()
+    o = Oracle(m, 32, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    sd = d.class_pass(3, 0)
+    so = o.class_pass(3, 0)
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
+    assert sd[-1] == so[-1] == 0
+    frac, worst = task_flips(d.download(), o.get_state(), m, 1e-9, 1e-9)
+    print(f"FP64 class pass, separable walk from {sep} units: flipped tasks {frac:.4f}, worst other {worst:.2e}")
+    assert frac <= 0.02
+
+
+@pytest.mark.parametrize("sep", [0, 2])
+@pytest.mark.parametrize("limit", [1, 20])
+def test_moves_fp32_walk_modes(equilibrated, sep, limit):
+    """The first moves of every task of the FP32 build with either walk of the separable moves."""
+    m, st = equilibrated
+    d = DeviceChain(m, 32, precision=32, seed=5)
+    d.upload(st)
+    d.set_sep_walk(sep)
+    d.rebuild()
+    o = Oracle(m, 32, seed=5)
+    o.set_state(st)
+    o.rebuild()
+    sd = d.class_pass(3, 1, limit)
+    so = o.class_pass(3, 1, limit)
+    assert np.array_equal(sd[:-1:2], so[:-1:2])
+    frac, worst = task_flips(d.download(), o.get_state(), m, 2e-3, 4e-3)
+    print(f"FP32 first {limit} moves, separable walk from {sep} units: flipped {frac:.4f}, worst other {worst:.2e}")
+    assert frac <= 0.02
+
+
 @pytest.mark.parametrize("wpb,wps", [(1, 8), (2, 0), (4, 0), (4, 16)])
 def test_class_pass_fp64_grids(base, wpb, wps):
     """The same class pass with every k_move block shape and a reduced grid: the work items are
