@@ -908,6 +908,11 @@ int esm_class_pass(esm_ctx *c, int64_t sweep, int32_t cls, int32_t move_limit, i
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
     if (cls < 0 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
     CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * (2 * (ESM_NFAM + 1) + 1), c->stream));
+    double *mlog = c->precision == 64 ? c->Md.mlog : c->Mf.mlog;
+    if (mlog) {  // entries of moves that made no move (and beyond the limit) read NaN
+        size_t nmoves = c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
+        CK(cudaMemsetAsync(mlog, 0xff, sizeof(double) * nmoves * c->class_len[cls] * c->Md.mlog_nrep, c->stream));
+    }
     int rc = class_pass_any(c, (uint32_t)sweep, cls, move_limit);
     if (rc) return rc;
     c->has_scores = false;
@@ -1568,6 +1573,41 @@ int esm_set_move_grid(esm_ctx *c, int32_t warps_per_block, int32_t warps_per_sm)
         }
     c->move_wpb = warps_per_block;
     c->max_warps = w;
+    return ESM_OK;
+}
+
+int esm_set_move_log(esm_ctx *c, int32_t nreps) {
+    if (!c) return ESM_EINVAL;
+    if (nreps < 0 || nreps > c->R) return fail(c, ESM_EINVAL, "nreps must be in 0 .. R");
+    int rc = esm_sync(c, 600.0);  // the captured class passes hold the old setting: drop them
+    if (rc) return rc;
+    for (auto &g : c->graph)
+        if (g) {
+            CK(cudaGraphExecDestroy(g));
+            g = nullptr;
+        }
+    double *p = nullptr;
+    if (nreps > 0) {
+        size_t nmoves = c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
+        size_t ns = 0;
+        for (int k = 0; k < c->ncls; ++k) ns = std::max(ns, (size_t)c->class_len[k]);
+        if ((rc = dalloc(c, &p, nmoves * ns * (size_t)nreps))) return rc;
+        CK(cudaMemsetAsync(p, 0xff, sizeof(double) * nmoves * ns * nreps, c->stream));
+    }
+    c->Mf.mlog = c->Md.mlog = p;
+    c->Mf.mlog_nrep = c->Md.mlog_nrep = nreps;
+    return ESM_OK;
+}
+
+int esm_move_log(esm_ctx *c, int32_t cls, double *out) {
+    if (!c || !out) return ESM_EINVAL;
+    if (!c->Md.mlog && !c->Mf.mlog) return fail(c, ESM_ESTATE, "the move log is off (esm_set_move_log)");
+    if (cls < 0 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
+    size_t nmoves = c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
+    size_t n = nmoves * (size_t)c->class_len[cls] * (size_t)c->Md.mlog_nrep;
+    double *src = c->precision == 64 ? c->Md.mlog : c->Mf.mlog;
+    CK(cudaMemcpyAsync(out, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return ESM_OK;
 }
 

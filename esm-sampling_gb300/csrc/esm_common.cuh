@@ -120,6 +120,10 @@ struct DevModel {
     const int *lb0_ptr, *lb0_line;
     // state
     real *theta, *g, *e, *r, *F, *z;
+    // move log (diagnostics, NULL: off): the t every line move of a class pass took for replicas
+    // below mlog_nrep, at [(move * nsteps + q) * mlog_nrep + replica] for the class's q-th step
+    double *mlog;
+    int mlog_nrep;
 };
 
 __host__ __device__ inline size_t sidx(int x, int t, int rep, int T, int R) { return ((size_t)x * T + t) * R + rep; }

@@ -1706,6 +1706,7 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
             }
         }
         if (t != 0) Ln.commit(t);
+        if (M.mlog && Ln.rep < M.mlog_nrep) M.mlog[((size_t)mi * nsteps + q) * M.mlog_nrep + Ln.rep] = (double)t;
         ++tried;
         if (t != 0) ++moved;
     }

@@ -691,6 +691,8 @@ __global__ void __launch_bounds__(32 * WPB)
         real t = W.sample_line((real)uc, (real)uo, &guard);
         if (guard) ++guards;
         if (t != 0) W.commit(t);
+        if (M.mlog && W.rep < M.mlog_nrep && lane == 0)
+            M.mlog[((size_t)mi * nsteps + q) * M.mlog_nrep + W.rep] = (double)t;
         ++tried;
         if (t != 0) ++moved;
         __syncwarp();

@@ -24,7 +24,7 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
            "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
            "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe", "esm_set_sep_walk",
-           "esm_sep_walk")
+           "esm_sep_walk", "esm_set_move_log", "esm_move_log")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -79,6 +79,8 @@ def load(build_if_missing=True):
     L.esm_lag_probe.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int64, P_f64, P_f64]
     L.esm_move_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
     L.esm_set_sep_walk.argtypes = [C.c_void_p, C.c_int32]
+    L.esm_set_move_log.argtypes = [C.c_void_p, C.c_int32]
+    L.esm_move_log.argtypes = [C.c_void_p, C.c_int32, P_f64]
     L.esm_sep_walk.argtypes = [C.c_void_p, P_i32, P_i32]
     L.esm_autotune_moves.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
     L.esm_launch_count.restype = C.c_int64
@@ -255,6 +257,18 @@ class DeviceChain:
     def set_move_grid(self, warps_per_block=1, warps_per_sm=0):
         """Line-move grid: blocks of 1, 2 or 4 warps, resident warps per SM (0: that shape's limit)."""
         self._check(self.L.esm_set_move_grid(self.h, int(warps_per_block), int(warps_per_sm)), "esm_set_move_grid")
+
+    def set_move_log(self, nreps):
+        """Record the t of every line move of each class pass for replicas below nreps (0: off)."""
+        self._check(self.L.esm_set_move_log(self.h, int(nreps)), "esm_set_move_log")
+        self._mlog_nrep = int(nreps)
+
+    def move_log(self, cls, nmoves, nsteps):
+        """The move log of the last class pass (class cls): [move, class step, replica], NaN where the
+        selection made no move."""
+        out = np.zeros(nmoves * nsteps * self._mlog_nrep)
+        self._check(self.L.esm_move_log(self.h, int(cls), _p(out)), "esm_move_log")
+        return out.reshape(nmoves, nsteps, self._mlog_nrep)
 
     def set_sep_walk(self, min_units):
         """The cooperative walk for separable moves of at least min_units units (0: off)."""

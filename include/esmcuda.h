@@ -257,6 +257,14 @@ int esm_state_restore(esm_ctx *ctx);
 int esm_set_move_grid(esm_ctx *ctx, int32_t warps_per_block, int32_t warps_per_sm);
 int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limits_per_sm);
 
+/* Move log (diagnostics of parity tests; no reference counterpart): with nreps > 0 every class pass
+   of esm_class_pass records the t that each line move took for the replicas below nreps (device
+   memory: moves x longest class x nreps doubles); 0 switches it off. esm_move_log copies the log of
+   the last class pass, which must have been class cls, as [(move * nsteps + q) * nreps + replica]
+   for the class's q-th step (nsteps its steps); moves whose selection made no move read NaN. */
+int esm_set_move_log(esm_ctx *ctx, int32_t nreps);
+int esm_move_log(esm_ctx *ctx, int32_t cls, double *out);
+
 /* The cooperative walk of the separable moves. A move whose terms are storage units at distinct
    nodes and nothing else (the state-of-charge atoms, walk!, src/local.jl:1294, on a potential that
    is a sum of per-unit functions) with at least min_units units runs one (step, replica) task per

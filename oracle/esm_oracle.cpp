@@ -466,6 +466,10 @@ struct Walk {
     int cap;
     bool full = false;
     int nprim = 0, nray = 0;  // primary breakpoints and ray steps visited (diagnostics)
+    // the stop test's margins (diagnostics): c - cmin - maxnats where the walk stopped, and the
+    // largest value it took at an earlier primary breakpoint or ray point (how near a stop came)
+    double stop = NAN, near_ = -INFINITY;
+    double ray_from = NAN;  // where the ray steps began (the last primary breakpoint, or 0)
     void push(double x, double cx) {
         if ((int)pts.size() >= cap) {
             full = true;
@@ -518,6 +522,7 @@ static int walk(Walk &W, Mover &mv, vector<double> &bp, double sgn, double maxna
             if (t == tp) continue;
             W.nprim += 1;
         } else {
+            if (W.nray == 0) W.ray_from = tp;
             W.nray += 1;
             double cprev = W.cs.empty() ? 0.0 : W.cs.back();
             double hp = 1e-6 * std::max(1.0, fabs(tp));
@@ -574,7 +579,11 @@ static int walk(Walk &W, Mover &mv, vector<double> &bp, double sgn, double maxna
         }
         W.push(t, cval);
         cmin = std::min(cmin, cval);
-        if (cval + 0.0 - cmin > maxnats) return 1;
+        if (cval + 0.0 - cmin > maxnats) {
+            W.stop = cval - cmin - maxnats;
+            return 1;
+        }
+        W.near_ = std::max(W.near_, cval - cmin - maxnats);
         if (W.full) return 1;
         tp = t;
     }
@@ -925,7 +934,8 @@ static bool prep_family(const Ctx &c, TileStream &ts, int fam, WS &ws, WS &wa, i
 // the moves of one (replica, step) task: the body of the threaded loop of local_sweep!
 // (src/local.jl:1954-2051)
 static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int tau, int rep, uint32_t sweep,
-                     int64_t *stats, WS &ws, WS &wa, int limit) {
+                     int64_t *stats, WS &ws, WS &wa, int limit, int m0 = 0, double *tlog = nullptr,
+                     size_t tlog_stride = 0, size_t tlog_at = 0) {
     const Model &m = c.m;
     int T = m.T;
     int taum = (tau - 1 + T) % T;
@@ -941,6 +951,10 @@ static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int t
         jac.clear();
         const MoveRef &mr = moves[mi];
         int fi;
+        if ((int)mi < m0) {  // before the range: only the selection draws, to keep the stream position
+            if (mr.kind >= 0) prep_family(c, ts, mr.kind, ws, wa, rep, &jac);
+            continue;
+        }
         if (mr.kind < 0) {  // prep_atom! (src/local.jl:1567)
             int role = m.frole[mr.field];
             int kind = role == ESM_ROLE_THETA ? EK_THETA : (role == ESM_ROLE_GEN ? EK_GEN : EK_SE);
@@ -967,6 +981,7 @@ static void run_task(Ctx &c, const vector<MoveRef> &moves, TileStream ts0, int t
             if (uj >= exp(std::min(0.0, lj))) t = 0.0;
         }
         commit(c, mv, t);
+        if (tlog) tlog[mi * tlog_stride + tlog_at] = t;
         stats[2 * fi] += 1;
         stats[2 * fi + 1] += t != 0.0;
     }
@@ -990,7 +1005,8 @@ static void class_steps(int T, int cls, vector<int> &out) {
 
 static int span_of(const Ctx &c) { return c.o.span > 0 ? c.o.span : std::max(1, 32 / c.o.R); }
 
-static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthreads, int limit = 0) {
+static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthreads, int limit = 0, int m0 = 0,
+                       double *tlog = nullptr) {
     vector<int> steps;
     class_steps(c.m.T, cls, steps);
     int span = span_of(c);
@@ -1010,7 +1026,9 @@ static void class_pass(Ctx &c, uint32_t sweep, int cls, int64_t *stats, int nthr
 #pragma omp for schedule(dynamic, 1)
         for (int tile = 0; tile < ntile; ++tile) {
             for (int q = tile * span; q < std::min((int)steps.size(), (tile + 1) * span); ++q)
-                for (int rep = 0; rep < R; ++rep) run_task(c, moves, ts0, steps[q], rep, sweep, loc.data(), ws, wa, limit);
+                for (int rep = 0; rep < R; ++rep)
+                    run_task(c, moves, ts0, steps[q], rep, sweep, loc.data(), ws, wa, limit, m0, tlog,
+                             steps.size() * (size_t)R, (size_t)q * R + rep);
         }
 #pragma omp critical
         for (int i = 0; i < nst; ++i) stats[i] += loc[i];
@@ -1933,6 +1951,37 @@ void orc_class_pass(void *p, int64_t sweep, int cls, int limit, int64_t *stats, 
 
 // n sweeps: caches rebuilt at each sweep start (LocalCost, src/local.jl:1940), classes in the
 // sweep's order
+// Moves [m0, m1) of every task of class cls of sweep `sweep` (m1 < 0: to the end of the list); the
+// selection draws of the earlier moves are replayed, so the range continues a pass that ran [0, m0).
+// tlog (may be NULL): the t of every move of the range, at [(move * nsteps + q) * R + rep] for the
+// class's q-th step (entries of moves that made no move are left as they are).
+void orc_class_pass_range(void *p, int64_t sweep, int cls, int m0, int m1, int64_t *stats, int nthreads,
+                          double *tlog) {
+    Ctx *c = (Ctx *)p;
+    if (m1 >= 0 && m1 <= m0) return;
+    class_pass(*c, (uint32_t)sweep, cls, stats, nthreads, m1 > 0 ? m1 : 0, m0, tlog);
+}
+
+// Moves [m0, m1) (m1 < 0: to the end) of one task of a class pass: the class's q-th step of replica
+// rep (the tasks of a class are independent, so this advances that task alone). Returns the number
+// of moves in the class list.
+int orc_task_moves(void *p, int64_t sweep, int cls, int q, int rep, int m0, int m1) {
+    Ctx &c = *(Ctx *)p;
+    vector<int> steps;
+    class_steps(c.m.T, cls, steps);
+    if (q < 0 || q >= (int)steps.size() || rep < 0 || rep >= c.o.R) return -1;
+    TileStream ts0{c.o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
+    vector<MoveRef> moves;
+    move_list(c, ts0, moves);
+    WS ws, wa;
+    ws.init(c.m);
+    wa.init(c.m);
+    vector<int64_t> st(2 * (ESM_NFAM + 1) + 1, 0);
+    if (m1 >= 0 && m1 <= m0) return (int)moves.size();
+    run_task(c, moves, ts0, steps[q], rep, (uint32_t)sweep, st.data(), ws, wa, m1 > 0 ? m1 : 0, m0);
+    return (int)moves.size();
+}
+
 void orc_sweeps(void *p, int n, int64_t sweep0, int64_t *stats, int nthreads) {
     Ctx *c = (Ctx *)p;
     for (int s = 0; s < n; ++s) {
@@ -2094,6 +2143,170 @@ int orc_move_walk(void *p, int fam, int tau, int rep, int cls, int64_t sweep, do
     put(0.0, 0.0);
     for (size_t j = 0; j < Wr.pts.size(); ++j) put(Wr.pts[j], Wr.cs[j]);
     return n;
+}
+
+// Diagnosis of one move of a class pass (test infrastructure): move mi of the class list of
+// (cls, sweep) at the class's q-th step, replica rep, prepared on the current state (call it after
+// orc_class_pass_range ran moves [0, mi)), with its walks and draws; t_other is the t another
+// implementation drew for the same move. out[0..19]:
+//   0 t drawn (before the Jacobian test), 1 t after it, 2 segments, 3 the drawn segment jj,
+//   4 the segment holding t_other (-1 outside the walks, -2 t_other = 0), 5 how far u = u_cat tot
+//   lies from that segment's cumulative-mass interval, relative to tot (0 inside), 6 the distance of
+//   u from the nearer end of jj's interval, relative to tot, 7 log-Jacobian at t, 8 the Jacobian
+//   uniform, 9 log-Jacobian at t_other, 10/11 the stop margins of the right and left walks
+//   (c - cmin - maxnats where they stopped), 12/13 the largest c - cmin - maxnats at an earlier
+//   primary breakpoint or ray point (how near an earlier stop came), 14/15 their points, 16 the
+//   family (-1 atom), 17 the move's entries, 18 0 proper walks, 1 improper, 2 point cap, 19 tot,
+//   20/21 where the right and left walks began their ray steps (NaN: none), 22 |g L| of the drawn
+//   segment (the potential's change across it, nats), 23 its length L.
+// Returns 1, 0 when the selection made no move, -1 on a bad index.
+int orc_explain(void *p, int64_t sweep, int cls, int mi, int q, int rep, double t_other, double *out) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    vector<int> steps;
+    class_steps(m.T, cls, steps);
+    if (q < 0 || q >= (int)steps.size() || rep < 0 || rep >= c.o.R) return -1;
+    int tau = steps[q], T = m.T, taum = (tau - 1 + T) % T;
+    TileStream ts0{c.o.seed, 0u, (uint32_t)cls, (uint32_t)sweep};
+    vector<MoveRef> moves;
+    move_list(c, ts0, moves);
+    if (mi < 0 || mi >= (int)moves.size()) return -1;
+    TileStream ts = ts0;
+    WS ws, wa;
+    ws.init(m);
+    wa.init(m);
+    vector<Kink> jac;
+    for (int k = 0; k <= mi; ++k) {
+        ws.clear();
+        wa.clear();
+        ws.tau = tau;
+        wa.tau = taum;
+        jac.clear();
+        if (k < mi) {
+            if (moves[k].kind >= 0) prep_family(c, ts, moves[k].kind, ws, wa, rep, &jac);
+        }
+    }
+    const MoveRef &mr = moves[mi];
+    for (int i = 0; i < 24; ++i) out[i] = NAN;
+    if (mr.kind < 0) {
+        int role = m.frole[mr.field];
+        int kind = role == ESM_ROLE_THETA ? EK_THETA : (role == ESM_ROLE_GEN ? EK_GEN : EK_SE);
+        for (int k = m.ap[mr.atom]; k < m.ap[mr.atom + 1]; ++k) ws.add_entry(kind, m.ai[k], m.av[k]);
+    } else if (!prep_family(c, ts, mr.kind, ws, wa, rep, &jac)) {
+        return 0;
+    }
+    finalize_ws(c, ws, rep);
+    if (ws.ent.empty()) return 0;
+    finalize_ws(c, wa, rep);
+    link_soc(m, wa, ws);
+    out[16] = mr.kind < 0 ? -1.0 : (double)mr.kind;
+    out[17] = (double)(ws.ent.size() + wa.ent.size());
+    Mover mv{&c, {&wa, &ws}, rep, m.beta_v, {}};
+    double uc, uo, uj, un;
+    orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)tau, (uint32_t)rep, (uint32_t)sweep, &uc, &uo);
+    orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)tau, (uint32_t)rep, (uint32_t)sweep, &uj,
+                 &un);
+    out[8] = uj;
+    vector<double> right, left;
+    for (const WS *w : mv.w)
+        for (double x : w->bps) {
+            if (!std::isfinite(x)) continue;
+            if (x > 0.0)
+                right.push_back(x);
+            else if (x < 0.0)
+                left.push_back(x);
+        }
+    mv.eval(0.0);
+    vector<double> sec0 = mv.sec;
+    Walk Wr, Wl;
+    Wr.cap = Wl.cap = c.o.max_points;
+    int okr = walk(Wr, mv, right, 1.0, c.o.maxnats, sec0);
+    int okl = okr && !Wr.full ? walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) : 0;
+    out[10] = Wr.stop;
+    out[11] = Wl.stop;
+    out[12] = Wr.near_;
+    out[13] = Wl.near_;
+    out[14] = (double)Wr.pts.size();
+    out[15] = (double)Wl.pts.size();
+    out[20] = Wr.ray_from;
+    out[21] = Wl.ray_from;
+    auto ljac = [&](double t) {
+        double lj = 0.0;
+        for (auto &k : jac) lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
+        return lj;
+    };
+    if (Wr.full || Wl.full) {
+        out[18] = 2;
+        out[0] = out[1] = 0.0;
+        return 1;
+    }
+    if (!okr || !okl) {
+        out[18] = 1;
+        out[0] = out[1] = 0.0;
+        return 1;
+    }
+    out[18] = 0;
+    vector<double> pts, cs;
+    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) {
+        pts.push_back(Wl.pts[j]);
+        cs.push_back(Wl.cs[j]);
+    }
+    pts.push_back(0.0);
+    cs.push_back(0.0);
+    pts.insert(pts.end(), Wr.pts.begin(), Wr.pts.end());
+    cs.insert(cs.end(), Wr.cs.begin(), Wr.cs.end());
+    int nseg = (int)pts.size() - 1;
+    vector<double> lm(nseg), A(nseg + 1, 0.0);
+    double mx = -INFINITY;
+    for (int j = 0; j < nseg; ++j) {
+        double L = pts[j + 1] - pts[j];
+        lm[j] = L > 0 ? -std::min(cs[j], cs[j + 1]) + logseg(L, fabs(cs[j + 1] - cs[j])) : -INFINITY;
+        mx = std::max(mx, lm[j]);
+    }
+    double tot = 0.0;
+    for (int j = 0; j < nseg; ++j) tot += exp(lm[j] - mx);
+    double u = uc * tot, acc = 0.0;
+    int jj = nseg - 1;
+    bool found = false;
+    for (int k = 0; k < nseg; ++k) {
+        acc += exp(lm[k] - mx);
+        A[k + 1] = acc;
+        if (!found && u <= acc) {
+            jj = k;
+            found = true;
+        }
+    }
+    double L = pts[jj + 1] - pts[jj];
+    double g = (cs[jj + 1] - cs[jj]) / L;
+    double t = (g >= 0 || fabs(g * L) < 1e-10) ? pts[jj] + trexp_offset(uo, g, L) : pts[jj + 1] - trexp_offset(uo, -g, L);
+    out[0] = t;
+    out[22] = fabs(g * L);
+    out[23] = L;
+    out[2] = nseg;
+    out[3] = jj;
+    out[19] = tot;
+    out[6] = std::min(u - A[jj], A[jj + 1] - u) / tot;
+    bool compensated = mr.kind == ESM_FAM_XLOCC || mr.kind == ESM_FAM_TPOT || mr.kind == ESM_FAM_TSOC;
+    double t1 = t;
+    if (compensated && t != 0.0 && !jac.empty()) {
+        double lj = ljac(t);
+        out[7] = lj;
+        if (uj >= exp(std::min(0.0, lj))) t1 = 0.0;
+    }
+    out[1] = t1;
+    if (compensated && !jac.empty() && t_other != 0.0) out[9] = ljac(t_other);
+    int jo = -1;
+    if (t_other == 0.0)
+        jo = -2;
+    else
+        for (int j = 0; j < nseg; ++j)
+            if (pts[j] <= t_other && t_other <= pts[j + 1]) {
+                jo = j;
+                break;
+            }
+    out[4] = jo;
+    if (jo >= 0) out[5] = jo > jj ? (A[jo] - u) / tot : (jo < jj ? (u - A[jo + 1]) / tot : 0.0);
+    return 1;
 }
 
 // The walk of atom `atom` (index into the model's atoms) at 0-based step tau of replica rep on the

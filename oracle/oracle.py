@@ -65,6 +65,13 @@ def lib():
         L.orc_storage_long_plan.argtypes = [C.c_void_p, C.c_int64, P_i32, C.c_int]
         L.orc_storage_long_plan.restype = C.c_int
         L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
+        L.orc_class_pass_range.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, P_i64, C.c_int, P_f64]
+        L.orc_task_moves.restype = C.c_int
+        L.orc_task_moves.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_explain.restype = C.c_int
+        L.orc_explain.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P_f64]
+        L.orc_atom_walk.restype = C.c_int
+        L.orc_atom_walk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_f64, P_f64, C.c_int, P_i32]
         L.orc_class_order.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32]
         L.orc_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64, C.c_int]
         L.orc_langevin_step.restype = C.c_int
@@ -164,6 +171,43 @@ class Oracle:
         st = np.zeros(NSTAT, np.int64)
         lib().orc_class_pass(self.h, sweep, cls, limit, _p(st, P_i64), self.threads)
         return st
+
+    def class_pass_range(self, sweep, cls, m0, m1, tlog=None):
+        """Moves [m0, m1) of every task of a class pass (m1 < 0: to the end); tlog (float64 array
+        [moves, class steps, R], may be None) receives the t of every move of the range."""
+        st = np.zeros(NSTAT, np.int64)
+        lib().orc_class_pass_range(self.h, sweep, cls, m0, m1, _p(st, P_i64), self.threads,
+                                   None if tlog is None else tlog.ctypes.data_as(P_f64))
+        return st
+
+    def task_moves(self, sweep, cls, q, rep, m0, m1):
+        """Moves [m0, m1) (m1 < 0: to the end) of the one task at the class's q-th step of replica rep."""
+        n = lib().orc_task_moves(self.h, sweep, cls, q, rep, m0, m1)
+        if n < 0:
+            raise ValueError("orc_task_moves: bad index")
+        return n
+
+    EXPLAIN = ("t", "t_jac", "nseg", "seg", "seg_other", "cat_margin", "seg_margin", "lj", "uj", "lj_other",
+               "stop_r", "stop_l", "near_r", "near_l", "npts_r", "npts_l", "fam", "entries", "walk", "tot",
+               "ray_r", "ray_l", "gL", "L")
+
+    def explain(self, sweep, cls, mi, q, rep, t_other):
+        """Diagnosis of move mi at the class's q-th step of replica rep on the current state (see
+        orc_explain): a dict of EXPLAIN, or None when the selection made no move."""
+        out = np.zeros(24)
+        rc = lib().orc_explain(self.h, sweep, cls, mi, q, rep, float(t_other), _p(out))
+        if rc < 0:
+            raise ValueError("orc_explain: bad index")
+        return dict(zip(self.EXPLAIN, out.tolist())) if rc else None
+
+    def atom_walk(self, atom, tau, rep, maxn=8192):
+        """The walk of an atom move on the current state: (points, potentials, [right points, left
+        points, primary breakpoints, ray steps]), or None."""
+        pts, cs, info = np.zeros(maxn), np.zeros(maxn), np.zeros(4, np.int32)
+        n = lib().orc_atom_walk(self.h, atom, tau, rep, _p(pts), _p(cs), maxn, _p(info, P_i32))
+        if n <= 0:
+            return None
+        return pts[:n].copy(), cs[:n].copy(), info.tolist()
 
     def sweeps(self, n, sweep0=0):
         st = np.zeros(NSTAT, np.int64)
