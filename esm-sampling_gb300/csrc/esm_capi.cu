@@ -55,6 +55,7 @@ struct esm_ctx {
     // the cooperative walk of the separable moves (k_move_sep): moves with at least sep_min units
     // (0: off), its grid and where its per-warp walk buffers live
     int sep_min = ESM_SEP_MIN_DEFAULT, sep_max_warps = 0, sep_in_smem = 1;
+    int sl_nunits = 0;  // eligible units of the last long-range storage sweep (its move log)
     char *d_sep_slab = nullptr;
     int warps_cap[3] = {0, 0, 0};  // the resident limit per block shape (1, 2, 4 warps per block)
     int nsm = 0;
@@ -1062,6 +1063,9 @@ int sl_sweep_any(esm_ctx *c, uint32_t sweep) {
     if ((rc = sms_scratch(c))) return rc;
     if ((rc = rebuild_any(c))) return rc;  // LocalCost at the start (src/storage_long.jl:250)
     CK(cudaMemcpyAsync(c->d_sl_plan, plan.data(), sizeof(int) * plan.size(), cudaMemcpyHostToDevice, c->stream));
+    c->sl_nunits = nu;
+    double *mlog = c->precision == 64 ? c->Md.mlog : c->Mf.mlog;
+    if (mlog) CK(cudaMemsetAsync(mlog, 0xff, sizeof(double) * nu * 5 * c->Md.mlog_nrep, c->stream));
     Span sp(c, ESM_KT_STORAGE);
     if (c->precision == 64)
         CK(esm::launch_storage_long<double>(c->Md, c->d_sl_plan, nu, sweep, (double *)c->d_sms_scratch, c->sms_threads,
@@ -1602,9 +1606,10 @@ int esm_set_move_log(esm_ctx *c, int32_t nreps) {
 int esm_move_log(esm_ctx *c, int32_t cls, double *out) {
     if (!c || !out) return ESM_EINVAL;
     if (!c->Md.mlog && !c->Mf.mlog) return fail(c, ESM_ESTATE, "the move log is off (esm_set_move_log)");
-    if (cls < 0 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
+    if (cls < -1 || cls >= c->ncls) return fail(c, ESM_EINVAL, "class %d out of range", cls);
     size_t nmoves = c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
-    size_t n = nmoves * (size_t)c->class_len[cls] * (size_t)c->Md.mlog_nrep;
+    size_t n = cls < 0 ? (size_t)c->sl_nunits * 5 * (size_t)c->Md.mlog_nrep
+                       : nmoves * (size_t)c->class_len[cls] * (size_t)c->Md.mlog_nrep;
     double *src = c->precision == 64 ? c->Md.mlog : c->Mf.mlog;
     CK(cudaMemcpyAsync(out, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

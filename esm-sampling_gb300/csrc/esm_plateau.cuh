@@ -826,6 +826,8 @@ __global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__
                 }
             }
             if (t != 0) Ln.commit(t);
+            if (M.mlog && Ln.rep < M.mlog_nrep && Ln.lane == 0)
+                M.mlog[((task / M.R) * 5 + m) * M.mlog_nrep + Ln.rep] = (double)t;
             ++tried;
             if (t != 0) ++moved;
         }

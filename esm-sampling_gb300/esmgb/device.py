@@ -270,6 +270,13 @@ class DeviceChain:
         self._check(self.L.esm_move_log(self.h, int(cls), _p(out)), "esm_move_log")
         return out.reshape(nmoves, nsteps, self._mlog_nrep)
 
+    def storage_long_log(self, nunits):
+        """The move log of the last long-range storage sweep: [unit, move (5), replica], NaN where no
+        move was made."""
+        out = np.zeros(nunits * 5 * self._mlog_nrep)
+        self._check(self.L.esm_move_log(self.h, -1, _p(out)), "esm_move_log")
+        return out.reshape(nunits, 5, self._mlog_nrep)
+
     def set_sep_walk(self, min_units):
         """The cooperative walk for separable moves of at least min_units units (0: off)."""
         self._check(self.L.esm_set_sep_walk(self.h, int(min_units)), "esm_set_sep_walk")

@@ -261,7 +261,9 @@ int esm_move_grid(const esm_ctx *ctx, int32_t *warps_per_block, int32_t *warps_p
    of esm_class_pass records the t that each line move took for the replicas below nreps (device
    memory: moves x longest class x nreps doubles); 0 switches it off. esm_move_log copies the log of
    the last class pass, which must have been class cls, as [(move * nsteps + q) * nreps + replica]
-   for the class's q-th step (nsteps its steps); moves whose selection made no move read NaN. */
+   for the class's q-th step (nsteps its steps); moves whose selection made no move read NaN. With
+   cls = -1 it copies the log of the last esm_storage_long: [(unit * 5 + move) * nreps + replica]
+   over the sweep's eligible units in plan order (at most 5 moves each). */
 int esm_set_move_log(esm_ctx *ctx, int32_t nreps);
 int esm_move_log(esm_ctx *ctx, int32_t cls, double *out);
 

@@ -1289,7 +1289,45 @@ static bool prep_level(const Ctx &c, vector<WS> &wss, int j, int rep) {
     return true;
 }
 
-static void sl_sweep(Ctx &c, uint32_t sweep, int64_t *stats3, int nthreads) {
+// the moves [m0, m1) (m1 < 0: all) of one (unit, replica) task of the long-range storage sweep:
+// unit j (the ui-th eligible unit), its move list ms; tlog (may be NULL): the t of move mi at
+// [(ui * 5 + mi) * R + rep]
+static void sl_task(Ctx &c, uint32_t sweep, int ui, int j, int rep, const vector<SlMove> &ms, int m0, int m1,
+                    vector<WS> &wss, vector<Kink> &jac, int64_t *loc, double *tlog) {
+    const Model &m = c.m;
+    int T = m.T, R = c.o.R;
+    int mend = m1 < 0 ? (int)ms.size() : std::min(m1, (int)ms.size());
+    for (int mi = m0; mi < mend; ++mi) {
+        const SlMove &sm = ms[mi];
+        bool level = sm.L == T;
+        jac.clear();
+        if (level)
+            prep_level(c, wss, j, rep);
+        else if (!prep_plateau(c, wss, sm.a, sm.L, {j}, rep, &jac))
+            continue;
+        Mover mv{&c, {}, rep, m.beta_v, {}};
+        mv.cyclic = level;
+        int n = level ? T : sm.L + 1;
+        for (int k = 0; k < n; ++k) mv.w.push_back(&wss[k]);
+        double uc, uo, uj, un;
+        orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi, (uint32_t)j, (uint32_t)rep, sweep, &uc, &uo);
+        orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi + 1, (uint32_t)j, (uint32_t)rep, sweep, &uj, &un);
+        bool guard = false;
+        double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
+        if (guard) loc[2] += 1;
+        if (t != 0.0 && !jac.empty()) {
+            double lj = 0.0;
+            for (auto &kk : jac) lj += kk.nm * log(fabs((std::max(kk.Q + kk.g * t, 0.0) + kk.e) / kk.Pm));
+            if (uj >= exp(std::min(0.0, lj))) t = 0.0;
+        }
+        commit(c, mv, t);
+        if (tlog) tlog[((size_t)ui * 5 + mi) * R + rep] = t;
+        loc[0] += 1;
+        loc[1] += t != 0.0;
+    }
+}
+
+static void sl_sweep(Ctx &c, uint32_t sweep, int64_t *stats3, int nthreads, double *tlog = nullptr) {
     const Model &m = c.m;
     int T = m.T, R = c.o.R;
     vector<int> units;
@@ -1306,34 +1344,8 @@ static void sl_sweep(Ctx &c, uint32_t sweep, int64_t *stats3, int nthreads) {
         vector<Kink> jac;
 #pragma omp for schedule(dynamic, 1)
         for (int q = 0; q < nu * R; ++q) {
-            int ui = q / R, rep = q % R, j = units[ui];
-            for (size_t mi = 0; mi < moves[ui].size(); ++mi) {
-                const SlMove &sm = moves[ui][mi];
-                bool level = sm.L == T;
-                jac.clear();
-                if (level)
-                    prep_level(c, wss, j, rep);
-                else if (!prep_plateau(c, wss, sm.a, sm.L, {j}, rep, &jac))
-                    continue;
-                Mover mv{&c, {}, rep, m.beta_v, {}};
-                mv.cyclic = level;
-                int n = level ? T : sm.L + 1;
-                for (int k = 0; k < n; ++k) mv.w.push_back(&wss[k]);
-                double uc, uo, uj, un;
-                orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi, (uint32_t)j, (uint32_t)rep, sweep, &uc, &uo);
-                orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi + 1, (uint32_t)j, (uint32_t)rep, sweep, &uj, &un);
-                bool guard = false;
-                double t = sample_line(mv, c.o.maxnats, c.o.max_points, uc, uo, &guard);
-                if (guard) loc[2] += 1;
-                if (t != 0.0 && !jac.empty()) {
-                    double lj = 0.0;
-                    for (auto &kk : jac) lj += kk.nm * log(fabs((std::max(kk.Q + kk.g * t, 0.0) + kk.e) / kk.Pm));
-                    if (uj >= exp(std::min(0.0, lj))) t = 0.0;
-                }
-                commit(c, mv, t);
-                loc[0] += 1;
-                loc[1] += t != 0.0;
-            }
+            int ui = q / R, rep = q % R;
+            sl_task(c, sweep, ui, units[ui], rep, moves[ui], 0, -1, wss, jac, loc, tlog);
         }
         for (auto &w : wss) w.clear();
 #pragma omp critical
@@ -2013,6 +2025,69 @@ void orc_storage_long(void *p, int64_t sweep, int64_t *stats3, int nthreads) {
     sl_sweep(*(Ctx *)p, (uint32_t)sweep, stats3, nthreads);
 }
 
+// the same with the t of every move of the eligible units' tasks logged at [(ui * 5 + m) * R + rep]
+// (ui the unit's place among the eligible units, m its move; moves that made no move are left as
+// they are)
+void orc_storage_long_log(void *p, int64_t sweep, int64_t *stats3, int nthreads, double *tlog) {
+    sl_sweep(*(Ctx *)p, (uint32_t)sweep, stats3, nthreads, tlog);
+}
+
+// Moves [m0, m1) (m1 < 0: to the end) of one task of the long-range sweep: the ui-th eligible unit,
+// replica rep (no cache rebuild: call after a sweep or orc_rebuild). Returns the moves of its list.
+int orc_sl_task(void *p, int64_t sweep, int ui, int rep, int m0, int m1) {
+    Ctx &c = *(Ctx *)p;
+    vector<int> units;
+    vector<vector<SlMove>> moves;
+    sl_plan(c, (uint32_t)sweep, units, moves);
+    if (ui < 0 || ui >= (int)units.size() || rep < 0 || rep >= c.o.R) return -1;
+    vector<WS> wss(c.m.T);
+    for (auto &w : wss) w.init(c.m);
+    vector<Kink> jac;
+    int64_t loc[3] = {0, 0, 0};
+    if (!(m1 >= 0 && m1 <= m0)) sl_task(c, (uint32_t)sweep, ui, units[ui], rep, moves[ui], m0, m1, wss, jac, loc, nullptr);
+    return (int)moves[ui].size();
+}
+
+static void explain_mover(Ctx &c, Mover &mv, vector<Kink> &jac, bool compensated, double uc, double uo, double uj,
+                          double t_other, double *out);
+
+// orc_explain for move mi of the ui-th eligible unit's task (replica rep) of the long-range sweep on
+// the current state; out as orc_explain (16: -2 a level move, -3 a long-range plateau; 17: its
+// length). Returns 1, 0 when the move makes no move, -1 on a bad index.
+int orc_sl_explain(void *p, int64_t sweep, int ui, int rep, int mi, double t_other, double *out) {
+    Ctx &c = *(Ctx *)p;
+    const Model &m = c.m;
+    int T = m.T;
+    vector<int> units;
+    vector<vector<SlMove>> moves;
+    sl_plan(c, (uint32_t)sweep, units, moves);
+    if (ui < 0 || ui >= (int)units.size() || rep < 0 || rep >= c.o.R) return -1;
+    if (mi < 0 || mi >= (int)moves[ui].size()) return -1;
+    for (int i = 0; i < 24; ++i) out[i] = NAN;
+    vector<WS> wss(T);
+    for (auto &w : wss) w.init(m);
+    vector<Kink> jac;
+    int j = units[ui];
+    const SlMove &sm = moves[ui][mi];
+    bool level = sm.L == T;
+    if (level)
+        prep_level(c, wss, j, rep);
+    else if (!prep_plateau(c, wss, sm.a, sm.L, {j}, rep, &jac))
+        return 0;
+    Mover mv{&c, {}, rep, m.beta_v, {}};
+    mv.cyclic = level;
+    int n = level ? T : sm.L + 1;
+    for (int k = 0; k < n; ++k) mv.w.push_back(&wss[k]);
+    double uc, uo, uj, un;
+    orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi, (uint32_t)j, (uint32_t)rep, (uint32_t)sweep, &uc, &uo);
+    orc_uniform2(c.o.seed, ESM_TAG_SLL, 2u * (uint32_t)mi + 1, (uint32_t)j, (uint32_t)rep, (uint32_t)sweep, &uj, &un);
+    out[16] = level ? -2.0 : -3.0;
+    out[17] = sm.L;
+    explain_mover(c, mv, jac, !level, uc, uo, uj, t_other, out);
+    for (auto &w : wss) w.clear();
+    return 1;
+}
+
 // its plan: per eligible unit (stor index) its moves (length, start); returns the number of moves
 int orc_storage_long_plan(void *p, int64_t sweep, int32_t *out, int maxn) {
     Ctx *c = (Ctx *)p;
@@ -2160,6 +2235,111 @@ int orc_move_walk(void *p, int fam, int tau, int rep, int cls, int64_t sweep, do
 //   20/21 where the right and left walks began their ray steps (NaN: none), 22 |g L| of the drawn
 //   segment (the potential's change across it, nats), 23 its length L.
 // Returns 1, 0 when the selection made no move, -1 on a bad index.
+// the explanation of one prepared move (its Mover, Jacobian kinks and uniforms) for orc_explain and
+// orc_sl_explain: out[0..23] as orc_explain describes (16 and 17 are set by the caller)
+static void explain_mover(Ctx &c, Mover &mv, vector<Kink> &jac, bool compensated, double uc, double uo, double uj,
+                          double t_other, double *out) {
+    out[8] = uj;
+    vector<double> right, left;
+    for (const WS *w : mv.w)
+        for (double x : w->bps) {
+            if (!std::isfinite(x)) continue;
+            if (x > 0.0)
+                right.push_back(x);
+            else if (x < 0.0)
+                left.push_back(x);
+        }
+    mv.eval(0.0);
+    vector<double> sec0 = mv.sec;
+    Walk Wr, Wl;
+    Wr.cap = Wl.cap = c.o.max_points;
+    int okr = walk(Wr, mv, right, 1.0, c.o.maxnats, sec0);
+    int okl = okr && !Wr.full ? walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) : 0;
+    out[10] = Wr.stop;
+    out[11] = Wl.stop;
+    out[12] = Wr.near_;
+    out[13] = Wl.near_;
+    out[14] = (double)Wr.pts.size();
+    out[15] = (double)Wl.pts.size();
+    out[20] = Wr.ray_from;
+    out[21] = Wl.ray_from;
+    auto ljac = [&](double t) {
+        double lj = 0.0;
+        for (auto &k : jac) lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
+        return lj;
+    };
+    if (Wr.full || Wl.full) {
+        out[18] = 2;
+        out[0] = out[1] = 0.0;
+        return;
+    }
+    if (!okr || !okl) {
+        out[18] = 1;
+        out[0] = out[1] = 0.0;
+        return;
+    }
+    out[18] = 0;
+    vector<double> pts, cs;
+    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) {
+        pts.push_back(Wl.pts[j]);
+        cs.push_back(Wl.cs[j]);
+    }
+    pts.push_back(0.0);
+    cs.push_back(0.0);
+    pts.insert(pts.end(), Wr.pts.begin(), Wr.pts.end());
+    cs.insert(cs.end(), Wr.cs.begin(), Wr.cs.end());
+    int nseg = (int)pts.size() - 1;
+    vector<double> lm(nseg), A(nseg + 1, 0.0);
+    double mx = -INFINITY;
+    for (int j = 0; j < nseg; ++j) {
+        double L = pts[j + 1] - pts[j];
+        lm[j] = L > 0 ? -std::min(cs[j], cs[j + 1]) + logseg(L, fabs(cs[j + 1] - cs[j])) : -INFINITY;
+        mx = std::max(mx, lm[j]);
+    }
+    double tot = 0.0;
+    for (int j = 0; j < nseg; ++j) tot += exp(lm[j] - mx);
+    double u = uc * tot, acc = 0.0;
+    int jj = nseg - 1;
+    bool found = false;
+    for (int k = 0; k < nseg; ++k) {
+        acc += exp(lm[k] - mx);
+        A[k + 1] = acc;
+        if (!found && u <= acc) {
+            jj = k;
+            found = true;
+        }
+    }
+    double L = pts[jj + 1] - pts[jj];
+    double g = (cs[jj + 1] - cs[jj]) / L;
+    double t = (g >= 0 || fabs(g * L) < 1e-10) ? pts[jj] + trexp_offset(uo, g, L) : pts[jj + 1] - trexp_offset(uo, -g, L);
+    out[0] = t;
+    out[22] = fabs(g * L);
+    out[23] = L;
+    out[2] = nseg;
+    out[3] = jj;
+    out[19] = tot;
+    out[6] = std::min(u - A[jj], A[jj + 1] - u) / tot;
+    double t1 = t;
+    if (compensated && t != 0.0 && !jac.empty()) {
+        double lj = ljac(t);
+        out[7] = lj;
+        if (uj >= exp(std::min(0.0, lj))) t1 = 0.0;
+    }
+    out[1] = t1;
+    if (compensated && !jac.empty() && t_other != 0.0) out[9] = ljac(t_other);
+    int jo = -1;
+    if (t_other == 0.0)
+        jo = -2;
+    else
+        for (int j = 0; j < nseg; ++j)
+            if (pts[j] <= t_other && t_other <= pts[j + 1]) {
+                jo = j;
+                break;
+            }
+    out[4] = jo;
+    if (jo >= 0) out[5] = jo > jj ? (A[jo] - u) / tot : (jo < jj ? (u - A[jo + 1]) / tot : 0.0);
+}
+
 int orc_explain(void *p, int64_t sweep, int cls, int mi, int q, int rep, double t_other, double *out) {
     Ctx &c = *(Ctx *)p;
     const Model &m = c.m;
@@ -2206,106 +2386,8 @@ int orc_explain(void *p, int64_t sweep, int cls, int mi, int q, int rep, double 
     orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)tau, (uint32_t)rep, (uint32_t)sweep, &uc, &uo);
     orc_uniform2(c.o.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)tau, (uint32_t)rep, (uint32_t)sweep, &uj,
                  &un);
-    out[8] = uj;
-    vector<double> right, left;
-    for (const WS *w : mv.w)
-        for (double x : w->bps) {
-            if (!std::isfinite(x)) continue;
-            if (x > 0.0)
-                right.push_back(x);
-            else if (x < 0.0)
-                left.push_back(x);
-        }
-    mv.eval(0.0);
-    vector<double> sec0 = mv.sec;
-    Walk Wr, Wl;
-    Wr.cap = Wl.cap = c.o.max_points;
-    int okr = walk(Wr, mv, right, 1.0, c.o.maxnats, sec0);
-    int okl = okr && !Wr.full ? walk(Wl, mv, left, -1.0, c.o.maxnats, sec0) : 0;
-    out[10] = Wr.stop;
-    out[11] = Wl.stop;
-    out[12] = Wr.near_;
-    out[13] = Wl.near_;
-    out[14] = (double)Wr.pts.size();
-    out[15] = (double)Wl.pts.size();
-    out[20] = Wr.ray_from;
-    out[21] = Wl.ray_from;
-    auto ljac = [&](double t) {
-        double lj = 0.0;
-        for (auto &k : jac) lj += k.nm * log(fabs((std::max(k.Q + k.g * t, 0.0) + k.e) / k.Pm));
-        return lj;
-    };
-    if (Wr.full || Wl.full) {
-        out[18] = 2;
-        out[0] = out[1] = 0.0;
-        return 1;
-    }
-    if (!okr || !okl) {
-        out[18] = 1;
-        out[0] = out[1] = 0.0;
-        return 1;
-    }
-    out[18] = 0;
-    vector<double> pts, cs;
-    for (int j = (int)Wl.pts.size() - 1; j >= 0; --j) {
-        pts.push_back(Wl.pts[j]);
-        cs.push_back(Wl.cs[j]);
-    }
-    pts.push_back(0.0);
-    cs.push_back(0.0);
-    pts.insert(pts.end(), Wr.pts.begin(), Wr.pts.end());
-    cs.insert(cs.end(), Wr.cs.begin(), Wr.cs.end());
-    int nseg = (int)pts.size() - 1;
-    vector<double> lm(nseg), A(nseg + 1, 0.0);
-    double mx = -INFINITY;
-    for (int j = 0; j < nseg; ++j) {
-        double L = pts[j + 1] - pts[j];
-        lm[j] = L > 0 ? -std::min(cs[j], cs[j + 1]) + logseg(L, fabs(cs[j + 1] - cs[j])) : -INFINITY;
-        mx = std::max(mx, lm[j]);
-    }
-    double tot = 0.0;
-    for (int j = 0; j < nseg; ++j) tot += exp(lm[j] - mx);
-    double u = uc * tot, acc = 0.0;
-    int jj = nseg - 1;
-    bool found = false;
-    for (int k = 0; k < nseg; ++k) {
-        acc += exp(lm[k] - mx);
-        A[k + 1] = acc;
-        if (!found && u <= acc) {
-            jj = k;
-            found = true;
-        }
-    }
-    double L = pts[jj + 1] - pts[jj];
-    double g = (cs[jj + 1] - cs[jj]) / L;
-    double t = (g >= 0 || fabs(g * L) < 1e-10) ? pts[jj] + trexp_offset(uo, g, L) : pts[jj + 1] - trexp_offset(uo, -g, L);
-    out[0] = t;
-    out[22] = fabs(g * L);
-    out[23] = L;
-    out[2] = nseg;
-    out[3] = jj;
-    out[19] = tot;
-    out[6] = std::min(u - A[jj], A[jj + 1] - u) / tot;
     bool compensated = mr.kind == ESM_FAM_XLOCC || mr.kind == ESM_FAM_TPOT || mr.kind == ESM_FAM_TSOC;
-    double t1 = t;
-    if (compensated && t != 0.0 && !jac.empty()) {
-        double lj = ljac(t);
-        out[7] = lj;
-        if (uj >= exp(std::min(0.0, lj))) t1 = 0.0;
-    }
-    out[1] = t1;
-    if (compensated && !jac.empty() && t_other != 0.0) out[9] = ljac(t_other);
-    int jo = -1;
-    if (t_other == 0.0)
-        jo = -2;
-    else
-        for (int j = 0; j < nseg; ++j)
-            if (pts[j] <= t_other && t_other <= pts[j + 1]) {
-                jo = j;
-                break;
-            }
-    out[4] = jo;
-    if (jo >= 0) out[5] = jo > jj ? (A[jo] - u) / tot : (jo < jj ? (u - A[jo + 1]) / tot : 0.0);
+    explain_mover(c, mv, jac, compensated, uc, uo, uj, t_other, out);
     return 1;
 }
 

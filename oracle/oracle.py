@@ -66,6 +66,11 @@ def lib():
         L.orc_storage_long_plan.restype = C.c_int
         L.orc_sweeps.argtypes = [C.c_void_p, C.c_int, C.c_int64, P_i64, C.c_int]
         L.orc_class_pass_range.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, P_i64, C.c_int, P_f64]
+        L.orc_storage_long_log.argtypes = [C.c_void_p, C.c_int64, P_i64, C.c_int, P_f64]
+        L.orc_sl_task.restype = C.c_int
+        L.orc_sl_task.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_sl_explain.restype = C.c_int
+        L.orc_sl_explain.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, P_f64]
         L.orc_task_moves.restype = C.c_int
         L.orc_task_moves.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_explain.restype = C.c_int
@@ -227,6 +232,28 @@ class Oracle:
         st = np.zeros(3, np.int64)
         lib().orc_storage_long(self.h, sweep, _p(st, P_i64), self.threads)
         return st
+
+    def storage_long_log(self, sweep, tlog):
+        """The long-range storage sweep with the t of every move logged into tlog (float64 [units,
+        5, R], the sweep's eligible units in plan order); returns (tried, taken, guards)."""
+        st = np.zeros(3, np.int64)
+        lib().orc_storage_long_log(self.h, sweep, _p(st, P_i64), self.threads, tlog.ctypes.data_as(P_f64))
+        return st
+
+    def sl_task(self, sweep, ui, rep, m0, m1):
+        """Moves [m0, m1) (m1 < 0: to the end) of the long-range task of eligible unit ui, replica rep."""
+        n = lib().orc_sl_task(self.h, sweep, ui, rep, m0, m1)
+        if n < 0:
+            raise ValueError("orc_sl_task: bad index")
+        return n
+
+    def sl_explain(self, sweep, ui, rep, mi, t_other):
+        """Oracle.explain for move mi of the long-range task of eligible unit ui, replica rep."""
+        out = np.zeros(24)
+        rc = lib().orc_sl_explain(self.h, sweep, ui, rep, mi, float(t_other), _p(out))
+        if rc < 0:
+            raise ValueError("orc_sl_explain: bad index")
+        return dict(zip(self.EXPLAIN, out.tolist())) if rc else None
 
     def storage_long_plan(self, sweep, maxn=4096):
         """Its moves: [(unit, length, start)] (length T: the level move)."""

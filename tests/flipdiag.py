@@ -10,10 +10,15 @@ boundary:
   jacobian  the accept test of a compensated move: |u_j - exp(min(0, log J))|;
   stop      where a walk stops (c - cmin - maxnats at a primary breakpoint), over maxnats;
   offset    the same segment with another offset: the continuous map from u_off to t within the
-            segment carries the round-off of the segment's end points (margin |t_dev - t| / L),
-            and the FP32 build draws a segment whose potential changes by less than its round-off
-            scale (about 1e-3 nats on storage moves) uniformly where the oracle draws the truncated
-            exponential (margin 0 when |g L| is below 1e-2 nats in FP32);
+            segment carries the round-off of the segment's end points (margin |t_dev - t| / L);
+            a segment flat to round-off (|g L| below 1e-8 nats in FP64, 1e-2 in FP32) has margin 0:
+            there trexp_offset (src/local.jl:1106) draws from the left end (u L) when |g L| is below
+            its threshold or g >= 0, and from the right end ((1 - u) L) otherwise, so the round-off
+            sign of g picks the mirrored map -- both exact draws of the uniform conditional. Flat
+            segments are exact where a move changes no term (a level move of the long-range storage
+            sweep while every state stays inside the box), and a year-long move's potential carries
+            round-off near the threshold's 1e-10 nats; the FP32 build also draws segments flat to
+            its round-off scale (about 1e-3 nats on storage moves) uniformly;
   ray       (FP32 only) one of the two draws lies where its walk took ray steps, past every primary
             breakpoint: the FP32 build probes the ray slope 1e-3 ahead instead of 1e-6, so its ray
             points, and with them the map from the uniforms to t, differ there while the potential
@@ -45,10 +50,14 @@ def in_ray(e, t):
 
 
 def classify(e, maxnats, fp32=False):
-    """(kind, margin) of one explained flip (the smallest margin among the choices that apply)."""
+    """(kind, margin) of one explained flip: the same segment is an offset; otherwise the smallest
+    margin among the discrete choices that apply."""
     cands = []
     if fp32 and (in_ray(e, e["t"]) or in_ray(e, e["t_dev"])):
         return ("ray", 0.0)
+    if e["seg_other"] == e["seg"]:
+        flat = abs(e["gL"]) <= (1e-2 if fp32 else 1e-8)
+        return ("offset", 0.0 if flat else abs(e["t_dev"] - e["t"]) / max(e["L"], 1e-300))
     if e["seg_other"] >= 0 and e["seg_other"] != e["seg"]:
         cands.append(("segment", abs(e["cat_margin"])))
     for key in ("lj", "lj_other"):
@@ -57,9 +66,6 @@ def classify(e, maxnats, fp32=False):
     for key in ("stop_r", "stop_l", "near_r", "near_l"):
         if np.isfinite(e[key]):
             cands.append(("stop", abs(e[key]) / maxnats))
-    if e["seg_other"] == e["seg"]:
-        flat = fp32 and abs(e["gL"]) <= 1e-2
-        cands.append(("offset", 0.0 if flat else abs(e["t_dev"] - e["t"]) / max(e["L"], 1e-300)))
     if not cands:
         return ("unknown", np.inf)
     return min(cands, key=lambda x: x[1])

@@ -93,7 +93,8 @@ def test_operation_sweeps_with_storage(state):
 def test_storage_long_sweep(state, prec, tol, maxflip):
     """The long-range storage sweep (storage_long_sweep!, src/storage_long.jl:245): every eligible
     unit's level move and long-range plateaus; parity per (unit, replica) task over the year (5 moves
-    per task, each over up to the whole year: measured 1.8 % FP64, 1.2 % FP32 tasks flipped)."""
+    per task, each over up to the whole year: measured 1.8 % FP64, 1.2 % FP32 tasks flipped; the FP64
+    flips are mirrored draws on segments flat to round-off, test_storage_long_flips_explained)."""
     m, st = state
     d = DeviceChain(m, 32, precision=prec, seed=5)
     d.upload(st)
@@ -114,3 +115,50 @@ def test_storage_long_sweep(state, prec, tol, maxflip):
         ok = de <= tol
         dg = np.abs(a["g"] - b["g"]).max()
         assert ok.all() or dg > 0  # (the dispatch follows the flipped tasks only)
+
+
+def test_storage_long_flips_explained(state):
+    """Each (unit, replica) task of the FP64 long-range sweep whose draws differ from the oracle's,
+    explained at its first differing move (tests/flipdiag.py): the discrete choice there and how near
+    its boundary the oracle's own draw was. Every one is a round-off flip: within 1e-8 of a segment,
+    stop or Jacobian boundary, or the same segment with an offset within 1e-6 of its length, or a
+    segment flat to round-off drawn from the other end (measured: these mirrored draws on flat
+    segments of level moves and long plateaus, |g L| about 1e-10 nats, make up the flipped tasks)."""
+    from flipdiag import classify, first_diffs, summary
+    m, st = state
+    R = 32
+    d = DeviceChain(m, R, precision=64, seed=5)
+    d.upload(st)
+    d.set_move_log(R)
+    o = Oracle(m, R, seed=5)
+    o.set_state(st)
+    plan = o.storage_long_plan(9)
+    order = []
+    for u, _, _ in plan:
+        if u not in order:
+            order.append(u)
+    nu = len(order)
+    d.storage_long(9)
+    tdev = d.storage_long_log(nu)                       # [unit, move, replica]
+    tlog = np.full((nu, 5, R), np.nan)
+    o.storage_long_log(9, tlog)
+    first = first_diffs(tdev.transpose(1, 0, 2), tlog.transpose(1, 0, 2), 1e-9, 1e-12)   # [unit, replica]
+    o2 = Oracle(m, R, seed=5)
+    o2.set_state(st)
+    o2.rebuild()
+    flips = []
+    for ui, rep in zip(*np.nonzero(first >= 0)):
+        mi = int(first[ui, rep])
+        o2.sl_task(9, int(ui), int(rep), 0, mi)
+        e = o2.sl_explain(9, int(ui), int(rep), mi, float(np.nan_to_num(tdev[ui, mi, rep])))
+        assert e is not None
+        e["t_dev"] = float(tdev[ui, mi, rep])
+        kind, margin = classify(e, 40.0)
+        flips.append(dict(unit=int(ui), rep=int(rep), move=mi, kind=kind, margin=margin, **e))
+    print(f"storage_long FP64: {nu} units x {R} replicas, tasks with a differing draw {(first >= 0).mean():.4f};",
+          "by kind (count, largest margin):", summary(flips))
+    for f in sorted(flips, key=lambda f: -f["margin"])[:6]:
+        print({k: f[k] for k in ("unit", "rep", "move", "kind", "margin", "fam", "entries", "t", "t_dev", "seg",
+                                 "seg_other", "nseg", "npts_r", "npts_l", "gL", "L")})
+    d.set_move_log(0)
+    assert all(f["margin"] <= (1e-6 if f["kind"] == "offset" else 1e-8) for f in flips), summary(flips)
