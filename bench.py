@@ -151,6 +151,102 @@ def e2e_loop(d, m, ctl, R_set, it0, n, rng):
     return h2d / n, d2h / n
 
 
+def carrier_totals(m, k):
+    """ktot (src/replicas.jl:812): the capacity of every carrier, summed over its units."""
+    return np.bincount(np.asarray(m.unit_group), weights=np.asarray(k, float), minlength=len(m.carriers))
+
+
+def capacity_ess(m, kt, seconds):
+    """The metric's capacity ESS/s: the bulk ESS (src/convergence.jl:125) of every carrier total over
+    the steps of one chain, the smallest over carriers, per wall second; with the relative MCSE of
+    each carrier's mean (src/convergence.jl:141)."""
+    from esmgb.convergence import ess_bulk, mcse_rel
+    kt = np.asarray(kt)
+    ess, mcse = {}, {}
+    for i, c in enumerate(m.carriers):
+        x = kt[:, i]
+        if not np.all(np.isfinite(x)) or np.ptp(x) == 0:   # a carrier that did not move has no samples
+            ess[c], mcse[c] = 0.0, float("inf")
+        else:
+            ess[c], mcse[c] = float(ess_bulk([x])), float(mcse_rel([x]))
+    worst = min(ess, key=ess.get)
+    w = np.log(np.maximum(kt, 1e-300))
+    msjd = float(np.mean(np.sum(np.diff(w, axis=0) ** 2, axis=1))) if len(kt) > 1 else 0.0
+    return {"value": ess[worst] / seconds, "unit": "ESS/s", "ess_min": ess[worst], "carrier": worst,
+            "steps": len(kt), "seconds": seconds, "ess": ess, "mcse_rel": mcse,
+            "msjd_log_ktot_per_step": msjd}
+
+
+def ess_arms(d, m, ctl, it0, n, arms=("plain", "learned", "da")):
+    """Capacity ESS/s of the plain replica step and of the learned capacity steps over n steps each,
+    every arm from the same saved chain state and over the same weather schedule; each step is one
+    plain evaluation (an operation sweep and the scores). The learned arms use the surrogate of the
+    learned-proposal configuration: 3 hidden layers of 512, minibatches of 1024, Adam at 1e-3, 4x the
+    plain step; it is trained on the plain arm's pairs before its arms (not timed) and online during
+    them.
+      plain    the device Langevin step on the replica-averaged score (replica_step!, src/replicas.jl:676)
+      learned  SurrogateLangevin: the surrogate's drift at 4x the plain step, judged by the plain scores
+      da       DALangevin: 4x proposals, delayed acceptance with the plain estimate as second stage"""
+    from esmgb.surrogate import DALangevin, ScoreSurrogate, SurrogateLangevin
+    eta, ks = carrier_params(m)
+    w = np.full(d.R, 1.0 / d.R)
+    rng = np.random.Generator(np.random.PCG64(99))
+    sched = [schedule(ctl, it0 + q, d.R, rng) for q in range(n)]
+    d.sync(600.0)
+    d.state_save()
+    out = {}
+    pairs = []
+    k = d.download_k()
+    occ = d.regime_occupancy()
+    kt = []
+    t0 = time.perf_counter()
+    for q in range(n):
+        moved, theta, window, wstart, _ = sched[q]
+        if moved.any():
+            d.weather_step(moved, theta, window, wstart, it=it0 + q)
+            occ = d.regime_occupancy()
+        d.sweeps(1, sweep0=it0 + q, stats=False)
+        sk, _, _ = d.scores()
+        pairs.append((k, occ, w @ sk))
+        k, _ = d.langevin_step(w, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it0 + q)
+        kt.append(carrier_totals(m, k))
+    d.sync(600.0)
+    out["plain"] = capacity_ess(m, kt, time.perf_counter() - t0)
+    learned = [a for a in arms if a != "plain"]
+    if not learned:
+        d.state_restore()
+        return out
+    sur = ScoreSurrogate(m, hidden=(512, 512, 512), capacity=8192, batch=1024, lr=1e-3, seed=1,
+                         min_pairs=min(16, n))
+    for kk, oc, sb in pairs:
+        sur.add(kk, oc, sb)
+    sur.train(200)
+    for arm in learned:
+        d.state_restore()
+        if arm == "learned":
+            stepper = SurrogateLangevin(d, m, sur, eta, ks, ctl.kappa_min, ctl.clip, mult=4.0, seed=3)
+        else:
+            stepper = DALangevin(d, m, sur, eta, ks, ctl.kappa_min, ctl.clip, mult=4.0, seed=3)
+        kt = []
+        t0 = time.perf_counter()
+        for q in range(n):
+            if arm == "learned":
+                stepper.step(it0 + q, sched[q])
+            else:
+                moved, theta, window, wstart, _ = sched[q]
+                if moved.any():
+                    d.weather_step(moved, theta, window, wstart, it=it0 + q)
+                stepper.step(it0 + q)
+            kt.append(carrier_totals(m, stepper.k))
+        d.sync(600.0)
+        out[arm] = capacity_ess(m, kt, time.perf_counter() - t0)
+        out[arm]["stats"] = dict(stepper.stats)
+        out[arm]["ratio_to_plain"] = out[arm]["value"] / out["plain"]["value"]
+    sur.close()
+    d.state_restore()
+    return out
+
+
 def cpu_sample(threads, sweeps=1, R=2, storage_ms=0):
     """The oracle on the host cores: operation sweeps from sweep 1 and the scores of R of the
     replicas; with storage_ms, two sweeps (the storage multiscale sweep runs in sweep 1, not in 2:
@@ -328,6 +424,9 @@ def main():
     ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--ess-steps", type=int, default=32,
+                    help="steps of each arm of the capacity ESS/s measurement (plain, learned, delayed "
+                         "acceptance); 0: none")
     ap.add_argument("--storage-ms", action="store_true",
                     help="operation sweeps include the storage sweeps: multiscale (probability 1/2) and long-range")
     ap.add_argument("--autotune", action="store_true", help="--case small: the autotuner picks the line-move grid")
@@ -410,6 +509,8 @@ def main():
     sl = d.storage_long(it0 + args.warmup + 2 * args.steps)
     d.sync(600.0)
     sl_ms = d.timing()["storage"][0]
+    d.set_timing(False)
+    ess = ess_arms(d, m, ctl, it0 + args.warmup + 2 * args.steps + 1, args.ess_steps) if args.ess_steps > 0 else None
     if rank != 0:
         return
     # roofline of the dominant kernels (one colour class: k_prep_moves and one k_move launch per
@@ -452,6 +553,17 @@ def main():
                              "note": "long-range storage sweep timed alone; every operation sweep with "
                                      "--storage-ms"},
             "wall_device_loop_s": wall_dev}
+    if ess:
+        line["capacity_ess_per_s"] = {
+            "plain": ess["plain"]["value"], "learned": ess.get("learned", {}).get("value"),
+            "delayed_acceptance": ess.get("da", {}).get("value"),
+            "learned_over_plain": ess.get("learned", {}).get("ratio_to_plain"),
+            "delayed_acceptance_over_plain": ess.get("da", {}).get("ratio_to_plain"),
+            "steps_per_arm": args.ess_steps, "unit": "ESS/s",
+            "note": ("min over carriers of the bulk ESS of the carrier totals per wall second, each arm from the same "
+                     "chain state (after the timed and end-to-end steps) over the same weather schedule; "
+                     "short chains: the ESS is of the steps measured, with the per-carrier detail below"),
+            "detail": ess}
     if not args.no_cpu_baseline:
         try:
             from oracle import oracle as O

@@ -56,6 +56,8 @@ struct esm_ctx {
     // (0: off), its grid and where its per-warp walk buffers live
     int sep_min = ESM_SEP_MIN_DEFAULT, sep_max_warps = 0, sep_in_smem = 1;
     int sl_nunits = 0;  // eligible units of the last long-range storage sweep (its move log)
+    int device = -1;                   // the device the context was created on
+    double *score_scratch = nullptr;   // device address of the static score scratch on that device
     char *d_sep_slab = nullptr;
     int warps_cap[3] = {0, 0, 0};  // the resident limit per block shape (1, 2, 4 warps per block)
     int nsm = 0;
@@ -75,6 +77,7 @@ struct esm_ctx {
     double *d_lo = nullptr, *d_hi = nullptr, *d_capex = nullptr;
     double *d_k = nullptr, *d_kold = nullptr, *d_knew = nullptr, *d_k1 = nullptr, *d_kmid = nullptr;
     double *d_dk = nullptr, *d_sk = nullptr, *d_fk = nullptr, *d_parts = nullptr;
+    double *d_score_part = nullptr;  // the chunk partials of the fused score pass
     double *d_w = nullptr, *d_eta = nullptr, *d_kappa = nullptr, *d_xi = nullptr;
     int *d_nclip = nullptr;
     unsigned long long *d_stats = nullptr;
@@ -513,25 +516,18 @@ int alloc_state(esm_ctx *c) {
     return ESM_OK;
 }
 
-// FP32 build: an FP64 copy of the state (fields and weather) and its caches. The capacity scores
-// weigh every node balance by the shed or the dump price according to its sign, and near equilibrium
-// many balances sit within FP32 round-off of zero: the scores are therefore computed in FP64 on the
-// widened FP32 state, with the FP64 parameters, as the FP64 build computes them.
+// FP32 build: the FP64 clamped capacities of the FP64 model (its tables and parameters) that the
+// capacity scores are computed with. The scores weigh every node balance by the shed or the dump
+// price according to its sign, and near equilibrium many balances sit within FP32 round-off of zero:
+// the fused score pass therefore forms every balance and term in FP64 from the FP32 state.
 int alloc_shadow(esm_ctx *c) {
     esm::DevModel<double> &M = c->Md;
-    size_t TR = (size_t)M.T * M.R;
     double *p;
     int rc;
 #define AL(field, n)                       \
     if ((rc = dalloc(c, &p, (size_t)(n)))) \
         return rc;                         \
     M.field = p;
-    AL(theta, M.N * TR);
-    AL(g, M.D * TR);
-    AL(e, M.S * TR);
-    AL(r, M.N * TR);
-    AL(F, M.L * TR);
-    AL(z, M.n0 * TR);
     AL(kc_d, M.D);
     AL(kc_s, M.S);
     AL(kc_r, std::max(M.Nren, 1));
@@ -539,30 +535,23 @@ int alloc_shadow(esm_ctx *c) {
     return ESM_OK;
 }
 
-__global__ void k_widen(size_t n, const float *a, double *b) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        b[i] = (double)a[i];
-}
-
-int widen_state(esm_ctx *c) {
-    const esm::DevModel<float> &A = c->Mf;
-    esm::DevModel<double> &B = c->Md;
-    size_t TR = (size_t)A.T * A.R;
-    struct {
-        const float *a;
-        double *b;
-        size_t n;
-    } v[4] = {{A.theta, B.theta, A.N * TR}, {A.g, B.g, A.D * TR}, {A.e, B.e, A.S * TR}, {A.z, B.z, A.n0 * TR}};
-    for (auto &x : v) {
-        if (x.n == 0) continue;
-        k_widen<<<(unsigned)std::min<size_t>((x.n + 255) / 256, 152 * 16), 256, 0, c->stream>>>(x.n, x.a, x.b);
-        CK(cudaGetLastError());
+// the capacity scores of the current state: the fused pass (partials in `partial`, sums in dk and
+// parts) and the finish into the context's sk and fk
+int scores_any(esm_ctx *c, double *partial, double *dk, double *parts) {
+    Span sp(c, ESM_KT_SCORE);
+    if (c->precision == 64) {
+        CK(esm::launch_scores_fused<double>(c->Md, c->Md.theta, c->Md.g, c->Md.e, c->Md.z, partial, dk, parts,
+                                            c->stream));
+    } else {
+        CK(esm::launch_set_kc<double>(c->K, c->d_k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (double *)c->Md.kc_d,
+                                      (double *)c->Md.kc_s, (double *)c->Md.kc_r, c->stream));
+        CK(esm::launch_scores_fused<float>(c->Md, c->Mf.theta, c->Mf.g, c->Mf.e, c->Mf.z, partial, dk, parts,
+                                           c->stream));
         c->launches += 1;
     }
-    CK(esm::launch_set_kc<double>(c->K, c->d_k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (double *)B.kc_d,
-                                  (double *)B.kc_s, (double *)B.kc_r, c->stream));
-    CK(esm::launch_rebuild<double>(B, c->stream));
-    c->launches += 2;
+    CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
+                                        c->physical, dk, c->d_sk, c->d_fk, parts, c->stream));
+    c->launches += 3;
     return ESM_OK;
 }
 
@@ -683,6 +672,10 @@ int stats_out(esm_ctx *c, int64_t *stats) {
 // =============================================================================================
 extern "C" {
 
+namespace {
+int static_scores_setup(esm_ctx *c);
+}
+
 int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     if (!out) return ESM_EINVAL;
     *out = nullptr;
@@ -778,6 +771,7 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         if ((rc = dalloc(c, &dp, K))) return rc;
         *pp = dp;
     }
+    if ((rc = dalloc(c, &c->d_score_part, esm::score_partial_doubles(c->T, c->R, c->K, c->N)))) return rc;
     for (double **pp : {&c->d_dk, &c->d_sk}) {
         if ((rc = dalloc(c, &dp, (size_t)c->R * K))) return rc;
         *pp = dp;
@@ -823,6 +817,7 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
             return fail(c, prc, "probe context: %s", msg.c_str());
         }
     }
+    if ((rc = static_scores_setup(c))) return rc;
     return ESM_OK;
 }
 
@@ -1132,24 +1127,8 @@ int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) 
 int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
     if (!c) return ESM_EINVAL;
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
-    int rc = rebuild_any(c);
+    int rc = scores_any(c, c->d_score_part, c->d_dk, c->d_parts);
     if (rc) return rc;
-    CK(cudaMemsetAsync(c->d_dk, 0, sizeof(double) * c->R * c->K, c->stream));
-    CK(cudaMemsetAsync(c->d_parts, 0, sizeof(double) * c->R * 8, c->stream));
-    {
-    Span sp(c, ESM_KT_SCORE);
-    if (c->precision == 64) {
-        CK(esm::launch_scores<double>(c->Md, c->d_dk, c->d_parts, c->stream));
-        CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
-                                            c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
-    } else {
-        if ((rc = widen_state(c))) return rc;
-        CK(esm::launch_scores<double>(c->Md, c->d_dk, c->d_parts, c->stream));
-        CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
-                                            c->physical, c->d_dk, c->d_sk, c->d_fk, c->d_parts, c->stream));
-    }
-    }
-    c->launches += 2;
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * c->R * c->K, cudaMemcpyDeviceToHost, c->stream));
     if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
     if (parts) CK(cudaMemcpyAsync(parts, c->d_parts, sizeof(double) * c->R * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1198,60 +1177,51 @@ int follow_any(esm_ctx *c, double kappa_min) {
 // device -- and a caller whose step must not stall, as cudaMalloc/cudaFree can synchronise the
 // device. The score accumulators (the R x K score sums and the R x 8 cost parts) live in one
 // file-scope device array instead of buffers of the context.
-//   Limit: R * (K + 8) <= ESM_SCORE_SCRATCH_DOUBLES (8 MiB); larger contexts get ESM_EINVAL.
-//   Set-up: the first call on a device, with that device current, resolves the array's address
-//   (cudaGetSymbolAddress) once; make it before any stream capture. The first call on a context
-//   also reserves that context's error-message buffer.
+//   Limit: the fused pass's chunk partials (esm::score_partial_doubles, which takes fewer chunks to
+//   fit) and the R * (K + 8) sums within ESM_SCORE_SCRATCH_DOUBLES (8 MiB); larger contexts get
+//   ESM_EINVAL.
+//   Set-up: esm_create, which allocates anyway, resolves the array's address on the context's
+//   device (cudaGetSymbolAddress, with that device current) and loads the score kernels, so the
+//   call itself places nothing on the device. The call must be made with the context's device
+//   current (else ESM_EINVAL). A cudaDeviceReset ends the contexts on that device, and with them
+//   the addresses they hold.
 //   The array is shared by every context on the device: overlapping calls (two streams, two
 //   threads, two contexts) race on it and must be serialised by the caller.
 // ---------------------------------------------------------------------------------------------
 static __device__ __align__(256) double g_score_scratch[ESM_SCORE_SCRATCH_DOUBLES];
 
 namespace {
-std::mutex g_scratch_mu;
-double *g_scratch_dev[ESM_MAX_DEVICES] = {};
-
-int score_scratch(esm_ctx *c, double **out) {
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= ESM_MAX_DEVICES) return fail(c, ESM_EINVAL, "device %d beyond %d", dev, ESM_MAX_DEVICES);
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_dev[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_score_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(c, ESM_ECUDA, "cudaGetSymbolAddress of the score scratch: %s", cudaGetErrorString(e));
-        g_scratch_dev[dev] = (double *)p;
-    }
-    *out = g_scratch_dev[dev];
+// esm_create's set-up of the static score path: the context's device, the scratch array's address
+// there, the kernels of the path loaded and the error buffer reserved
+int static_scores_setup(esm_ctx *c) {
+    CK(cudaGetDevice(&c->device));
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_score_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(c, ESM_ECUDA, "cudaGetSymbolAddress of the score scratch: %s", cudaGetErrorString(e));
+    c->score_scratch = (double *)p;
+    CK(esm::preload_score_kernels());
+    c->err.reserve(512);
     return ESM_OK;
 }
 }  // namespace
 
 int esm_capacity_scores_static(esm_ctx *c, double *sk, double *fk, double *parts) {
     if (!c) return ESM_EINVAL;
-    if (c->err.capacity() < 512) c->err.reserve(512);
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
-    size_t R = c->R, K = c->K, need = R * (K + 8);
+    size_t R = c->R, K = c->K;
+    size_t npart = esm::score_partial_doubles(c->T, c->R, c->K, c->N), need = npart + R * (K + 8);
     if (need > (size_t)ESM_SCORE_SCRATCH_DOUBLES)
-        return fail(c, ESM_EINVAL, "R*(K+8) = %zu doubles of score scratch needed, the static scratch holds %d",
-                    need, ESM_SCORE_SCRATCH_DOUBLES);
-    double *dk = nullptr;
-    int rc = score_scratch(c, &dk);
-    if (rc) return rc;
-    double *pd = dk + R * K;
-    if (c->precision == 64) {
-        CK(esm::launch_rebuild<double>(c->Md, c->stream));
-    } else {
-        CK(esm::launch_rebuild<float>(c->Mf, c->stream));
-        if ((rc = widen_state(c))) return rc;
-    }
-    // the accumulators start at zero (the score kernel adds into them)
-    CK(cudaMemsetAsync(dk, 0, sizeof(double) * need, c->stream));
-    CK(esm::launch_scores<double>(c->Md, dk, pd, c->stream));
-    CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
-                                        c->physical, dk, c->d_sk, c->d_fk, pd, c->stream));
-    c->launches += 3;
+        return fail(c, ESM_EINVAL, "%zu doubles of score scratch needed (R*(K+8) = %zu), the static scratch holds %d",
+                    need, R * (K + 8), ESM_SCORE_SCRATCH_DOUBLES);
+    int dev = -1, rc;
+    CK(cudaGetDevice(&dev));
+    if (dev != c->device || !c->score_scratch)
+        return fail(c, ESM_EINVAL, "device %d is current, the context was created on device %d", dev, c->device);
+    // the partials, then the summed gradient and the cost parts; every element is written by the
+    // pass before it is read, so nothing carries over from an earlier call
+    double *part = c->score_scratch, *dk = part + npart, *pd = dk + R * K;
+    if ((rc = scores_any(c, part, dk, pd))) return rc;
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * R * K, cudaMemcpyDeviceToHost, c->stream));
     if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
     if (parts) CK(cudaMemcpyAsync(parts, pd, sizeof(double) * R * 8, cudaMemcpyDeviceToHost, c->stream));

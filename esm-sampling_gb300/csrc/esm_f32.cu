@@ -20,7 +20,6 @@ template size_t sep_region_bytes<float>(const DevModel<float> &);
 template int sep_warps_per_sm<float>(const DevModel<float> &, int *);
 template int linemove_blocks_per_sm<float>(const DevModel<float> &, int);
 template cudaError_t launch_rebuild<float>(const DevModel<float> &, cudaStream_t);
-template cudaError_t launch_scores<float>(const DevModel<float> &, double *, double *, cudaStream_t);
 template cudaError_t launch_score_finish<float>(const DevModel<float> &, const double *, const double *, const double *,
                                                 const double *, double, double, int, double *, double *, double *,
                                                 double *, cudaStream_t);

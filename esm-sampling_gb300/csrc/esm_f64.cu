@@ -5,6 +5,20 @@
 #include "esm_plateau.cuh"
 
 namespace esm {
+template cudaError_t launch_scores_fused<float>(const DevModel<double> &, const float *, const float *, const float *,
+                                                const float *, double *, double *, double *, cudaStream_t);
+template cudaError_t launch_scores_fused<double>(const DevModel<double> &, const double *, const double *,
+                                                 const double *, const double *, double *, double *, double *,
+                                                 cudaStream_t);
+cudaError_t preload_score_kernels() {
+    cudaFuncAttributes a;
+    cudaError_t e;
+    if ((e = cudaFuncGetAttributes(&a, k_scores_fused<float>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&a, k_scores_fused<double>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&a, k_score_reduce)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&a, k_score_finish<double>)) != cudaSuccess) return e;
+    return cudaFuncGetAttributes(&a, k_set_kc<double>);
+}
 template int plateau_threads<double>(const DevModel<double> &);
 template size_t plateau_scratch_reals<double>(const DevModel<double> &);
 template cudaError_t launch_plateau<double>(const DevModel<double> &, const PlatMoves &, uint32_t, double *, int,
@@ -20,7 +34,6 @@ template size_t sep_region_bytes<double>(const DevModel<double> &);
 template int sep_warps_per_sm<double>(const DevModel<double> &, int *);
 template int linemove_blocks_per_sm<double>(const DevModel<double> &, int);
 template cudaError_t launch_rebuild<double>(const DevModel<double> &, cudaStream_t);
-template cudaError_t launch_scores<double>(const DevModel<double> &, double *, double *, cudaStream_t);
 template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *, const double *,
                                                 const double *, double, double, int, double *, double *, double *,
                                                 double *, cudaStream_t);

@@ -76,104 +76,167 @@ __global__ void k_rebuild(DevModel<real> M) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// energy cost and capacity gradient (src/energy.jl:551-757: gen_grad :835, soc_grad :466), per
-// (node, step chunk, replica), partial sums in FP64 added atomically per (replica, unit).
-// acc layout: dk [R*K], then parts [R*8] (capex, op, gen, storage, shed, dump, penalty, -)
+// Energy cost and capacity gradient (src/energy.jl:551-757: gen_grad :835, soc_grad :466) in one
+// pass over the state, whatever its precision: the state S
+// (the FP32 production state or the FP64 parity state) is read and every term is formed in FP64
+// with the FP64 parameters of M -- the residual of every (node, step) and the flows of its lines
+// by the rebuild's arithmetic (k_rebuild, in its order), then the terms of k_scores -- so no cache
+// and no FP64 copy of the state is read. Thread (replica lane, node slot) of block (replica tile,
+// node group of ESM_SCORE_NSLOT nodes, step chunk) sums its node's terms over the chunk's steps in
+// FP64. Every (chunk, replica, unit) partial of the gradient has one writer (the thread of the
+// unit's node); the cost parts are summed over the block's node slots in slot order. k_score_reduce
+// sums the chunks in chunk order: the scores are the same from run to run, bit for bit.
+//   dkp [nchunk][R][K]; pp [nchunk][ngroups][R][5]: gen, storage, shed, dump, penalty
 // ---------------------------------------------------------------------------------------------
-template <class real>
-__global__ void k_scores(DevModel<real> M, int tchunk, double *dk_out, double *parts_out) {
-    int n = blockIdx.x;
-    int c = blockIdx.y;
-    int rep = blockIdx.z * blockDim.x + threadIdx.x;
-    if (rep >= M.R) return;
-    int T = M.T, R = M.R;
-    int t0 = c * tchunk, t1 = min(T, t0 + tchunk);
-    real dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
-    const int MAXU = 8;
-    double dk[MAXU];
-    double dkbox[MAXU];
-    int nu = M.nu_ptr[n + 1] - M.nu_ptr[n];
-    for (int q = 0; q < MAXU; ++q) dk[q] = dkbox[q] = 0;
-    double cgen = 0, cst = 0, pen = 0, shed = 0, dump = 0;
-    for (int t = t0; t < t1; ++t) {
-        real rr = M.r[sidx(n, t, rep, T, R)];
-        real Gn = dt * (rr > 0 ? M.c_shed : (rr < 0 ? -M.c_dump : real(0)));
-        if (rr > 0)
-            shed += (double)(dt * rr);
-        else
-            dump -= (double)(dt * rr);
-        for (int p = M.lb0_ptr[n]; p < M.lb0_ptr[n + 1]; ++p) {
-            int e = M.lb0_line[p];
-            real fe = M.F[sidx(e, t, rep, T, R)];
-            pen += (double)(cv * dt * (M.ls[e] * fmax(fabs(fe) / M.ls[e] - real(1), real(0))));
-        }
-        for (int q = 0; q < nu && q < MAXU; ++q) {
-            int u = M.nu_unit[M.nu_ptr[n] + q], j = M.u_loc[u];
-            int kd = M.u_kind[u];
-            if (kd == ESM_UNIT_REN) {
-                real A = avail_map<real>(wraw(M, M.r_series[j], t, rep));
-                real p_ = A * M.kc_r[j] * real(1);
-                cgen += (double)(dt * (M.r_mc[j] * p_));
-                real dck = M.r_mc[j] * A * real(1);
-                dk[q] += (double)(dt * dck - A * real(1) * Gn);
-            } else if (kd == ESM_UNIT_DISP) {
-                real A = M.d_avail[j], kv = M.kc_d[j];
-                real Y = M.g[sidx(j, t, rep, T, R)];
-                real Yc = clampr<real>(Y, 0, 1);
-                real p_ = A * kv * Yc;
-                cgen += (double)(dt * (M.d_mc[j] * p_));
-                real ex = fabs(Y - Yc);
-                if (ex > 0) pen += (double)(cv * dt * (kv + k0) * ex);
-                if (!(real(0) < Y && Y < real(1))) dk[q] += (double)(cv * dt * fabs(Y - Yc));
-                real dck = M.d_mc[j] * A * Yc;
-                dk[q] += (double)(dt * dck - A * Yc * Gn);
-            } else {
-                real kv = M.kc_s[j];
-                real h = M.s_hours[j];
-                real ye = M.e[sidx(j, t, rep, T, R)], ye1 = M.e[sidx(j, (t + 1) % T, rep, T, R)];
-                real dd, jj;
-                real cc = soc_cost<real>(h, M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], kv, kv + k0, dt, cv, ye,
-                                         ye1, &dd, &jj);
-                real Ec = clampr<real>(ye, 0, 1), Ec1 = clampr<real>(ye1, 0, 1);
-                real d = h * (Ec1 - Ec) / dt - M.s_qt[j];
-                real pc, mcx;
+#define ESM_SCORE_NSLOT 8
+template <class S>
+__global__ void __launch_bounds__(32 * ESM_SCORE_NSLOT)
+    k_scores_fused(const __grid_constant__ DevModel<double> M, const S *theta, const S *gv, const S *ev, const S *zv,
+                   int tchunk, double *dkp, double *pp) {
+    __shared__ double sp[ESM_SCORE_NSLOT][32][5];
+    int lane = threadIdx.x, slot = threadIdx.y;
+    int rep = blockIdx.x * 32 + lane;
+    int n = blockIdx.y * ESM_SCORE_NSLOT + slot;
+    int c = blockIdx.z;
+    int T = M.T, R = M.R, K = M.K;
+    double part[5] = {0, 0, 0, 0, 0};  // gen, storage, shed, dump, penalty
+    if (rep < R && n < M.N) {
+        int t0 = c * tchunk, t1 = min(T, t0 + tchunk);
+        double dt = M.dt, cv = M.c_viol, k0 = M.kappa0;
+        const int MAXU = 8;
+        double dk[MAXU], dkbox[MAXU];
+        int nu = M.nu_ptr[n + 1] - M.nu_ptr[n];
+        for (int q = 0; q < MAXU; ++q) dk[q] = dkbox[q] = 0;
+        auto wr = [&](int s_, int t) {
+            return M.xbar[(size_t)s_ * T + t] + M.wscale[s_] * (double)zv[sidx(s_, t, rep, T, R)];
+        };
+        for (int t = t0; t < t1; ++t) {
+            // the residual (k_rebuild's order: load, lines, generation, storage)
+            double x = wr(n, t);
+            double rr = x > 0 ? x : 0.0;
+            for (int p = M.nlp[n]; p < M.nlp[n + 1]; ++p) {
+                int e = M.nl[p];
+                int a = M.bus0[e], b = M.bus1[e];
+                double fl = M.lb[e] * ((double)theta[sidx(a, t, rep, T, R)] - (double)theta[sidx(b, t, rep, T, R)]);
+                if (a == n) {
+                    rr += fl + 0.5 * 0.0;
+                    part[4] += cv * dt * (M.ls[e] * fmax(fabs(fl) / M.ls[e] - 1.0, 0.0));
+                } else {
+                    rr += -fl + 0.5 * 0.0;
+                }
+            }
+            for (int p = M.nu_ptr[n]; p < M.nu_ptr[n + 1]; ++p) {
+                int u = M.nu_unit[p], j = M.u_loc[u];
+                int kd = M.u_kind[u];
+                if (kd == ESM_UNIT_REN)
+                    rr -= avail_map<double>(wr(M.r_series[j], t)) * M.kc_r[j] * 1.0;
+                else if (kd == ESM_UNIT_DISP)
+                    rr -= M.d_avail[j] * M.kc_d[j] * clampr<double>((double)gv[sidx(j, t, rep, T, R)], 0, 1);
+            }
+            for (int p = M.nu_ptr[n]; p < M.nu_ptr[n + 1]; ++p) {
+                int u = M.nu_unit[p], j = M.u_loc[u];
+                if (M.u_kind[u] != ESM_UNIT_STOR) continue;
+                double ec = clampr<double>((double)ev[sidx(j, t, rep, T, R)], 0, 1);
+                double ec1 = clampr<double>((double)ev[sidx(j, (t + 1) % T, rep, T, R)], 0, 1);
+                double d = M.s_hours[j] * (ec1 - ec) / M.dt - M.s_qt[j];
+                double pc, mcx;
                 if (d >= 0) {
-                    pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : real(0);
+                    pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : 0.0;
                     mcx = 0;
                 } else {
                     pc = 0;
-                    mcx = fmin(-d * M.s_etaout[j], real(1));
+                    mcx = fmin(-d * M.s_etaout[j], 1.0);
                 }
-                real run = dt * M.s_mc[j] * kv * (pc + mcx);
-                cst += (double)run;
-                pen += (double)(cc - run);
-                // soc_grad (src/energy.jl:470-491)
-                real g = Gn;
-                if (d >= 0 && M.s_etain[j] <= 0) {
-                    dk[q] += (double)(cv * dt * d);
-                } else if (d >= 0) {
-                    real pcc = d / M.s_etain[j];
-                    dk[q] += (double)(dt * M.s_mc[j] * pcc + g * pcc + (pcc > 1 ? cv * dt * (pcc - 1) : real(0)));
+                rr += M.kc_s[j] * (pc - mcx);
+            }
+            // the terms of the cost and of its gradient (k_scores)
+            double Gn = dt * (rr > 0 ? M.c_shed : (rr < 0 ? -M.c_dump : 0.0));
+            if (rr > 0)
+                part[2] += dt * rr;
+            else
+                part[3] -= dt * rr;
+            for (int q = 0; q < nu && q < MAXU; ++q) {
+                int u = M.nu_unit[M.nu_ptr[n] + q], j = M.u_loc[u];
+                int kd = M.u_kind[u];
+                if (kd == ESM_UNIT_REN) {
+                    double A = avail_map<double>(wr(M.r_series[j], t));
+                    part[0] += dt * (M.r_mc[j] * (A * M.kc_r[j] * 1.0));
+                    dk[q] += dt * (M.r_mc[j] * A * 1.0) - A * 1.0 * Gn;
+                } else if (kd == ESM_UNIT_DISP) {
+                    double A = M.d_avail[j], kv = M.kc_d[j];
+                    double Y = (double)gv[sidx(j, t, rep, T, R)];
+                    double Yc = clampr<double>(Y, 0, 1);
+                    part[0] += dt * (M.d_mc[j] * (A * kv * Yc));
+                    double exs = fabs(Y - Yc);
+                    if (exs > 0) part[4] += cv * dt * (kv + k0) * exs;
+                    if (!(0.0 < Y && Y < 1.0)) dk[q] += cv * dt * fabs(Y - Yc);
+                    dk[q] += dt * (M.d_mc[j] * A * Yc) - A * Yc * Gn;
                 } else {
-                    real mc_ = -d * M.s_etaout[j];
-                    real mcc = fmin(mc_, real(1));
-                    dk[q] += (double)(dt * M.s_mc[j] * mcc - g * mcc +
-                                      ((mc_ > 1 && M.s_qt[j] <= 0) ? cv * dt * (mc_ - 1) : real(0)));
+                    double kv = M.kc_s[j], h = M.s_hours[j];
+                    double ye = (double)ev[sidx(j, t, rep, T, R)], ye1 = (double)ev[sidx(j, (t + 1) % T, rep, T, R)];
+                    double dd, jj;
+                    double cc = soc_cost<double>(h, M.s_qt[j], M.s_etain[j], M.s_etaout[j], M.s_mc[j], kv, kv + k0, dt,
+                                                 cv, ye, ye1, &dd, &jj);
+                    double Ec = clampr<double>(ye, 0, 1), Ec1 = clampr<double>(ye1, 0, 1);
+                    double d = h * (Ec1 - Ec) / dt - M.s_qt[j];
+                    double pc, mcx;
+                    if (d >= 0) {
+                        pc = M.s_etain[j] > 0 ? d / M.s_etain[j] : 0.0;
+                        mcx = 0;
+                    } else {
+                        pc = 0;
+                        mcx = fmin(-d * M.s_etaout[j], 1.0);
+                    }
+                    double run = dt * M.s_mc[j] * kv * (pc + mcx);
+                    part[1] += run;
+                    part[4] += cc - run;
+                    if (d >= 0 && M.s_etain[j] <= 0) {  // soc_grad (src/energy.jl:470-491)
+                        dk[q] += cv * dt * d;
+                    } else if (d >= 0) {
+                        double pcc = d / M.s_etain[j];
+                        dk[q] += dt * M.s_mc[j] * pcc + Gn * pcc + (pcc > 1 ? cv * dt * (pcc - 1) : 0.0);
+                    } else {
+                        double mc_ = -d * M.s_etaout[j];
+                        double mcc = fmin(mc_, 1.0);
+                        dk[q] += dt * M.s_mc[j] * mcc - Gn * mcc + ((mc_ > 1 && M.s_qt[j] <= 0) ? cv * dt * (mc_ - 1) : 0.0);
+                    }
+                    if (!(0.0 < ye && ye < 1.0)) dkbox[q] += cv * h * fabs(ye - Ec);
                 }
-                if (!(real(0) < ye && ye < real(1))) dkbox[q] += (double)(cv * h * fabs(ye - Ec));
             }
         }
+        for (int q = 0; q < nu && q < MAXU; ++q) {
+            int u = M.nu_unit[M.nu_ptr[n] + q];
+            dkp[((size_t)c * R + rep) * K + u] = dk[q] + dkbox[q];
+        }
     }
-    for (int q = 0; q < nu && q < MAXU; ++q) {
-        int u = M.nu_unit[M.nu_ptr[n] + q];
-        atomicAdd(&dk_out[(size_t)rep * M.K + u], dk[q] + dkbox[q]);
+    for (int i = 0; i < 5; ++i) sp[slot][lane][i] = part[i];
+    __syncthreads();
+    if (slot == 0 && rep < R) {
+        double acc[5] = {0, 0, 0, 0, 0};
+        for (int s2 = 0; s2 < ESM_SCORE_NSLOT; ++s2)
+            for (int i = 0; i < 5; ++i) acc[i] += sp[s2][lane][i];
+        double *P = pp + (((size_t)c * gridDim.y + blockIdx.y) * R + rep) * 5;
+        for (int i = 0; i < 5; ++i) P[i] = acc[i];
     }
-    double *P = parts_out + (size_t)rep * 8;
-    atomicAdd(&P[2], cgen);
-    atomicAdd(&P[3], cst);
-    atomicAdd(&P[4], shed);
-    atomicAdd(&P[5], dump);
-    atomicAdd(&P[6], pen);
+}
+
+// the chunk partials of k_scores_fused summed in chunk order: dk [R*K] and parts [R*8] (slots 2-6)
+static __global__ void k_score_reduce(int R, int K, int nchunk, int ngroups, const double *dkp, const double *pp, double *dk,
+                               double *parts) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t nrk = (size_t)R * K;
+    if (i < nrk) {
+        double a = 0;
+        for (int c = 0; c < nchunk; ++c) a += dkp[(size_t)c * nrk + i];
+        dk[i] = a;
+    } else if (i < nrk + (size_t)R * 5) {
+        size_t k = i - nrk;
+        int rep = (int)(k / 5), f = (int)(k % 5);
+        double a = 0;
+        for (int c = 0; c < nchunk; ++c)
+            for (int g = 0; g < ngroups; ++g) a += pp[(((size_t)c * ngroups + g) * R + rep) * 5 + f];
+        parts[(size_t)rep * 8 + 2 + f] = a;
+    }
 }
 
 // capacity_scores (src/replicas.jl:329): sk = -beta_v mask dk + log-measure gradient; fk = beta_k dK/dk;
@@ -426,13 +489,36 @@ cudaError_t launch_rebuild(const DevModel<real> &M, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <class real>
-cudaError_t launch_scores(const DevModel<real> &M, double *dk, double *parts, cudaStream_t s) {
-    int tchunk = 128;
-    int nch = (M.T + tchunk - 1) / tchunk;
-    int bx = M.R < 64 ? M.R : 64;
-    dim3 grid(M.N, nch, (M.R + bx - 1) / bx);
-    k_scores<real><<<grid, bx, 0, s>>>(M, tchunk, dk, parts);
+
+// step chunks of the fused score pass: one per 64 steps, fewer where the partials (and the R*(K+8)
+// final sums) would not fit the static score scratch of 2^20 doubles, so that both score entry
+// points sum in the same order
+__host__ inline int score_chunks(int T, int R, int K, int N) {
+    int ng = (N + ESM_SCORE_NSLOT - 1) / ESM_SCORE_NSLOT;
+    long long room = (1LL << 20) - (long long)R * (K + 8);
+    long long nmax = room > 0 ? room / ((long long)R * (K + 5 * ng)) : 0;
+    int n = (T + 63) / 64;
+    if (nmax >= 1 && n > nmax) n = (int)nmax;
+    return n < 1 ? 1 : n;
+}
+__host__ inline size_t score_partial_doubles(int T, int R, int K, int N) {
+    int ng = (N + ESM_SCORE_NSLOT - 1) / ESM_SCORE_NSLOT;
+    return (size_t)score_chunks(T, R, K, N) * R * (K + 5 * (size_t)ng);
+}
+
+template <class S>
+cudaError_t launch_scores_fused(const DevModel<double> &M, const S *theta, const S *g, const S *e, const S *z,
+                                double *partial, double *dk, double *parts, cudaStream_t s) {
+    int nchunk = score_chunks(M.T, M.R, M.K, M.N);
+    int ng = (M.N + ESM_SCORE_NSLOT - 1) / ESM_SCORE_NSLOT;
+    int tchunk = (M.T + nchunk - 1) / nchunk;
+    double *dkp = partial, *pp = partial + (size_t)nchunk * M.R * M.K;
+    dim3 grid((M.R + 31) / 32, ng, nchunk), block(32, ESM_SCORE_NSLOT);
+    k_scores_fused<S><<<grid, block, 0, s>>>(M, theta, g, e, z, tchunk, dkp, pp);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    size_t n = (size_t)M.R * M.K + (size_t)M.R * 5;
+    k_score_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M.R, M.K, nchunk, ng, dkp, pp, dk, parts);
     return cudaGetLastError();
 }
 

@@ -7,10 +7,17 @@
 #include "esm_linemove.cuh"
 
 namespace esm {
+// Load the kernels of the capacity scores now (esm_f64.cu): under lazy module loading a kernel's
+// code is placed on the device at its first use, and the score entry point that allocates nothing
+// must not be that first use.
+cudaError_t preload_score_kernels();
+// the fused score pass (esm_kernels_impl.cuh): its step chunks and partial buffer, and its launch
+// (instantiated for float and double states in esm_f64.cu, without FMA contraction like the oracle)
+template <class S>
+cudaError_t launch_scores_fused(const DevModel<double> &M, const S *theta, const S *g, const S *e, const S *z,
+                                double *partial, double *dk, double *parts, cudaStream_t s);
 template <class real>
 cudaError_t launch_rebuild(const DevModel<real> &M, cudaStream_t s);
-template <class real>
-cudaError_t launch_scores(const DevModel<real> &M, double *dk, double *parts, cudaStream_t s);
 template <class real>
 cudaError_t launch_score_finish(const DevModel<real> &M, const double *k_raw, const double *lo, const double *hi,
                                 const double *capex, double gamma_k, double beta_k, int physical, double *dk,

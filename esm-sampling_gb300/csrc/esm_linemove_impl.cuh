@@ -1689,20 +1689,21 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
         real t = Ln.sample_line((real)uc, (real)uo, &guard);
         if (guard) ++guards;
         bool compensated = fi == ESM_FAM_XLOCC || fi == ESM_FAM_TPOT || fi == ESM_FAM_TSOC;
-        if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041)
+        if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041), in FP64 in both builds
             int nk = d.hdr[3];
             bool any = false;
-            real lj = 0;
+            double lj = 0;
             for (int k = 0; k < nk; ++k) {
                 if (Ln.S(LL.kv, k) == 0) continue;
                 any = true;
-                real Q = Ln.S(LL.kq, k);
-                lj += Ln.S(LL.knm, k) * log(fabs((fmax(Q + d.kg[k] * t, real(0)) + Ln.S(LL.ke, k)) / Ln.S(LL.kp, k)));
+                double Q = Ln.S(LL.kq, k);
+                lj += (double)Ln.S(LL.knm, k) *
+                      log(fabs((fmax(Q + (double)d.kg[k] * (double)t, 0.0) + (double)Ln.S(LL.ke, k)) / (double)Ln.S(LL.kp, k)));
             }
             if (any) {
                 uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uj,
                          &un);
-                if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+                if (uj >= exp(fmin(0.0, lj))) t = 0;
             }
         }
         if (t != 0) Ln.commit(t);

@@ -679,15 +679,17 @@ struct PLane {
                                                : p1 - trexp_offset(uoff, -g, Ls, flat);
     }
 
-    // logjac (src/local.jl:1871) of the compensations
-    __device__ real logjac(real t, bool *any) const {
-        real lj = 0;
+    // logjac (src/local.jl:1871) of the compensations, in FP64 in both builds (the log-acceptance
+    // ratio is an FP64 quantity; its inputs are the build's values)
+    __device__ double logjac(real t, bool *any) const {
+        double lj = 0;
         *any = false;
         for (int i = 0; i < (lvl ? 0 : 2 * U); ++i) {
             if (S(LL.kv, i) == 0) continue;
             *any = true;
-            real Q = S(LL.kq, i);
-            lj += S(LL.knm, i) * log(fabs((fmax(Q + S(LL.kg, i) * t, real(0)) + S(LL.ke, i)) / S(LL.kp, i)));
+            double Q = S(LL.kq, i);
+            lj += (double)S(LL.knm, i) *
+                  log(fabs((fmax(Q + (double)S(LL.kg, i) * (double)t, 0.0) + (double)S(LL.ke, i)) / (double)S(LL.kp, i)));
         }
         return lj;
     }
@@ -762,10 +764,10 @@ __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevM
             if (guard) ++guards;
             if (t != 0) {
                 bool any;
-                real lj = Ln.logjac(t, &any);
+                double lj = Ln.logjac(t, &any);
                 if (any) {
                     uniform2(M.seed, ESM_TAG_SML, w0 + 1, (uint32_t)Ln.b0, (uint32_t)Ln.rep, sweep, &uj, &un);
-                    if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+                    if (uj >= exp(fmin(0.0, lj))) t = 0;
                 }
             }
             if (t != 0) Ln.commit(t);
@@ -818,11 +820,11 @@ __global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__
             if (guard) ++guards;
             if (t != 0 && !Ln.lvl) {
                 bool any;
-                real lj = Ln.logjac(t, &any);
+                double lj = Ln.logjac(t, &any);
                 if (any) {
                     uniform2(M.seed, ESM_TAG_SLL, 2u * (uint32_t)m + 1, (uint32_t)pu[0], (uint32_t)Ln.rep, sweep, &uj,
                              &un);
-                    if ((real)uj >= exp(fmin(real(0), lj))) t = 0;
+                    if (uj >= exp(fmin(0.0, lj))) t = 0;
                 }
             }
             if (t != 0) Ln.commit(t);

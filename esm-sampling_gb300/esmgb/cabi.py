@@ -2,7 +2,7 @@
 :class:`~esmgb.model.SynthModel`.
 
 The same ``esm_model`` struct is what a Julia ``ccall`` shim would fill from the reference's
-``EnergyModel``/``LocalModel`` (see INTEGRATION.md); here it is filled from the synthetic model.
+``EnergyModel``/``LocalModel``; here it is filled from the synthetic model.
 """
 from __future__ import annotations
 

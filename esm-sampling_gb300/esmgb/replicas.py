@@ -193,8 +193,10 @@ def masked_mean(v, mask):
 
 
 def _div(a, b):
-    """a / b with the IEEE result where b is 0 (the reference's Float64 division), not an error."""
-    return float(np.float64(a) / np.float64(b)) if b != 0 else (math.nan if a == 0 or a != a else math.copysign(math.inf, a))
+    """a / b with the IEEE result for every b, a zero of either sign included (the reference's
+    Float64 division), not an error."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(a) / np.float64(b))
 
 
 def masked_means(v, mask, groups, nfields):

@@ -278,3 +278,110 @@ class DALangevin:
             self.sur.add(self.k, occ, sbar)
         self.sur.train(self.train_steps)
         return accepted
+
+
+# ---------------------------------------------------------------------------------------------
+# surrogate-drift Langevin step of the capacities
+# ---------------------------------------------------------------------------------------------
+class SurrogateLangevin:
+    """The learned capacity step that keeps the plain step's form: the Langevin update of
+    langevin_update (src/replicas.jl:368; w = log(k + kappa_s), w' = w + clamp(h G, +-clip) +
+    sqrt(2 h) xi, reflected at w_min and, from below, at the box) at `mult` times the plain step size,
+    its drift G = (k + kappa_s)(-fk + (beta_k/beta_v) s) + 1 taken from the surrogate s_hat(k) instead
+    of the plain replica estimate s_bar. Every replica then follows the new capacities and sweeps, and
+    the plain scores there (one plain evaluation per iteration, as the plain step) train the surrogate
+    and judge it: a running mean (decay `decay`) of the discrepancy between the plain estimate and
+    the surrogate per capacity, in units of the plain estimate's own noise (the spread of the
+    replicas' scores over sqrt(R)). While the surrogate is untrained, or the mean absolute judged
+    discrepancy of the moving capacities exceeds `tol`, the iteration is the plain step (the plain
+    drift at the plain step size).
+
+    The plain step is a Langevin step on a noisy drift (the replica average of R scores): at a step
+    size h its noise adds about h^2 Var(G) per step to the 2h of the injected noise. The surrogate's
+    drift averages the plain estimates of many iterations, so a longer step does not carry that
+    noise; what it carries instead is the surrogate's error, which the judge bounds."""
+
+    def __init__(self, d, m, sur, eta, kappa_s, kmin=1.0, clip=0.02, mult=4.0, weights=None, seed=0,
+                 train_steps=1, tol=1.0, decay=0.9):
+        self.d, self.m, self.sur = d, m, sur
+        ug = np.asarray(m.unit_group)
+        self.eta_u = np.asarray(eta, float)[ug]
+        self.ks_u = np.asarray(kappa_s, float)[ug]
+        self.moving = self.eta_u > 0
+        self.mult, self.clip, self.kmin = mult, clip, kmin
+        self.hi = np.asarray(m.unit_hi, float)
+        self.ratio = m.beta_k / m.beta_v
+        self.w = np.full(d.R, 1.0 / d.R) if weights is None else np.asarray(weights, float)
+        self.rng = np.random.default_rng(seed)
+        self.train_steps, self.tol, self.decay = train_steps, tol, decay
+        self.k = np.asarray(d.download_k(), float).copy()
+        self.z = np.zeros(m.Kunits)
+        self.G = self.fk = None
+        self.occ = None
+        self.stats = {"iters": 0, "learned": 0, "plain_evals": 0}
+
+    def grad_w(self, k, sbar, fk):
+        return (k + self.ks_u) * (-fk + self.ratio * sbar) + 1.0
+
+    def update(self, k, G, h, clip):
+        """langevin_update on the moving capacities (the device's k_langevin, on the host)."""
+        mv = self.moving
+        ks = self.ks_u[mv]
+        w = np.log(k[mv] + ks)
+        w1 = w + np.clip(h[mv] * G[mv], -clip, clip) + np.sqrt(2 * h[mv]) * self.rng.standard_normal(mv.sum())
+        wmin = np.log(self.kmin + ks)
+        w1 = np.where(w1 < wmin, 2 * wmin - w1, w1)
+        wmax = np.log(np.maximum(self.hi[mv], self.kmin + 1.0) + ks)
+        w1 = np.where((w1 > wmax) & (w <= wmax), np.maximum(2 * wmax - w1, wmin), w1)
+        out = k.copy()
+        out[mv] = np.exp(w1) - ks
+        return out
+
+    def plain(self, it):
+        """One plain evaluation at the current capacities: (s_bar, fk, the noise sd of G)."""
+        self.d.sweeps(1, sweep0=it, stats=False)
+        sk, fk, _ = self.d.scores()
+        self.stats["plain_evals"] += 1
+        sbar = self.w @ sk
+        sd = (self.k + self.ks_u) * self.ratio * sk.std(axis=0) / np.sqrt(len(sk))
+        return sbar, fk, sd
+
+    def step(self, it, weather=None):
+        """One iteration; weather (optional): the weather draws of the step, applied first."""
+        d = self.d
+        self.stats["iters"] += 1
+        if weather is not None and weather[0].any():
+            moved, theta, window, wstart = weather[:4]
+            d.weather_step(moved, theta, window, wstart, it=it)
+            self.occ = None
+        if self.occ is None:
+            self.occ = d.regime_occupancy()
+        if self.G is None:
+            sbar, self.fk, _ = self.plain(it)
+            self.G = self.grad_w(self.k, sbar, self.fk)
+            self.sur.add(self.k, self.occ, sbar)
+        judged = np.mean(np.abs(self.z[self.moving]))
+        use = self.sur.ready and judged <= self.tol
+        if use:
+            s_hat = self.sur.predict(self.k, self.occ)
+            # a prediction outside what the buffer has seen (or not finite) is not trusted
+            use = bool(np.all(np.isfinite(s_hat)) and
+                       np.all(np.abs(s_hat - self.sur.mu) <= 10 * self.sur.sd + 1e-12))
+        if use:
+            Gs = self.grad_w(self.k, s_hat, self.fk)
+            k1 = self.update(self.k, Gs, self.mult * self.eta_u, self.mult * self.clip)
+            self.stats["learned"] += 1
+        else:
+            k1 = self.update(self.k, self.G, self.eta_u, self.clip)
+        self.k = d.follow_capacities(k1, self.kmin)
+        sbar, self.fk, sd = self.plain(it)
+        self.G = self.grad_w(self.k, sbar, self.fk)
+        if self.sur.ready:
+            Gs1 = self.grad_w(self.k, self.sur.predict(self.k, self.occ), self.fk)
+            # the noise scale of the plain drift, floored where the replicas agree to round-off
+            scale = np.maximum(sd, 1e-3 * np.abs(self.G) + 1e-6)
+            zz = np.nan_to_num((self.G - Gs1) / scale, nan=10.0, posinf=10.0, neginf=-10.0)
+            self.z = self.decay * self.z + (1 - self.decay) * np.clip(zz, -10, 10)
+        self.sur.add(self.k, self.occ, sbar)
+        self.sur.train(self.train_steps)
+        return use

@@ -205,19 +205,25 @@ int esm_storage_long(esm_ctx *ctx, int64_t sweep, int64_t *stats);
 /* Capacity scores per replica: sk [R*K] (s_k = -beta_v dC/dk + dlogJ/dk, node space) and the
    capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with
    grad (src/energy.jl:551) and log_measure_grad (:811). parts (may be NULL): [R*8] cost parts
-   per replica: capex, op, gen, storage, shed, dump, penalty, 0 (CostParts, src/energy.jl:531). */
+   per replica: capex, op, gen, storage, shed, dump, penalty, 0 (CostParts, src/energy.jl:531).
+   One pass over the state computes every node balance and term in FP64 (from the FP32 state in
+   the production build) and sums them in a fixed order: the same state gives the same scores bit
+   for bit. */
 int esm_capacity_scores(esm_ctx *ctx, double *sk, double *fk, double *parts);
 
 /* esm_capacity_scores without allocating in the call (no counterpart in the reference): for a
    caller that must not allocate device memory here -- one whose device memory is held by a caching
    allocator or a capped pool, or whose step must not stall on cudaMalloc/cudaFree. The score
-   accumulators live in a file-scope device array of ESM_SCORE_SCRATCH_DOUBLES doubles (8 MiB);
-   R*(K+8) beyond that is rejected with ESM_EINVAL. The first call on a device (with it current)
-   resolves the array's address: make it before any stream capture. The array is shared by all
-   contexts on a device, so overlapping calls race: serialise them. Same outputs and effect as
-   esm_capacity_scores (a following esm_langevin_step uses these scores). */
+   accumulators -- the partial sums of the score pass over step chunks and the R*(K+8) totals --
+   live in a file-scope device array of ESM_SCORE_SCRATCH_DOUBLES doubles (8 MiB); the pass takes
+   fewer chunks where that is needed to fit (the same chunks as esm_capacity_scores, so both give the
+   same scores bit for bit), and contexts that do not fit even with one chunk (R*(K+8) near 2^20)
+   are rejected with ESM_EINVAL. esm_create, which allocates anyway, resolves
+   the array's address on the context's device and loads the score kernels, so the call places
+   nothing on the device; it must be made with the context's device current (else ESM_EINVAL). The
+   array is shared by all contexts on a device, so overlapping calls race: serialise them. Same
+   outputs and effect as esm_capacity_scores (a following esm_langevin_step uses these scores). */
 #define ESM_SCORE_SCRATCH_DOUBLES (1 << 20)
-#define ESM_MAX_DEVICES 64
 int esm_capacity_scores_static(esm_ctx *ctx, double *sk, double *fk, double *parts);
 
 /* The Langevin step of the shared capacities from the replica-weighted score

@@ -75,3 +75,48 @@ def test_surrogate_learns_and_da_mechanics():
     assert np.isfinite(msj_da) and np.isfinite(msj_plain)
     sur.close()
     d.close()
+
+
+def test_surrogate_langevin_mixing():
+    """SurrogateLangevin (the surrogate's drift at 4x the plain step, judged by the plain scores)
+    against the plain step from one saved state, one plain evaluation per iteration each: the mean
+    squared jump of w = log(k + kappa_s) per plain evaluation, printed with the share of iterations
+    that used the surrogate; asserted: the states stay finite and the bookkeeping adds up."""
+    from esmgb.surrogate import SurrogateLangevin
+    m, d, eta, ks = _setup()
+    ug = np.asarray(m.unit_group)
+    mv = eta[ug] > 0
+    R = d.R
+    w = np.full(R, 1.0 / R)
+    sur = ScoreSurrogate(m, hidden=(512, 512, 512), capacity=2048, batch=1024, lr=1e-3, seed=1)
+    for it in range(160):
+        d.sweeps(1, sweep0=it, stats=False)
+        sk, fk, _ = d.scores()
+        sur.add(d.download_k(), d.regime_occupancy(), w @ sk)
+        sur.train(4)
+        d.langevin_step(w, eta, ks, 1.0, 0.02, True, None, it)
+    d.state_save()
+    n = 60
+    W = []
+    for it in range(n):
+        d.sweeps(1, sweep0=2000 + it, stats=False)
+        d.scores()
+        k, _ = d.langevin_step(w, eta, ks, 1.0, 0.02, True, None, 2000 + it)
+        W.append(np.log(k + ks[ug]))
+    msj_plain = np.mean(np.sum(np.diff(np.array(W)[:, mv], axis=0) ** 2, axis=1))
+    d.state_restore()
+    sl = SurrogateLangevin(d, m, sur, eta, ks, mult=4.0, seed=2, train_steps=2)
+    W = []
+    for it in range(n):
+        sl.step(2000 + it)
+        W.append(np.log(sl.k + ks[ug]))
+    W = np.array(W)
+    msj = np.mean(np.sum(np.diff(W[:, mv], axis=0) ** 2, axis=1))
+    st = sl.stats
+    print(f"surrogate drift vs plain: msjd per plain evaluation {msj:.3e} vs {msj_plain:.3e} "
+          f"(ratio {msj / msj_plain:.3f}); surrogate steps {st['learned']}/{st['iters']}, "
+          f"judged discrepancy {np.mean(np.abs(sl.z[mv])):.3f}")
+    assert np.all(np.isfinite(W))
+    assert st["plain_evals"] == st["iters"] + 1
+    sur.close()
+    d.close()

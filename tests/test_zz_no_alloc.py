@@ -1,6 +1,7 @@
 """esm_capacity_scores_static (the score entry point that allocates nothing in the call) against
-esm_capacity_scores on the same state, through the C ABI, on two calls in a row; and its size
-limit. Collected last so that it also runs after every other GPU test."""
+esm_capacity_scores on the same state, through the C ABI, on two calls in a row; a first call with
+no other device work before it leaves the device's free memory unchanged; and its size limit.
+Collected last so that it also runs after every other GPU test."""
 import numpy as np
 import pytest
 
@@ -33,6 +34,44 @@ def test_static_scores_match(prec):
         assert (np.abs(sk - sk0) / scale).max() < 1e-9
         np.testing.assert_allclose(fk, fk0, rtol=1e-14)
         np.testing.assert_allclose(parts, p0, rtol=1e-9, atol=1e-6)
+    d.close()
+
+
+def _free_device_bytes():
+    """Free device memory (cudaMemGetInfo) through the CUDA runtime loaded in this process, else the
+    toolkit's; None when neither can be found."""
+    import ctypes
+    import os
+    paths = [ln.split()[-1] for ln in open("/proc/self/maps") if "libcudart" in ln]
+    paths += ["/usr/local/cuda/lib64/libcudart.so"]
+    for path in paths:
+        if os.path.exists(path):
+            rt = ctypes.CDLL(path)
+            free, total = ctypes.c_size_t(), ctypes.c_size_t()
+            if rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0:
+                return free.value
+    return None
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_static_scores_first_call_allocates_nothing(prec):
+    """A context whose first device work after the upload is the static scores: the device's free
+    memory is the same before and after the call (esm_create resolved the scratch array and loaded
+    the score kernels), and the scores equal esm_capacity_scores'."""
+    m = make_model(40, 60, 40, seed=13)
+    d = DeviceChain(m, 16, precision=prec, seed=7)
+    d.upload(_state(m, 16, seed=5))
+    d.sync(60.0)
+    free0 = _free_device_bytes()
+    if free0 is None:
+        pytest.skip("no CUDA runtime to read the free device memory")
+    sk, fk, parts = d.scores_static()
+    free1 = _free_device_bytes()
+    assert free1 == free0, f"the call placed {free0 - free1} bytes on the device"
+    sk0, fk0, p0 = d.scores()
+    scale = np.abs(sk0).max(axis=0) + 1e-3
+    assert (np.abs(sk - sk0) / scale).max() < 1e-9
+    np.testing.assert_allclose(fk, fk0, rtol=1e-14)
     d.close()
 
 
