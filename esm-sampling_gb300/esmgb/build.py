@@ -1,6 +1,8 @@
-"""Build libesmcuda.so for sm_103a with nvcc (no cmake): three translation units compiled in
-parallel -- the C ABI, the FP32 kernels and the FP64 kernels (the FP64 parity build without FMA
-contraction, like the CPU oracle) -- then linked into one shared library, in-tree.
+"""Build libesmcuda.so for sm_103a with nvcc (no cmake): the translation units compiled in
+parallel -- the C ABI, the FP32 kernels (the production build, with the approximate single-precision
+division: 2 ulp, 12 % faster line moves at the benchmarked size), the FP64 kernels (the parity build
+without FMA contraction and with IEEE division, like the CPU oracle) and the surrogate MLP -- then
+linked into one shared library, in-tree.
 """
 from __future__ import annotations
 
@@ -14,7 +16,7 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libesmcuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-UNITS = [("esm_capi.cu", []), ("esm_f32.cu", []), ("esm_f64.cu", ["-fmad=false"]), ("esm_mlp.cu", [])]
+UNITS = [("esm_capi.cu", []), ("esm_f32.cu", ["-prec-div=false"]), ("esm_f64.cu", ["-fmad=false"]), ("esm_mlp.cu", [])]
 
 
 def nvcc():

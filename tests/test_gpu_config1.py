@@ -15,9 +15,11 @@ same-segment offsets within 1e-6 of the segment's length); FP32 elements 2e-3 (4
 utilisations and states of charge), first differing draws (beyond 1e-4 |t| + 1e-6) within 5e-3 of
 their boundary -- the FP32 potentials carry round-off up to about 1e-3 nats (4.8e-7 times the summed
 magnitudes of a move's terms), so segment masses and end points are known to about that relative
-accuracy -- (same-segment offsets: within 5e-3 of the length, or the segment flat to 1e-2 nats:
+accuracy -- (same-segment offsets: within 2e-2 of the length, or the segment flat to 1e-2 nats:
 the FP32 flat-segment threshold is the round-off scale of the segment's end points, about 1e-3 nats
-on storage moves). The absolute floor of 1e-6 is the FP32 resolution of the state: a state of charge
+on storage moves; the FP32 build divides with the approximate single-precision division, 2 ulp,
+so a breakpoint at t carries about 2.4e-7 |t| of placement error, which within a short segment near
+a clamp moves the offset by up to about 1e-2 of the segment's length). The absolute floor of 1e-6 is the FP32 resolution of the state: a state of charge
 near 1 has an ulp of 6e-8, so where it sits within 1e-5 of a clamp the clamp's breakpoint is placed
 only to about 1e-2 of its distance, and draws below 1e-6 (about 16 ulps of the state through the
 atoms' coefficients) differ by that placement, not by a discrete choice."""
@@ -139,5 +141,5 @@ def test_config1_moves_fp32(model, fp32_start, limit):
     for f in sorted(flips, key=lambda f: -f["margin"])[:5]:
         print({k: f.get(k) for k in ("q", "rep", "move", "kind", "margin", "fam", "entries", "t", "t_dev", "gL", "L")})
     assert frac <= 0.02
-    assert all(f["margin"] <= 5e-3 for f in flips), summary(flips)
+    assert all(f["margin"] <= (2e-2 if f["kind"] == "offset" else 5e-3) for f in flips), summary(flips)
     d.set_move_log(0)
