@@ -392,6 +392,128 @@ def batch_case(args):
                       "sizes": {"N": [n for n, _ in specs], "T": [t for _, t in specs]}}), flush=True)
 
 
+def n256_case(args):
+    """The full-scale configuration: 256 nodes, 420 lines, hourly T = 8760, 256 replicas, the storage
+    sweeps on (the multiscale sweep with probability 1/2, the long-range sweep every sweep, as
+    operation_sweep! runs them) and the automatic point cap of the 256-unit state-of-charge atoms
+    (1024). Steps as the default bench's (weather, operation sweep, scores, Langevin step), then one
+    training step of the 5 x 1024 surrogate on minibatches of 1024 (BF16 tensor cores), timed; the
+    oracle on a sample of one replica's moves (the first moves of one colour class), extrapolated to
+    the whole sweep of 256 replicas."""
+    from esmgb import build as B
+    B.build()
+    from esmgb import replicas as RP
+    from esmgb.device import DeviceChain
+    from esmgb.model import initial_state, make_model
+    from esmgb.surrogate import MLP
+    N, L, T, R = args.N or 256, args.L or 420, args.T or 8760, args.R or 256
+    m = make_model(N, L, T, seed=1234)
+    d = DeviceChain(m, R, precision=32, seed=1234, storage_ms=1, storage_long=1)
+    d.upload(initial_state(m, R, seed=7))
+    if args.grid:
+        d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
+    ctl = RP.ReplicaCtl(M=R)
+    rng = np.random.Generator(np.random.PCG64(1))
+    t0 = time.perf_counter()
+    device_loop(d, m, ctl, 1, args.warmup, rng, None)
+    d.sync(3600.0)
+    warm_s = time.perf_counter() - t0
+    d.set_timing(True)
+    st0 = np.zeros(2 * (12) + 1, np.int64)
+    t0 = time.perf_counter()
+    eta, ks = carrier_params(m)
+    w = np.full(R, 1.0 / R)
+    for q in range(args.steps):
+        it = 1 + args.warmup + q
+        moved, theta, window, wstart, _ = schedule(ctl, it, R, rng)
+        if moved.any():
+            d.weather_step(moved, theta, window, wstart, it=it)
+        st0 += d.sweeps(1, sweep0=it)
+        d.scores()
+        d.langevin_step(w, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
+    d.sync(3600.0)
+    wall = time.perf_counter() - t0
+    kt = d.timing()
+    dev_ms = sum(v[0] for v in kt.values())
+    cls_ms, cls_n = kt["class_pass"]
+    alg = 4 * (11 * N + 2 * L) * (T / 2) * R
+    per = cls_ms / max(cls_n, 1) / 1000.0
+    peak, kind = peaks()
+    tried = int(st0[:-1:2].sum())
+    out = {"case": "n256", "workload": f"{N} nodes, {L} lines, T={T} hourly, {R} replicas, storage sweeps on",
+           "steps": args.steps, "warmup": args.warmup, "warmup_s": warm_s,
+           "sweeps_per_s": args.steps / (dev_ms / 1000.0), "wall_s": wall, "ms_per_step": dev_ms / args.steps,
+           "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+           "moves_tried": tried, "guards": int(st0[-1]), "guard_rate": int(st0[-1]) / max(tried, 1),
+           "max_points": int(d.opts.max_points) or 4 * N,
+           "roofline_class_pass": {"bound": "hbm", "achieved": alg / per / 1e9 if per > 0 else 0.0, "peak": peak,
+                                   "unit": "GB/s", "frac": (alg / per / 1e9) / peak if per > 0 else 0.0,
+                                   "peak_kind": kind},
+           "move_grid": list(d.move_grid()[:2])}
+    # the surrogate of the full form: 5 hidden layers of 1024, minibatches of 1024
+    d_in = m.Kunits + 4 * m.K
+    dims = [d_in, 1024, 1024, 1024, 1024, 1024, m.Kunits]
+    mlp = MLP(dims, batch_max=1024, seed=1)
+    xr = np.random.default_rng(0)
+    x = xr.standard_normal((1024, d_in)).astype(np.float32)
+    y = xr.standard_normal((1024, m.Kunits)).astype(np.float32)
+    for _ in range(3):
+        mlp.train_step(x, y, 1e-3)
+    ns = 20
+    t0 = time.perf_counter()
+    for _ in range(ns):
+        mlp.train_step(x, y, 1e-3)
+    mlp_s = (time.perf_counter() - t0) / ns
+    flops = 3 * 2 * 1024 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+    out["surrogate_train_step"] = {"dims": dims, "batch": 1024, "ms": 1000 * mlp_s, "tflops": flops / mlp_s / 1e12,
+                                   "note": "forward + backward + Adam of one minibatch, wall time of the call "
+                                           "(host copies of the minibatch included)"}
+    mlp.close()
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        from oracle.oracle import Oracle
+        O.build()
+        st1 = d.download()
+        sub = {k: (v if k == "k" else np.ascontiguousarray(v[..., :1])) for k, v in st1.items()}
+        o = Oracle(m, 1, seed=1234, threads=os.cpu_count() or 1)
+        o.set_state(sub)
+        o.rebuild()
+        nm = sum(len(a.ptr) - 1 for a in m.atoms) + int(round(4.0 * N))
+        lim = min(nm, args.cpu_moves)
+        t0 = time.perf_counter()
+        o.class_pass_range(1 + args.warmup + args.steps, 0, 0, lim)
+        dt = time.perf_counter() - t0
+        sweep_s = dt * (nm / lim) * 2 * R
+        out["cpu_baseline"] = {"value": 1.0 / sweep_s, "unit": "local sweeps/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"the first {lim} of {nm} moves of one colour class of 1 "
+                                                         f"replica ({dt:.1f} s), extrapolated to 2 classes and {R} "
+                                                         f"replicas (local sweep only)"}
+    print(json.dumps(out), flush=True)
+
+
+def ess_case(args):
+    """Capacity ESS/s of the plain and learned capacity steps at the benchmarked configuration over
+    longer chains than the default line's: --warmup plain steps (untimed, from the bench's start
+    state), then ess_arms with --ess-steps steps per arm from the chain state they reached."""
+    from esmgb import build as B
+    B.build()
+    from esmgb import replicas as RP
+    m, st, d = setup_chain(32)
+    d.set_move_grid(2, 32)
+    ctl = RP.ReplicaCtl(M=d.R)
+    rng = np.random.Generator(np.random.PCG64(1))
+    t0 = time.perf_counter()
+    device_loop(d, m, ctl, 1, args.warmup, rng, None)
+    d.sync(3600.0)
+    warm = time.perf_counter() - t0
+    arms = tuple(a for a in args.arms.split(",") if a)
+    res = ess_arms(d, m, ctl, 1 + args.warmup, args.ess_steps, arms=arms)
+    out = {"case": "ess", "workload": config_dict()["workload"], "warmup_steps": args.warmup, "warmup_s": warm,
+           "steps_per_arm": args.ess_steps, "capacity_ess_per_s": {a: v["value"] for a, v in res.items()},
+           "ratio_to_plain": {a: v.get("ratio_to_plain") for a, v in res.items() if a != "plain"}, "detail": res}
+    print(json.dumps(out), flush=True)
+
+
 def job_rate(pg, world, steps, seconds):
     """Whole-job rate of `world` ranks that each ran `steps` units: world * steps over the slowest
     rank's time (max over ranks, after which every rank holds the same value); (rate, seconds)."""
@@ -432,7 +554,9 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="--case small: the autotuner picks the line-move grid")
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
-    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage"],
+    ap.add_argument("--cpu-moves", type=int, default=64, help="--case n256: moves of the oracle's sample")
+    ap.add_argument("--arms", default="plain,learned,da", help="--case ess: the arms measured")
+    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage", "n256", "ess"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
     if args.case == "small":
@@ -441,6 +565,10 @@ def main():
         return batch_case(args)
     if args.case == "storage":
         return storage_case(args)
+    if args.case == "n256":
+        return n256_case(args)
+    if args.case == "ess":
+        return ess_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
