@@ -170,11 +170,12 @@ def capacity_ess(m, kt, seconds):
         else:
             ess[c], mcse[c] = float(ess_bulk([x])), float(mcse_rel([x]))
     worst = min(ess, key=ess.get)
+    nonfinite = int((~np.isfinite(kt)).any(axis=1).sum())
     w = np.log(np.maximum(kt, 1e-300))
     msjd = float(np.mean(np.sum(np.diff(w, axis=0) ** 2, axis=1))) if len(kt) > 1 else 0.0
     return {"value": ess[worst] / seconds, "unit": "ESS/s", "ess_min": ess[worst], "carrier": worst,
             "steps": len(kt), "seconds": seconds, "ess": ess, "mcse_rel": mcse,
-            "msjd_log_ktot_per_step": msjd}
+            "msjd_log_ktot_per_step": msjd, "nonfinite_steps": nonfinite}
 
 
 def ess_arms(d, m, ctl, it0, n, arms=("plain", "learned", "da")):
@@ -241,7 +242,8 @@ def ess_arms(d, m, ctl, it0, n, arms=("plain", "learned", "da")):
         d.sync(600.0)
         out[arm] = capacity_ess(m, kt, time.perf_counter() - t0)
         out[arm]["stats"] = dict(stepper.stats)
-        out[arm]["ratio_to_plain"] = out[arm]["value"] / out["plain"]["value"]
+        pv = out["plain"]["value"]
+        out[arm]["ratio_to_plain"] = out[arm]["value"] / pv if pv > 0 else None
     sur.close()
     d.state_restore()
     return out
@@ -318,14 +320,45 @@ def profile_case(args):
         d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
     elif args.autotune:
         grid = d.autotune_moves(sweep=0)[0]
+    if args.sep:
+        d.set_sep_walk(args.sep)
     d.sweeps(args.warmup, 0, stats=False)
     d.set_timing(True)
     st = d.sweeps(args.steps, args.warmup)
+    d.scores()
     kt = d.timing()
     print(json.dumps({"case": "small", "N": w["N"], "T": w["T"], "R": w["R"], "sweeps": args.steps,
-                      "grid": list(d.move_grid()[:2]),
+                      "grid": list(d.move_grid()[:2]), "sep_walk_min_units": args.sep,
                       "kernel_ms": {k: v[0] for k, v in kt.items()}, "launches": {k: v[1] for k, v in kt.items()},
                       "moves_tried": int(st[:-1:2].sum()), "guards": int(st[-1])}), flush=True)
+
+
+def mlp_case(args):
+    """The surrogate's training step at the full form's sizes (5 hidden layers of 1024 between the
+    256-node model's 1357 capacities plus the 8-dim regime summary and its 1357 scores, minibatches of
+    1024), with the tcgen05 GEMMs and with the mma.sync GEMMs: wall time per step and TFLOP/s (the
+    forward, backward and weight-gradient GEMMs, 3 x 2 x B x the layers' weights)."""
+    from esmgb import build as B
+    B.build()
+    from esmgb.surrogate import MLP
+    dims = [1365, 1024, 1024, 1024, 1024, 1024, 1357]
+    flops = 3 * 2 * 1024 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1024, dims[0])).astype(np.float32)
+    t = rng.standard_normal((1024, dims[-1])).astype(np.float32)
+    out = {"case": "mlp", "dims": dims, "batch": 1024, "flops_per_step": flops}
+    for kind, name in ((1, "tcgen05"), (0, "mma_sync")):
+        net = MLP(dims, batch_max=1024, seed=1)
+        net.set_gemm(kind)
+        for _ in range(max(args.warmup, 1)):
+            net.train_step(x, t, 1e-3)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            net.train_step(x, t, 1e-3)
+        dt = (time.perf_counter() - t0) / args.steps
+        out[name] = {"ms": 1000 * dt, "tflops": flops / dt / 1e12}
+        net.close()
+    print(json.dumps(out), flush=True)
 
 
 def storage_case(args):
@@ -556,7 +589,9 @@ def main():
                                                "the autotuner's choice")
     ap.add_argument("--cpu-moves", type=int, default=64, help="--case n256: moves of the oracle's sample")
     ap.add_argument("--arms", default="plain,learned,da", help="--case ess: the arms measured")
-    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage", "n256", "ess"],
+    ap.add_argument("--sep", type=int, default=0, help="--case small: cooperative walk of separable moves of "
+                                                     "at least this many units (0: off)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage", "n256", "ess", "mlp"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
     if args.case == "small":
@@ -569,6 +604,8 @@ def main():
         return n256_case(args)
     if args.case == "ess":
         return ess_case(args)
+    if args.case == "mlp":
+        return mlp_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)

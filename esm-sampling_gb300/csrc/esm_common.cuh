@@ -72,6 +72,18 @@ __host__ __device__ inline double normal_at(uint64_t seed, uint32_t tag, uint32_
     return (j & 1) ? rr * sin(a) : rr * cos(a);
 }
 
+// A uniform of [0, 1) in the working precision. The 53-bit uniforms round up to 1 in FP32 when they
+// lie within 2^-25 of it (3e-8 of the draws), and u = 1 is outside the domain of the inverse-CDF
+// maps: the truncated exponential of a steep segment, -log1p(-u (1 - e^-gL)) / g, is infinite at
+// u = 1 once 1 - e^-gL rounds to 1. Such a draw is taken to the largest value below 1 instead.
+template <class real>
+__host__ __device__ inline real unit_uniform(double u) {
+    real v = (real)u;
+    if constexpr (sizeof(real) == 4)
+        return v < 1.0f ? v : 0.99999994f;
+    return v;
+}
+
 template <class real>
 __host__ __device__ inline real clampr(real x, real lo, real hi) {
     return x < lo ? lo : (x > hi ? hi : x);

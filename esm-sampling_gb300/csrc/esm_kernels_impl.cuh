@@ -455,7 +455,9 @@ __global__ void k_langevin(int K, int R, const int *u_group, const int *u_gidx, 
     double wv = log(k + ks);
     double dw0 = et * ((k + ks) * g + 1);
     if (fabs(dw0) > clip) atomicAdd(nclip, 1);
-    double w1 = wv + fmin(fmax(dw0, -clip), clip) + sqrt(2 * et) * x;
+    // clamp (src/replicas.jl:368) by comparisons, as the reference's clamp: a non-finite drift stays
+    // non-finite (fmin/fmax would turn NaN into -clip and hide a broken score)
+    double w1 = wv + (dw0 > clip ? clip : (dw0 < -clip ? -clip : dw0)) + sqrt(2 * et) * x;
     double wmin = log(kmin + ks);
     w1 = w1 < wmin ? 2 * wmin - w1 : w1;
     if (box) {
@@ -573,7 +575,7 @@ template <class real>
 __device__ inline double weather_normal(uint64_t seed, uint32_t j, uint32_t rep, uint32_t it) {
     double u0, u1;
     uniform2(seed, ESM_TAG_WTH, j >> 1, 0, rep, it, &u0, &u1);
-    real rr = sqrt(real(-2) * log(real(1) - (real)u0));
+    real rr = sqrt(real(-2) * log((real)(1.0 - u0)));   // 1 - u0 >= 2^-53 before the cast: never log(0)
     real a = real(6.283185307179586) * (real)u1;
     return (double)((j & 1) ? rr * sin(a) : rr * cos(a));
 }

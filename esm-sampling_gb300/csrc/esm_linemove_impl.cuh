@@ -1686,7 +1686,7 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
         double uc, uo, uj, un;
         uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
         bool guard;
-        real t = Ln.sample_line((real)uc, (real)uo, &guard);
+        real t = Ln.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), &guard);
         if (guard) ++guards;
         bool compensated = fi == ESM_FAM_XLOCC || fi == ESM_FAM_TPOT || fi == ESM_FAM_TSOC;
         if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041), in FP64 in both builds

@@ -1,6 +1,8 @@
 // Surrogate of the replica-averaged capacity score: a small MLP trained online on (capacity,
-// sampled score) pairs with hand-written BF16 tensor-core kernels (mma.sync m16n8k16, FP32
-// accumulation), SiLU hidden layers, mean-squared loss and Adam with FP32 master weights.
+// sampled score) pairs with hand-written BF16 tensor-core kernels (tcgen05.mma with the accumulator
+// in tensor memory, esm_tc_gemm.cuh; the warp-level mma.sync m16n8k16 kernel below stays selectable
+// as its check, esm_mlp_set_gemm), FP32 accumulation, SiLU hidden layers, mean-squared loss and
+// Adam with FP32 master weights.
 // The learned part is not in the reference (it is this repository's addition); its CPU check is
 // the oracle's FP32 MLP on the same BF16-rounded operands.
 #include <cuda_bf16.h>
@@ -14,6 +16,7 @@
 #include <vector>
 
 #include "../../include/esmcuda.h"
+#include "esm_tc_gemm.cuh"
 
 using std::vector;
 
@@ -206,6 +209,9 @@ struct esm_mlp {
     float *xin = nullptr;
     double *loss = nullptr;
     vector<void *> allocs;
+    int gemm_kind = 1;                             // 1: tcgen05 (k_gemm_tc), 0: mma.sync (k_gemm_bf16)
+    __nv_bfloat16 *tA = nullptr, *tB = nullptr;    // K-major copies of the weight-gradient operands
+    int *tc_err = nullptr;                         // set by k_gemm_tc when a wait ran out
 };
 
 namespace {
@@ -239,11 +245,75 @@ int malloc_(esm_mlp *c, T **p, size_t n) {
     return ESM_OK;
 }
 
+int gemm_tc(esm_mlp *c, const GemmArgs &g, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb) {
+    tc::GemmTC t{};
+    t.M = g.M;
+    t.N = g.N;
+    t.K = g.K;
+    t.A = A;
+    t.lda = lda;
+    t.B = B;
+    t.ldb = ldb;
+    t.C = g.C;
+    t.ldc = g.ldc;
+    t.accumulate = g.accumulate;
+    t.bias = g.bias;
+    t.silu = g.silu;
+    t.Cb = g.Cb;
+    t.ldcb = g.ldcb;
+    t.err = c->tc_err;
+    dim3 grid((g.N + TC_BN - 1) / TC_BN, (g.M + TC_BM - 1) / TC_BM);
+    tc::k_gemm_tc<<<grid, 128, TC_SMEM, c->stream>>>(t);
+    c->launches += 1;
+    MK(cudaGetLastError());
+    return ESM_OK;
+}
+
+// K-major copy of a BF16 operand given by strides: out[r*ld + k] = X(r, k), X(r, k) at X[r*sr + k*sk]
+// with sr == 1 (the row index fastest: a transpose of the row-major [k, r] matrix)
+int kmajor(esm_mlp *c, const __nv_bfloat16 *X, int rows, int K, long long sk, __nv_bfloat16 *out) {
+    dim3 grid((rows + 31) / 32, (K + 31) / 32), block(32, 8);
+    tc::k_transpose_bf16<<<grid, block, 0, c->stream>>>(K, rows, X, (int)sk, out, K);
+    c->launches += 1;
+    MK(cudaGetLastError());
+    return ESM_OK;
+}
+
 int gemm(esm_mlp *c, GemmArgs g) {
+    if (c->gemm_kind == 1) {
+        // the tensor-core path takes K-major operands: A(m, k) rows of A, B(k, n) rows of B indexed by n
+        bool ak = g.sak == 1, bk = g.sbk == 1;
+        const __nv_bfloat16 *A = g.A, *B = g.B;
+        int lda = (int)g.sam, ldb = (int)g.sbn;
+        int rc;
+        if (!ak) {
+            if (g.sam != 1) return mfail(c, ESM_EINVAL, "GEMM operand A with neither stride 1");
+            if ((rc = kmajor(c, g.A, g.M, g.K, g.sak, c->tA))) return rc;
+            A = c->tA;
+            lda = g.K;
+        }
+        if (!bk) {
+            if (g.sbn != 1) return mfail(c, ESM_EINVAL, "GEMM operand B with neither stride 1");
+            if ((rc = kmajor(c, g.B, g.N, g.K, g.sbk, c->tB))) return rc;
+            B = c->tB;
+            ldb = g.K;
+        }
+        return gemm_tc(c, g, A, lda, B, ldb);
+    }
     dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
     k_gemm_bf16<<<grid, 128, 0, c->stream>>>(g);
     c->launches += 1;
     MK(cudaGetLastError());
+    return ESM_OK;
+}
+
+// a wait of the tensor-core GEMM ran out: the stream's results are not to be used
+int tc_check(esm_mlp *c) {
+    if (c->gemm_kind != 1) return ESM_OK;
+    int e = 0;
+    MK(cudaMemcpyAsync(&e, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MK(cudaStreamSynchronize(c->stream));
+    if (e) return mfail(c, ESM_ETIMEOUT, "a tensor-core GEMM wait ran out");
     return ESM_OK;
 }
 
@@ -323,6 +393,10 @@ int esm_mlp_create(int32_t nlayers, const int32_t *dims, int32_t batch_max, uint
     if ((rc = malloc_(c, &c->target, (size_t)batch_max * c->dims[nlayers]))) return rc;
     if ((rc = malloc_(c, &c->xin, (size_t)batch_max * c->dims[0]))) return rc;
     if ((rc = malloc_(c, &c->loss, 1))) return rc;
+    if ((rc = malloc_(c, &c->tA, (size_t)batch_max * dmax))) return rc;
+    if ((rc = malloc_(c, &c->tB, (size_t)batch_max * dmax))) return rc;
+    if ((rc = malloc_(c, &c->tc_err, 1))) return rc;
+    MK(cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     // He-style initialisation from a fixed LCG stream (host), zero biases
     uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
     for (int l = 0; l < nlayers; ++l) {
@@ -393,7 +467,7 @@ int esm_mlp_forward(esm_mlp *c, int32_t B, const float *x, float *y) {
     if (rc) return rc;
     if (y) MK(cudaMemcpyAsync(y, c->Z[c->nl - 1], sizeof(float) * B * dout, cudaMemcpyDeviceToHost, c->stream));
     MK(cudaStreamSynchronize(c->stream));
-    return ESM_OK;
+    return tc_check(c);
 }
 
 // One Adam step on a minibatch (x [B, d0], target [B, d_out]); gradients of the mean-squared loss
@@ -474,9 +548,17 @@ int esm_mlp_train_step(esm_mlp *c, int32_t B, const float *x, const float *targe
     MK(cudaMemcpyAsync(&L, c->loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MK(cudaStreamSynchronize(c->stream));
     if (loss_out) *loss_out = L;
-    return ESM_OK;
+    return tc_check(c);
 }
 
 int64_t esm_mlp_launch_count(const esm_mlp *c) { return c ? c->launches : 0; }
+
+int esm_mlp_set_gemm(esm_mlp *c, int32_t kind) {
+    if (!c) return ESM_EINVAL;
+    if (kind != 0 && kind != 1) return mfail(c, ESM_EINVAL, "GEMM kind must be 0 (mma.sync) or 1 (tcgen05)");
+    MK(cudaStreamSynchronize(c->stream));
+    c->gemm_kind = kind;
+    return ESM_OK;
+}
 
 }  // extern "C"

@@ -760,7 +760,7 @@ __global__ void __launch_bounds__(128, 8) k_plateau(const __grid_constant__ DevM
             double uc, uo, uj, un;
             uniform2(M.seed, ESM_TAG_SML, w0, (uint32_t)Ln.b0, (uint32_t)Ln.rep, sweep, &uc, &uo);
             bool guard;
-            real t = Ln.sample_line((real)uc, (real)uo, &guard);
+            real t = Ln.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), &guard);
             if (guard) ++guards;
             if (t != 0) {
                 bool any;
@@ -816,7 +816,7 @@ __global__ void __launch_bounds__(128, 8) k_storage_long(const __grid_constant__
             double uc, uo, uj, un;
             uniform2(M.seed, ESM_TAG_SLL, 2u * (uint32_t)m, (uint32_t)pu[0], (uint32_t)Ln.rep, sweep, &uc, &uo);
             bool guard;
-            real t = Ln.sample_line((real)uc, (real)uo, &guard);
+            real t = Ln.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), &guard);
             if (guard) ++guards;
             if (t != 0 && !Ln.lvl) {
                 bool any;

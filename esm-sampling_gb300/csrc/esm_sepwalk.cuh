@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(32 * WPB)
         double uc, uo;
         uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)W.tau, (uint32_t)W.rep, sweep, &uc, &uo);
         bool guard;
-        real t = W.sample_line((real)uc, (real)uo, &guard);
+        real t = W.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), &guard);
         if (guard) ++guards;
         if (t != 0) W.commit(t);
         if (M.mlog && W.rep < M.mlog_nrep && lane == 0)

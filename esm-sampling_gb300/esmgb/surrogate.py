@@ -14,7 +14,7 @@ import numpy as np
 from .device import EsmError, load
 
 EXPORTS = ("esm_mlp_create", "esm_mlp_destroy", "esm_mlp_last_error", "esm_mlp_set_layer", "esm_mlp_get_layer",
-           "esm_mlp_forward", "esm_mlp_train_step", "esm_mlp_launch_count")
+           "esm_mlp_forward", "esm_mlp_train_step", "esm_mlp_launch_count", "esm_mlp_set_gemm")
 
 P_f32 = C.POINTER(C.c_float)
 P_f64 = C.POINTER(C.c_double)
@@ -34,6 +34,7 @@ def _lib():
         L.esm_mlp_train_step.argtypes = [C.c_void_p, C.c_int32, P_f32, P_f32, C.c_float, P_f64, P_f32]
         L.esm_mlp_launch_count.restype = C.c_int64
         L.esm_mlp_launch_count.argtypes = [C.c_void_p]
+        L.esm_mlp_set_gemm.argtypes = [C.c_void_p, C.c_int32]
         L._mlp_bound = True
     return L
 
@@ -113,6 +114,10 @@ class MLP:
 
     def launch_count(self):
         return int(self.L.esm_mlp_launch_count(self.h))
+
+    def set_gemm(self, kind):
+        """1: tcgen05 tensor-core GEMMs (default), 0: the mma.sync kernel."""
+        self._check(self.L.esm_mlp_set_gemm(self.h, int(kind)), "esm_mlp_set_gemm")
 
 
 # ---------------------------------------------------------------------------------------------

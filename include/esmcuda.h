@@ -355,6 +355,9 @@ int esm_mlp_forward(esm_mlp *mlp, int32_t B, const float *x, float *y);
 int esm_mlp_train_step(esm_mlp *mlp, int32_t B, const float *x, const float *target, float lr,
                        double *loss_out, float *grads_out);
 int64_t esm_mlp_launch_count(const esm_mlp *mlp);
+/* the GEMM kernels of the MLP: 1 (default) the 5th-generation tensor cores (tcgen05.mma, FP32
+   accumulator in tensor memory, one 128 x 64 tile per CTA), 0 the warp-level mma.sync kernel */
+int esm_mlp_set_gemm(esm_mlp *mlp, int32_t kind);
 
 #ifdef __cplusplus
 }

@@ -143,3 +143,18 @@ def test_config1_moves_fp32(model, fp32_start, limit):
     assert frac <= 0.02
     assert all(f["margin"] <= (2e-2 if f["kind"] == "offset" else 5e-3) for f in flips), summary(flips)
     d.set_move_log(0)
+
+
+def test_config1_sweep_state_finite(model):
+    """Every state value stays finite over FP32 sweeps at the benchmarked size (about five of the
+    3.6e8 line moves of a sweep draw an offset uniform that rounds to 1 in FP32; they must not make
+    an infinite step), and so do the capacity scores."""
+    d = DeviceChain(model, R, precision=32, seed=SEED)
+    d.upload(initial_state(model, R, seed=7))
+    d.sweeps(2, 0)
+    s = d.download()
+    for k in ("theta", "g", "e"):
+        assert np.all(np.isfinite(s[k])), k
+    sk, fk, parts = d.scores()
+    assert np.all(np.isfinite(sk)) and np.all(np.isfinite(parts))
+    d.close()

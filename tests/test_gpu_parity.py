@@ -25,9 +25,9 @@ def task_flips(sd, so, m, tol_rel, tol_abs):
     """Fraction of (step, replica) entries whose state differs beyond tolerance, and the largest
     difference among the others."""
     bad = np.zeros((m.T, so["g"].shape[2]), bool)
-    th = _rel(sd["theta"], so["theta"], 1.0 + np.abs(so["theta"]).max()).max(0)
-    gg = np.abs(sd["g"] - so["g"]).max(0)
-    ee = np.abs(sd["e"] - so["e"]).max(0)
+    th = np.nan_to_num(_rel(sd["theta"], so["theta"], 1.0 + np.abs(so["theta"]).max()), nan=np.inf).max(0)
+    gg = np.nan_to_num(np.abs(sd["g"] - so["g"]), nan=np.inf).max(0)    # (a non-finite entry is a flip)
+    ee = np.nan_to_num(np.abs(sd["e"] - so["e"]), nan=np.inf).max(0)
     bad |= th > tol_rel
     bad |= gg > tol_abs
     bad |= ee > tol_abs
