@@ -76,8 +76,9 @@ struct esm_ctx {
     int *d_disp = nullptr, *d_ugroup = nullptr, *d_ugidx = nullptr, *d_ukind = nullptr, *d_uloc = nullptr;
     double *d_lo = nullptr, *d_hi = nullptr, *d_capex = nullptr;
     double *d_k = nullptr, *d_kold = nullptr, *d_knew = nullptr, *d_k1 = nullptr, *d_kmid = nullptr;
-    double *d_dk = nullptr, *d_sk = nullptr, *d_fk = nullptr, *d_parts = nullptr;
+    double *d_sums = nullptr, *d_sk = nullptr, *d_fk = nullptr, *d_sk_err = nullptr;
     double *d_score_part = nullptr;  // the chunk partials of the fused score pass
+    const double *last_sums = nullptr;  // the sums (and bounds) of the last score call
     double *d_w = nullptr, *d_eta = nullptr, *d_kappa = nullptr, *d_xi = nullptr;
     int *d_nclip = nullptr;
     unsigned long long *d_stats = nullptr;
@@ -104,6 +105,7 @@ struct esm_ctx {
     unsigned long long *d_sms_stats = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // a whole class pass, per class
     // weather
+    double *d_season = nullptr;  // cos, sin of the seasonal phase per step
     double *d_phi = nullptr, *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr, *d_Ptr = nullptr, *d_pi0 = nullptr;
     double *d_wbeta = nullptr, *d_wtheta = nullptr, *d_wxi = nullptr;
     int *d_moved = nullptr, *d_window = nullptr, *d_wstart = nullptr, *d_wflag = nullptr;
@@ -537,21 +539,23 @@ int alloc_shadow(esm_ctx *c) {
 
 // the capacity scores of the current state: the fused pass (partials in `partial`, sums in dk and
 // parts) and the finish into the context's sk and fk
-int scores_any(esm_ctx *c, double *partial, double *dk, double *parts) {
+// the score pass into partial and sums (esm::score_sum_doubles: dk, parts and their bounds), then
+// the scores and their bounds into d_sk, d_sk_err
+int scores_any(esm_ctx *c, double *partial, double *sums) {
     Span sp(c, ESM_KT_SCORE);
     if (c->precision == 64) {
-        CK(esm::launch_scores_fused<double>(c->Md, c->Md.theta, c->Md.g, c->Md.e, c->Md.z, partial, dk, parts,
-                                            c->stream));
+        CK(esm::launch_scores_fused<double>(c->Md, c->Md.theta, c->Md.g, c->Md.e, c->Md.z, partial, sums, c->stream));
     } else {
+        // the FP64 capacities of the balances recomputed in FP64 near 0
         CK(esm::launch_set_kc<double>(c->K, c->d_k, c->d_lo, c->d_hi, c->d_ukind, c->d_uloc, (double *)c->Md.kc_d,
                                       (double *)c->Md.kc_s, (double *)c->Md.kc_r, c->stream));
-        CK(esm::launch_scores_fused<float>(c->Md, c->Mf.theta, c->Mf.g, c->Mf.e, c->Mf.z, partial, dk, parts,
-                                           c->stream));
+        CK(esm::launch_scores_f32(c->Mf, c->Md, partial, sums, c->stream));
         c->launches += 1;
     }
     CK(esm::launch_score_finish<double>(c->Md, c->d_k, c->d_lo, c->d_hi, c->d_capex, c->gamma_k, c->beta_k,
-                                        c->physical, dk, c->d_sk, c->d_fk, parts, c->stream));
+                                        c->physical, sums, c->d_sk, c->d_sk_err, c->d_fk, c->stream));
     c->launches += 3;
+    c->last_sums = sums;
     return ESM_OK;
 }
 
@@ -772,11 +776,11 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         *pp = dp;
     }
     if ((rc = dalloc(c, &c->d_score_part, esm::score_partial_doubles(c->T, c->R, c->K, c->N)))) return rc;
-    for (double **pp : {&c->d_dk, &c->d_sk}) {
+    for (double **pp : {&c->d_sk, &c->d_sk_err}) {
         if ((rc = dalloc(c, &dp, (size_t)c->R * K))) return rc;
         *pp = dp;
     }
-    if ((rc = dalloc(c, &c->d_parts, (size_t)c->R * 8))) return rc;
+    if ((rc = dalloc(c, &c->d_sums, esm::score_sum_doubles(c->R, K)))) return rc;
     if ((rc = dalloc(c, &c->d_w, c->R))) return rc;
     if ((rc = dalloc(c, &c->d_eta, 64))) return rc;
     if ((rc = dalloc(c, &c->d_kappa, 64))) return rc;
@@ -790,6 +794,9 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
     if ((rc = upload(c, &c->d_mu, m->mu, nr * n0 * 3))) return rc;
     if ((rc = upload(c, &c->d_sig, m->sig, nr * n0))) return rc;
     if ((rc = upload(c, &c->d_sig0, m->sig0, n0))) return rc;
+    if ((rc = dalloc(c, &c->d_season, 2 * (size_t)c->T))) return rc;
+    esm::k_season<<<(c->T + 255) / 256, 256, 0, c->stream>>>(c->T, c->d_season);
+    CK(cudaGetLastError());
     if ((rc = upload(c, &c->d_Ptr, m->Ptr, nr * nr))) return rc;
     if ((rc = upload(c, &c->d_pi0, m->pi0, nr))) return rc;
     if ((rc = dalloc(c, &c->d_wbeta, (size_t)c->R * nr * c->T))) return rc;
@@ -1127,13 +1134,27 @@ int esm_operation_sweeps(esm_ctx *c, int32_t n, int64_t sweep0, int64_t *stats) 
 int esm_capacity_scores(esm_ctx *c, double *sk, double *fk, double *parts) {
     if (!c) return ESM_EINVAL;
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
-    int rc = scores_any(c, c->d_score_part, c->d_dk, c->d_parts);
+    int rc = scores_any(c, c->d_score_part, c->d_sums);
     if (rc) return rc;
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * c->R * c->K, cudaMemcpyDeviceToHost, c->stream));
     if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * c->K, cudaMemcpyDeviceToHost, c->stream));
-    if (parts) CK(cudaMemcpyAsync(parts, c->d_parts, sizeof(double) * c->R * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (parts)
+        CK(cudaMemcpyAsync(parts, c->d_sums + (size_t)c->R * c->K, sizeof(double) * c->R * 8, cudaMemcpyDeviceToHost,
+                           c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->has_scores = true;
+    return ESM_OK;
+}
+
+int esm_score_errors(esm_ctx *c, double *sk_err, double *parts_err) {
+    if (!c) return ESM_EINVAL;
+    if (!c->has_scores || !c->last_sums) return fail(c, ESM_ESTATE, "no scores computed since the last state change");
+    size_t RK = (size_t)c->R * c->K;
+    if (sk_err) CK(cudaMemcpyAsync(sk_err, c->d_sk_err, sizeof(double) * RK, cudaMemcpyDeviceToHost, c->stream));
+    if (parts_err)
+        CK(cudaMemcpyAsync(parts_err, c->last_sums + 2 * RK + (size_t)c->R * 8, sizeof(double) * c->R * 8,
+                           cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return ESM_OK;
 }
 
@@ -1175,10 +1196,10 @@ int follow_any(esm_ctx *c, double kappa_min) {
 // in the call: a caller whose device memory is owned by a caching allocator (PyTorch's, a memory
 // pool with a hard cap) -- cudaMalloc behind its back fails or fragments once the pool holds the
 // device -- and a caller whose step must not stall, as cudaMalloc/cudaFree can synchronise the
-// device. The score accumulators (the R x K score sums and the R x 8 cost parts) live in one
-// file-scope device array instead of buffers of the context.
+// device. The score accumulators (the R x K score sums, the R x 8 cost parts and their bounds) live
+// in one file-scope device array instead of buffers of the context.
 //   Limit: the fused pass's chunk partials (esm::score_partial_doubles, which takes fewer chunks to
-//   fit) and the R * (K + 8) sums within ESM_SCORE_SCRATCH_DOUBLES (8 MiB); larger contexts get
+//   fit) and the 2 * R * (K + 8) sums within ESM_SCORE_SCRATCH_DOUBLES (8 MiB); larger contexts get
 //   ESM_EINVAL.
 //   Set-up: esm_create, which allocates anyway, resolves the array's address on the context's
 //   device (cudaGetSymbolAddress, with that device current) and loads the score kernels, so the
@@ -1210,18 +1231,19 @@ int esm_capacity_scores_static(esm_ctx *c, double *sk, double *fk, double *parts
     if (!c) return ESM_EINVAL;
     if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
     size_t R = c->R, K = c->K;
-    size_t npart = esm::score_partial_doubles(c->T, c->R, c->K, c->N), need = npart + R * (K + 8);
+    size_t npart = esm::score_partial_doubles(c->T, c->R, c->K, c->N), nsum = esm::score_sum_doubles(c->R, c->K);
+    size_t need = npart + nsum;
     if (need > (size_t)ESM_SCORE_SCRATCH_DOUBLES)
-        return fail(c, ESM_EINVAL, "%zu doubles of score scratch needed (R*(K+8) = %zu), the static scratch holds %d",
-                    need, R * (K + 8), ESM_SCORE_SCRATCH_DOUBLES);
+        return fail(c, ESM_EINVAL, "%zu doubles of score scratch needed (2*R*(K+8) = %zu), the static scratch holds %d",
+                    need, nsum, ESM_SCORE_SCRATCH_DOUBLES);
     int dev = -1, rc;
     CK(cudaGetDevice(&dev));
     if (dev != c->device || !c->score_scratch)
         return fail(c, ESM_EINVAL, "device %d is current, the context was created on device %d", dev, c->device);
-    // the partials, then the summed gradient and the cost parts; every element is written by the
-    // pass before it is read, so nothing carries over from an earlier call
-    double *part = c->score_scratch, *dk = part + npart, *pd = dk + R * K;
-    if ((rc = scores_any(c, part, dk, pd))) return rc;
+    // the partials, then the summed gradient, the cost parts and their bounds; every element is
+    // written by the pass before it is read, so nothing carries over from an earlier call
+    double *part = c->score_scratch, *sums = part + npart, *pd = sums + R * K;
+    if ((rc = scores_any(c, part, sums))) return rc;
     if (sk) CK(cudaMemcpyAsync(sk, c->d_sk, sizeof(double) * R * K, cudaMemcpyDeviceToHost, c->stream));
     if (fk) CK(cudaMemcpyAsync(fk, c->d_fk, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
     if (parts) CK(cudaMemcpyAsync(parts, pd, sizeof(double) * R * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1296,10 +1318,10 @@ int esm_weather_step(esm_ctx *c, const int32_t *moved, const double *theta, cons
     Span sp(c, ESM_KT_WEATHER);
     if (anyt) {  // pCN in the innovations at the current regimes
         if (c->precision == 64)
-            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
+            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_season, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
                                              c->d_reg, c->d_reg, dxi, c->seed, (uint32_t)it, 1, c->stream));
         else
-            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
+            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_season, c->d_sig, c->d_sig0, c->d_moved, c->d_wtheta,
                                             c->d_reg, c->d_reg, dxi, c->seed, (uint32_t)it, 1, c->stream));
         c->launches += 1;
     }
@@ -1309,10 +1331,10 @@ int esm_weather_step(esm_ctx *c, const int32_t *moved, const double *theta, cons
                                                                   c->d_wbeta, c->seed, (uint32_t)it);
         CK(cudaGetLastError());
         if (c->precision == 64)
-            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
+            CK(esm::launch_weather_z<double>(c->Md, c->d_phi, c->d_mu, c->d_season, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
                                              c->d_reg, c->d_reg2, nullptr, c->seed, (uint32_t)it, 0, c->stream));
         else
-            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
+            CK(esm::launch_weather_z<float>(c->Mf, c->d_phi, c->d_mu, c->d_season, c->d_sig, c->d_sig0, c->d_wflag, c->d_wtheta,
                                             c->d_reg, c->d_reg2, nullptr, c->seed, (uint32_t)it, 0, c->stream));
         CK(cudaMemcpyAsync(c->d_reg, c->d_reg2, sizeof(int32_t) * c->T * R, cudaMemcpyDeviceToDevice, c->stream));
         c->launches += 2;

@@ -5,15 +5,12 @@
 #include "esm_plateau.cuh"
 
 namespace esm {
-template cudaError_t launch_scores_fused<float>(const DevModel<double> &, const float *, const float *, const float *,
-                                                const float *, double *, double *, double *, cudaStream_t);
 template cudaError_t launch_scores_fused<double>(const DevModel<double> &, const double *, const double *,
-                                                 const double *, const double *, double *, double *, double *,
-                                                 cudaStream_t);
+                                                 const double *, const double *, double *, double *, cudaStream_t);
 cudaError_t preload_score_kernels() {
     cudaFuncAttributes a;
     cudaError_t e;
-    if ((e = cudaFuncGetAttributes(&a, k_scores_fused<float>)) != cudaSuccess) return e;
+    if ((e = preload_scores_f32()) != cudaSuccess) return e;
     if ((e = cudaFuncGetAttributes(&a, k_scores_fused<double>)) != cudaSuccess) return e;
     if ((e = cudaFuncGetAttributes(&a, k_score_reduce)) != cudaSuccess) return e;
     if ((e = cudaFuncGetAttributes(&a, k_score_finish<double>)) != cudaSuccess) return e;
@@ -34,17 +31,18 @@ template size_t sep_region_bytes<double>(const DevModel<double> &);
 template int sep_warps_per_sm<double>(const DevModel<double> &, int *);
 template int linemove_blocks_per_sm<double>(const DevModel<double> &, int);
 template cudaError_t launch_rebuild<double>(const DevModel<double> &, cudaStream_t);
-template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *, const double *,
-                                                const double *, double, double, int, double *, double *, double *,
-                                                double *, cudaStream_t);
+template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *,
+                                                const double *, const double *, double, double, int, double *,
+                                                double *, double *, double *, cudaStream_t);
 template cudaError_t launch_follow_disp<double>(const DevModel<double> &, const int *, const double *, const double *,
                                                const double *, const double *, cudaStream_t);
 template cudaError_t launch_kop<double>(const DevModel<double> &, const double *, const double *, const double *,
                                        const double *, double, cudaStream_t);
 template cudaError_t launch_set_kc<double>(int, const double *, const double *, const double *, const int *,
                                           const int *, double *, double *, double *, cudaStream_t);
-template cudaError_t launch_weather_z<double>(const DevModel<double> &, const double *, const double *, const double *,
-                                             const double *, const int *, const double *, const int *, const int *,
-                                             const double *, uint64_t, uint32_t, int, cudaStream_t);
+template cudaError_t launch_weather_z<double>(const DevModel<double> &, const double *, const double *,
+                                             const double *, const double *, const double *, const int *,
+                                             const double *, const int *, const int *, const double *, uint64_t,
+                                             uint32_t, int, cudaStream_t);
 template cudaError_t launch_compensate<double>(const DevModel<double> &, const int *, const double *, cudaStream_t);
 }  // namespace esm

@@ -21,8 +21,8 @@ NSTAT = 2 * (NFAM + 1) + 1
 EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "esm_download_state",
            "esm_rebuild_caches", "esm_download_caches", "esm_operation_sweeps", "esm_class_pass",
            "esm_capacity_scores", "esm_langevin_step", "esm_weather_step", "esm_sync", "esm_launch_count",
-           "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_follow_capacities",
-           "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
+           "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_score_errors",
+           "esm_follow_capacities", "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
            "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe", "esm_set_sep_walk",
            "esm_sep_walk", "esm_set_move_log", "esm_move_log")
 TUNE_MAX = 16  # ESM_TUNE_MAX
@@ -65,6 +65,7 @@ def load(build_if_missing=True):
     L.esm_class_pass.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, P_i64]
     L.esm_capacity_scores.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
     L.esm_capacity_scores_static.argtypes = [C.c_void_p, P_f64, P_f64, P_f64]
+    L.esm_score_errors.argtypes = [C.c_void_p, P_f64, P_f64]
     L.esm_follow_capacities.argtypes = [C.c_void_p, P_f64, C.c_double, P_f64]
     L.esm_state_save.argtypes = [C.c_void_p]
     L.esm_state_restore.argtypes = [C.c_void_p]
@@ -215,6 +216,15 @@ class DeviceChain:
         self._check(self.L.esm_capacity_scores_static(self.h, _p(sk), _p(fk), _p(parts)),
                     "esm_capacity_scores_static")
         return sk, fk, parts
+
+    def score_errors(self):
+        """esm_score_errors: bounds on the distance of the last scores [R, K] and cost parts [R, 8] from
+        the exact sums over the same state."""
+        m, R = self.m, self.R
+        ek = np.zeros((R, m.Kunits))
+        ep = np.zeros((R, 8))
+        self._check(self.L.esm_score_errors(self.h, _p(ek), _p(ep)), "esm_score_errors")
+        return ek, ep
 
     def follow_capacities(self, knew, kmin=1.0):
         """esm_follow_capacities: every replica follows the capacities to knew; returns the new k."""

@@ -206,18 +206,27 @@ int esm_storage_long(esm_ctx *ctx, int64_t sweep, int64_t *stats);
    capex force fk [K] (beta_k dK/dk), capacity_scores (src/replicas.jl:329) on energy_cost with
    grad (src/energy.jl:551) and log_measure_grad (:811). parts (may be NULL): [R*8] cost parts
    per replica: capex, op, gen, storage, shed, dump, penalty, 0 (CostParts, src/energy.jl:531).
-   One pass over the state computes every node balance and term in FP64 (from the FP32 state in
-   the production build) and sums them in a fixed order: the same state gives the same scores bit
-   for bit. */
+   One pass over the state, summed in a fixed order: the same state gives the same scores bit for
+   bit. The FP64 build forms every node balance and term in FP64. The FP32 production build forms
+   them in FP32 from its FP32 state and sums them with compensated (Neumaier) sums; the sign of a
+   node balance within its rounding bound of 0 is taken from the FP64 balance. Every score and cost
+   part carries a bound on its distance from the exact sums (esm_score_errors). */
 int esm_capacity_scores(esm_ctx *ctx, double *sk, double *fk, double *parts);
+
+/* The error bounds of the last esm_capacity_scores (or _static) call: sk_err [R*K] bounds
+   |sk - s_exact|, parts_err [R*8] bounds the cost parts, where s_exact are the same sums taken
+   exactly over the same state (running error analysis of the terms' and the sums' rounding).
+   Either may be NULL. ESM_ESTATE when the state changed since the last scores. */
+int esm_score_errors(esm_ctx *ctx, double *sk_err, double *parts_err);
 
 /* esm_capacity_scores without allocating in the call (no counterpart in the reference): for a
    caller that must not allocate device memory here -- one whose device memory is held by a caching
    allocator or a capped pool, or whose step must not stall on cudaMalloc/cudaFree. The score
-   accumulators -- the partial sums of the score pass over step chunks and the R*(K+8) totals --
+   accumulators -- the partial sums of the score pass over step chunks and the 2*R*(K+8) totals
+   and bounds --
    live in a file-scope device array of ESM_SCORE_SCRATCH_DOUBLES doubles (8 MiB); the pass takes
    fewer chunks where that is needed to fit (the same chunks as esm_capacity_scores, so both give the
-   same scores bit for bit), and contexts that do not fit even with one chunk (R*(K+8) near 2^20)
+   same scores bit for bit), and contexts that do not fit even with one chunk (2*R*(K+8) near 2^20)
    are rejected with ESM_EINVAL. esm_create, which allocates anyway, resolves
    the array's address on the context's device and loads the score kernels, so the call places
    nothing on the device; it must be made with the context's device current (else ESM_EINVAL). The

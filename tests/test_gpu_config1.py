@@ -158,3 +158,20 @@ def test_config1_sweep_state_finite(model):
     sk, fk, parts = d.scores()
     assert np.all(np.isfinite(sk)) and np.all(np.isfinite(parts))
     d.close()
+
+
+def test_config1_weather_finite(model):
+    """The weather anomalies stay finite over FP32 weather steps of every replica at the benchmarked
+    size: a step draws n0 * T * R normals, some of whose uniforms round to 1 in FP32 (a Box-Muller
+    radius from log(1 - u) must not become infinite and spread along the VAR recursion)."""
+    d = DeviceChain(model, R, precision=32, seed=SEED)
+    d.upload(initial_state(model, R, seed=7))
+    moved = np.ones(R, np.int32)
+    theta = np.full(R, 0.7)
+    window = np.zeros(R, np.int32)
+    wstart = np.ones(R, np.int32)
+    for it in range(1, 9):
+        d.weather_step(moved, theta, window, wstart, it=it)
+    s = d.download()
+    assert np.all(np.isfinite(s["z"])) and np.all(np.isfinite(s["g"]))
+    d.close()

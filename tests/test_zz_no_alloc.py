@@ -77,7 +77,7 @@ def test_static_scores_first_call_allocates_nothing(prec):
 
 def test_static_scores_size_limit():
     m = make_model(40, 60, 2, seed=11)
-    R = (1 << 20) // (m.Kunits + 8) + 1    # one replica beyond the static scratch
+    R = (1 << 19) // (m.Kunits + 8) + 1    # one replica beyond the static scratch (2 R (K + 8) sums)
     d = DeviceChain(m, R, precision=64, seed=5)
     d.upload(_state(m, R))
     with pytest.raises(EsmError, match="static scratch holds"):
