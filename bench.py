@@ -333,6 +333,99 @@ def profile_case(args):
                       "moves_tried": int(st[:-1:2].sum()), "guards": int(st[-1])}), flush=True)
 
 
+def learned_case(args):
+    """Long capacity chains of the plain step and the learned capacity steps on a reduced-T model of
+    the learned-proposal configuration (40 nodes, 60 lines, --T steps, default 120, --R replicas,
+    default 64; surrogate 3 x 512, minibatches of 1024, Adam 1e-3, 4x the plain step): --warmup plain
+    steps that train the surrogate (2 Adam steps per pair), then --ess-steps steps per arm, every arm
+    from the same saved state over the same weather schedule, one plain evaluation per step. Per arm:
+    the bulk ESS of every carrier total (src/convergence.jl:125) and its minimum per second, the
+    mean squared jump of the log carrier totals, the carrier means with their MCSE, and the shift of
+    each mean from the plain arm's in MCSE units.
+      plain    the plain step (device Langevin step, langevin_update, src/replicas.jl:368)
+      plain4   the plain step at 4x its size and clip
+      sur1     SurrogateLangevin with its judge (falls back to the plain step where the surrogate
+               disagrees with the plain estimates beyond their noise)
+      surinf   SurrogateLangevin with the judge off (the surrogate's drift whenever it is trained)"""
+    from esmgb import build as B
+    B.build()
+    from esmgb.convergence import ess_bulk
+    from esmgb.device import DeviceChain
+    from esmgb.model import LANGEVIN_KAPPA, initial_state, make_model
+    from esmgb.replicas import ReplicaCtl, replica_schedule
+    from esmgb.surrogate import ScoreSurrogate, SurrogateLangevin
+    T, R, N, W = args.T or 120, args.R or 64, args.ess_steps, args.warmup
+    m = make_model(40, 60, T, seed=5)
+    eta = np.full(len(m.carriers), 5e-4)
+    ks = np.array([LANGEVIN_KAPPA.get(c, 100.0) for c in m.carriers])
+    ug = np.asarray(m.unit_group)
+    d = DeviceChain(m, R, precision=32, seed=3)
+    d.upload(initial_state(m, R, seed=7))
+    ctl = ReplicaCtl(M=R)
+    w = np.full(R, 1.0 / R)
+    rng = np.random.Generator(np.random.PCG64(1))
+    sched = [replica_schedule(ctl, it, R, T, rng) for it in range(W + N + 1)]
+    sur = ScoreSurrogate(m, hidden=(512, 512, 512), capacity=8192, batch=1024, lr=1e-3, seed=1)
+    t0 = time.perf_counter()
+    for it in range(W):
+        mv, th, win, ws, _ = sched[it]
+        if mv.any():
+            d.weather_step(mv, th, win, ws, it=it)
+        d.sweeps(1, sweep0=it, stats=False)
+        sk, fk, _ = d.scores()
+        sur.add(d.download_k(), d.regime_occupancy(), w @ sk)
+        sur.train(2)
+        d.langevin_step(w, eta, ks, 1.0, 0.02, True, None, it)
+    d.sync(600.0)
+    out = {"case": "learned", "workload": f"40 nodes, 60 lines, T={T}, {R} replicas", "warmup_steps": W,
+           "warmup_s": time.perf_counter() - t0, "steps_per_arm": N, "arms": {}}
+    d.state_save()
+    for arm in [a for a in (args.arms or "plain,plain4,sur1,surinf").split(",") if a]:
+        d.state_restore()
+        kt = []
+        t0 = time.perf_counter()
+        st = None
+        if arm.startswith("plain"):
+            mult = 4.0 if arm == "plain4" else 1.0
+            for q in range(N):
+                it = W + q
+                mv, th, win, ws, _ = sched[it]
+                if mv.any():
+                    d.weather_step(mv, th, win, ws, it=it)
+                d.sweeps(1, sweep0=it, stats=False)
+                d.scores()
+                k, _ = d.langevin_step(w, mult * eta, ks, 1.0, mult * 0.02, True, None, it)
+                kt.append(carrier_totals(m, k))
+        else:
+            tol = {"sur1": 1.0, "surinf": float("inf")}[arm]
+            sl = SurrogateLangevin(d, m, sur, eta, ks, 1.0, 0.02, mult=4.0, seed=3, train_steps=2, tol=tol)
+            for q in range(N):
+                sl.step(W + q, sched[W + q])
+                kt.append(carrier_totals(m, sl.k))
+            st = dict(sl.stats)
+        d.sync(600.0)
+        secs = time.perf_counter() - t0
+        kt = np.asarray(kt)
+        ess = {c: (float(ess_bulk([kt[:, i]])) if np.ptp(kt[:, i]) > 0 and np.all(np.isfinite(kt[:, i])) else 0.0)
+               for i, c in enumerate(m.carriers)}
+        r = {"seconds": secs, "ess": ess, "ess_min": min(ess.values()), "ess_per_s": min(ess.values()) / secs,
+             "msjd_log_ktot": float(np.mean(np.sum(np.diff(np.log(kt), axis=0) ** 2, axis=1))),
+             "mean": {c: float(kt[:, i].mean()) for i, c in enumerate(m.carriers)},
+             "mcse": {c: float(kt[:, i].std() / np.sqrt(max(ess[c], 1.0))) for i, c in enumerate(m.carriers)}}
+        if st:
+            r["stats"] = st
+        out["arms"][arm] = r
+    sur.close()
+    p = out["arms"].get("plain")
+    if p:
+        for arm, r in out["arms"].items():
+            if arm != "plain":
+                r["shift_mcse"] = {c: (r["mean"][c] - p["mean"][c]) / math.hypot(r["mcse"][c], p["mcse"][c])
+                                   for c in m.carriers}
+                r["ess_per_s_over_plain"] = r["ess_per_s"] / p["ess_per_s"]
+    print(json.dumps(out), flush=True)
+
+
 def mlp_case(args):
     """The surrogate's training step at the full form's sizes (5 hidden layers of 1024 between the
     256-node model's 1357 capacities plus the 8-dim regime summary and its 1357 scores, minibatches of
@@ -386,13 +479,15 @@ def storage_case(args):
 
 
 def batch_case(args):
-    """Many independent models of uneven size on one GPU: N ~ U{10..128}, L = 1.5 N,
-    T in {1460, 2920, 8760}, 16 replicas each (seed-fixed). Every model is a context with its own
-    stream and graph-captured class passes; the host enqueues one sweep on every context, then waits
-    for all, so the models' kernels overlap on the GPU."""
+    """Many independent models of uneven size on one GPU (the batching configuration): N ~ U{10..128},
+    L = 1.5 N, T in {1460, 2920, 8760}, 16 replicas each (seed-fixed). Default: one esm_batch over
+    the models' contexts -- one captured graph per sweep, one line-move launch per move index over
+    the tasks of every model, the grid picked by the batch's autotuner (untimed); --batch-mode
+    streams: every model's own graph-captured sweep on its own stream, the host enqueuing one sweep
+    on every context before waiting for all. The timed region is --steps sweeps of every model."""
     from esmgb import build as B
     B.build()
-    from esmgb.device import DeviceChain
+    from esmgb.device import DeviceBatch, DeviceChain
     from esmgb.model import initial_state, make_model
     rng = np.random.default_rng(2024)
     nm = args.models
@@ -403,26 +498,48 @@ def batch_case(args):
         m = make_model(N, int(round(1.5 * N)), T, seed=1000 + i)
         d = DeviceChain(m, 16, precision=32, seed=1000 + i)
         d.upload(initial_state(m, 16, seed=7))
-        if args.grid:
+        if args.grid and args.batch_mode == "streams":
             d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
         chains.append((m, d))
     setup = time.perf_counter() - t0
-    for m, d in chains:                       # warm-up: captures each context's class graphs
-        d.sweeps(args.warmup, 0, stats=False)
-    for m, d in chains:
-        d.sync(600.0)
-    t0 = time.perf_counter()
-    for s in range(args.steps):
-        for m, d in chains:
-            d.sweeps(1, args.warmup + s, stats=False)
-    for m, d in chains:
-        d.sync(600.0)
-    dt = time.perf_counter() - t0
+    out = {"case": "batch", "mode": args.batch_mode, "models": nm, "replicas": 16, "sweeps": args.steps}
     moves = sum((sum(len(a.ptr) - 1 for a in m.atoms) + round(4.0 * m.N)) * m.T * 16 for m, _ in chains)
-    print(json.dumps({"case": "batch", "models": nm, "replicas": 16, "sweeps": args.steps,
-                      "model_sweeps_per_s": nm * args.steps / dt, "line_moves_per_s": moves * args.steps / dt,
-                      "wall_s": dt, "setup_s": setup,
-                      "sizes": {"N": [n for n, _ in specs], "T": [t for _, t in specs]}}), flush=True)
+    if args.batch_mode == "batch":
+        bt = DeviceBatch([d for _, d in chains])
+        t1 = time.perf_counter()
+        if args.grid:
+            bt.set_grid(*(int(x) for x in args.grid.lower().split("x")))
+        else:
+            best, cand = bt.autotune(sweep=0)
+            out["autotune_ms"] = {f"{a}x{b}": round(v, 2) for (a, b), v in cand.items()}
+        out["autotune_s"] = time.perf_counter() - t1
+        out["grid"] = list(bt.grid()[:2])
+        bt.sweeps(args.warmup, 0, stats=False)           # captures the batch's sweep graph
+        l0 = bt.launch_count()
+        t0 = time.perf_counter()
+        st = bt.sweeps(args.steps, args.warmup)
+        dt = time.perf_counter() - t0
+        dev = bt.last_ms() / 1e3
+        out.update({"model_sweeps_per_s": nm * args.steps / dev, "line_moves_per_s": moves * args.steps / dev,
+                    "device_s": dev, "wall_s": dt, "gpu_launches": bt.launch_count() - l0,
+                    "guards": int(st[:, -1].sum()), "moves_tried": int(st[:, :-1:2].sum())})
+        bt.close()
+    else:
+        for m, d in chains:                       # warm-up: captures each context's class graphs
+            d.sweeps(args.warmup, 0, stats=False)
+        for m, d in chains:
+            d.sync(600.0)
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            for m, d in chains:
+                d.sweeps(1, args.warmup + s, stats=False)
+        for m, d in chains:
+            d.sync(600.0)
+        dt = time.perf_counter() - t0
+        out.update({"model_sweeps_per_s": nm * args.steps / dt, "line_moves_per_s": moves * args.steps / dt,
+                    "wall_s": dt})
+    out.update({"setup_s": setup, "sizes": {"N": [n for n, _ in specs], "T": [t for _, t in specs]}})
+    print(json.dumps(out), flush=True)
 
 
 def n256_case(args):
@@ -539,7 +656,7 @@ def ess_case(args):
     device_loop(d, m, ctl, 1, args.warmup, rng, None)
     d.sync(3600.0)
     warm = time.perf_counter() - t0
-    arms = tuple(a for a in args.arms.split(",") if a)
+    arms = tuple(a for a in (args.arms or "plain,learned,da").split(",") if a)
     res = ess_arms(d, m, ctl, 1 + args.warmup, args.ess_steps, arms=arms)
     out = {"case": "ess", "workload": config_dict()["workload"], "warmup_steps": args.warmup, "warmup_s": warm,
            "steps_per_arm": args.ess_steps, "capacity_ess_per_s": {a: v["value"] for a, v in res.items()},
@@ -579,6 +696,8 @@ def main():
     ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--batch-mode", default="batch", choices=["batch", "streams"],
+                    help="--case batch: one esm_batch (default) or every model on its own stream")
     ap.add_argument("--ess-steps", type=int, default=32,
                     help="steps of each arm of the capacity ESS/s measurement (plain, learned, delayed "
                          "acceptance); 0: none")
@@ -588,10 +707,11 @@ def main():
     ap.add_argument("--grid", default="", help="line-move grid WPBxWPS (warps per block x per SM) instead of "
                                                "the autotuner's choice")
     ap.add_argument("--cpu-moves", type=int, default=64, help="--case n256: moves of the oracle's sample")
-    ap.add_argument("--arms", default="plain,learned,da", help="--case ess: the arms measured")
+    ap.add_argument("--arms", default="", help="the arms measured: --case ess (default plain,learned,da), "
+                    "--case learned (default plain,plain4,sur1,surinf)")
     ap.add_argument("--sep", type=int, default=0, help="--case small: cooperative walk of separable moves of "
                                                      "at least this many units (0: off)")
-    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage", "n256", "ess", "mlp"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "batch", "storage", "n256", "ess", "mlp", "learned"],
                     help="small: the reduced profiling case (sweeps only, no JSON contract line)")
     args = ap.parse_args()
     if args.case == "small":
@@ -606,6 +726,8 @@ def main():
         return ess_case(args)
     if args.case == "mlp":
         return mlp_case(args)
+    if args.case == "learned":
+        return learned_case(args)
     rank, world, local = rank_info()
     if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)

@@ -644,22 +644,7 @@ int class_pass_any(esm_ctx *c, uint32_t sweep, int cls, int limit = 0) {
 }
 
 void class_order(const esm_ctx *c, uint32_t sweep, int order[3], int *ncls) {
-    double u0, u1;
-    esm::uniform2(c->seed, ESM_TAG_SWEEP, 0, 0, 0, sweep, &u0, &u1);
-    if (c->T % 2 == 0) {
-        *ncls = 2;
-        order[0] = u0 < 0.5 ? 0 : 1;
-        order[1] = 1 - order[0];
-    } else {
-        *ncls = 3;
-        order[0] = 0;
-        order[1] = 1;
-        order[2] = 2;
-        int j = std::min(2, (int)floor(u0 * 3));
-        std::swap(order[2], order[j]);
-        j = std::min(1, (int)floor(u1 * 2));
-        std::swap(order[1], order[j]);
-    }
+    esm::class_order_of(c->seed, c->T, sweep, order, ncls);
 }
 
 int stats_out(esm_ctx *c, int64_t *stats) {
@@ -1728,4 +1713,359 @@ int esm_regime_occupancy(esm_ctx *c, double *occ) {
     CK(cudaStreamSynchronize(c->stream));
     for (int i = 0; i < n; ++i) occ[i] = (double)h[i] / (double)TR;
     return ESM_OK;
+}
+
+// =============================================================================================
+// A batch of chains whose operation sweeps run together (esm_batch_*)
+// =============================================================================================
+struct esm_batch {
+    int n = 0, precision = 32;
+    std::string err;
+    std::vector<esm_ctx *> ctx;   // in launch order: decreasing move count
+    std::vector<int> pos;         // pos[i]: the caller's index of ctx[i]
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<int> nact;        // per move index: the models that have it
+    esm::BatchLaunch bl{};
+    void *d_models = nullptr;     // BatchModel<real>[n]
+    uint32_t *d_sweep = nullptr;
+    int nsm = 0, cap[2] = {0, 0};
+    int scratch_warps = 0;        // warps the global walk slabs hold
+    cudaGraphExec_t graph = nullptr;
+    float last_ms = 0;
+    int64_t launches = 0;         // kernels launched by the batch's sweeps
+    std::vector<void *> allocs;
+};
+
+namespace {
+int bfail(esm_batch *b, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    return code;
+}
+
+#define BCK(call)                                                                                \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return bfail(b, e_ == cudaErrorMemoryAllocation ? ESM_ENOMEM : ESM_ECUDA, "%s: %s (%s:%d)", #call, \
+                         cudaGetErrorString(e_), __FILE__, __LINE__);                            \
+    } while (0)
+
+template <class T>
+int balloc(esm_batch *b, T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (n ? n : 1));
+    if (e != cudaSuccess) return bfail(b, ESM_ENOMEM, "cudaMalloc of %zu bytes: %s", sizeof(T) * n, cudaGetErrorString(e));
+    b->allocs.push_back(q);
+    *p = (T *)q;
+    return ESM_OK;
+}
+
+template <class real>
+const esm::DevModel<real> &ctx_model(const esm_ctx *c);
+template <>
+const esm::DevModel<float> &ctx_model<float>(const esm_ctx *c) { return c->Mf; }
+template <>
+const esm::DevModel<double> &ctx_model<double>(const esm_ctx *c) { return c->Md; }
+
+// the batch's device tables, grid limits and walk slabs
+template <class real>
+int batch_setup(esm_batch *b) {
+    int n = b->n, rc;
+    std::vector<esm::BatchModel<real>> hm(n);
+    size_t maxstride = 0, maxlane = 0;
+    b->bl.maxpass = 0;
+    for (int i = 0; i < n; ++i) {
+        esm_ctx *c = b->ctx[i];
+        esm::BatchModel<real> &m = hm[i];
+        m.M = ctx_model<real>(c);
+        m.M.mlog = nullptr;
+        m.M.mlog_nrep = 0;
+        for (int k = 0; k < 3; ++k) {
+            m.steps[k] = c->d_steps[k];
+            m.nsteps[k] = k < (int)c->class_len.size() ? c->class_len[k] : 0;
+        }
+        m.nmoves = m.M.natoms + m.M.nextra;
+        m.descs = c->d_descs;
+        m.stride = esm::linemove_smem_per_warp<real>(m.M);
+        m.stats = c->d_stats;
+        maxstride = std::max(maxstride, m.stride);
+        maxlane = std::max(maxlane, esm::linemove_scratch_reals<real>(m.M));
+        b->bl.maxpass = std::max(b->bl.maxpass, c->ncls);
+    }
+    if ((rc = balloc(b, (esm::BatchModel<real> **)&b->d_models, (size_t)n))) return rc;
+    BCK(cudaMemcpy(b->d_models, hm.data(), sizeof(esm::BatchModel<real>) * n, cudaMemcpyHostToDevice));
+    b->bl.nm = n;
+    b->bl.maxmoves = hm[0].nmoves;
+    b->bl.npass = b->bl.maxpass;
+    b->bl.nmove = b->bl.maxmoves;
+    b->nact.assign(b->bl.maxmoves, 0);
+    for (int mi = 0; mi < b->bl.maxmoves; ++mi)
+        while (b->nact[mi] < n && hm[b->nact[mi]].nmoves > mi) ++b->nact[mi];
+    b->bl.nact = b->nact.data();
+    b->bl.prep_smem = maxstride;
+    int dev = 0;
+    BCK(cudaGetDevice(&dev));
+    BCK(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int i = 0; i < 2; ++i) b->cap[i] = std::max(4, b->nsm * esm::batch_warps_per_sm<real>(1 << i));
+    b->bl.wpb = 1;
+    b->bl.warps = b->cap[0];
+    b->bl.scratch_per_warp = maxlane;
+    b->scratch_warps = 0;
+    if (maxlane > 0) {  // slabs for the largest grid, at most 1 GB (never fewer than the one-warp limit)
+        size_t fit = ((size_t)1 << 30) / (maxlane * sizeof(real));
+        size_t w = std::max((size_t)b->cap[0], std::min((size_t)std::max(b->cap[0], b->cap[1]), fit));
+        real *q;
+        if ((rc = balloc(b, &q, maxlane * w))) return rc;
+        b->bl.scratch = q;
+        b->scratch_warps = (int)w;
+    }
+    if ((rc = balloc(b, &b->bl.pass_cls, (size_t)b->bl.maxpass * n))) return rc;
+    if ((rc = balloc(b, &b->bl.off, (size_t)b->bl.maxpass * (n + 1)))) return rc;
+    if ((rc = balloc(b, &b->bl.counters, (size_t)b->bl.maxpass * b->bl.maxmoves))) return rc;
+    if ((rc = balloc(b, &b->d_sweep, 1))) return rc;
+    return ESM_OK;
+}
+
+// the rebuilds of every chain, then its passes: all of them (a sweep), or the first npass passes
+// with their first nmove moves each
+template <class real>
+int batch_record(esm_batch *b, int npass, int nmove) {
+    for (esm_ctx *c : b->ctx) BCK(esm::launch_rebuild<real>(ctx_model<real>(c), b->stream));
+    esm::BatchLaunch bl = b->bl;
+    bl.npass = npass;
+    bl.nmove = nmove;
+    BCK(esm::launch_batch_passes<real>((const esm::BatchModel<real> *)b->d_models, bl, b->d_sweep, b->stream));
+    return ESM_OK;
+}
+
+int batch_sweep(esm_batch *b, uint32_t sweep) {
+    k_set_word<<<1, 1, 0, b->stream>>>(b->d_sweep, sweep);
+    BCK(cudaGetLastError());
+    if (!b->graph) {
+        cudaGraph_t g = nullptr;
+        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int np = b->bl.maxpass, nm = b->bl.maxmoves;
+        int rc = b->precision == 64 ? batch_record<double>(b, np, nm) : batch_record<float>(b, np, nm);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        BCK(e);
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        BCK(e);
+    }
+    BCK(cudaGraphLaunch(b->graph, b->stream));
+    b->launches += 1 + b->n + b->bl.maxpass * (1 + b->bl.maxmoves);
+    return ESM_OK;
+}
+
+int batch_wait(esm_batch *b, double timeout_s) {
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaStreamQuery(b->stream);
+        if (e == cudaSuccess) return ESM_OK;
+        if (e != cudaErrorNotReady) return bfail(b, ESM_ECUDA, "stream: %s", cudaGetErrorString(e));
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > timeout_s) return bfail(b, ESM_ETIMEOUT, "batch stream not idle after %.1f s", timeout_s);
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+// the batch stream after every context's work so far
+int batch_join_in(esm_batch *b) {
+    for (esm_ctx *c : b->ctx) {
+        BCK(cudaEventRecord(b->ev, c->stream));
+        BCK(cudaStreamWaitEvent(b->stream, b->ev, 0));
+    }
+    return ESM_OK;
+}
+
+// every context's later work after the batch's
+int batch_join_out(esm_batch *b) {
+    BCK(cudaEventRecord(b->ev, b->stream));
+    for (esm_ctx *c : b->ctx) BCK(cudaStreamWaitEvent(c->stream, b->ev, 0));
+    return ESM_OK;
+}
+}  // namespace
+
+int esm_batch_create(esm_ctx *const *ctxs, int32_t n, esm_batch **out) {
+    if (!out) return ESM_EINVAL;
+    *out = nullptr;
+    if (!ctxs || n < 1) return ESM_EINVAL;
+    esm_batch *b = new esm_batch();
+    *out = b;
+    b->n = n;
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) {
+        esm_ctx *c = ctxs[i];
+        if (!c) return bfail(b, ESM_EINVAL, "context %d is NULL", i);
+        if (c->precision != ctxs[0]->precision) return bfail(b, ESM_EINVAL, "contexts of different precisions");
+        if (c->storage_ms || c->storage_long) return bfail(b, ESM_EINVAL, "context %d has the storage sweeps on", i);
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == c) return bfail(b, ESM_EINVAL, "context %d appears twice", i);
+        idx[i] = i;
+    }
+    b->precision = ctxs[0]->precision;
+    auto nmv = [&](int i) {
+        const esm_ctx *c = ctxs[i];
+        return c->precision == 64 ? c->Md.natoms + c->Md.nextra : c->Mf.natoms + c->Mf.nextra;
+    };
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return nmv(a) > nmv(c); });
+    for (int i = 0; i < n; ++i) {
+        b->ctx.push_back(ctxs[idx[i]]);
+        b->pos.push_back(idx[i]);
+    }
+    BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    BCK(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
+    BCK(cudaEventCreate(&b->t0));
+    BCK(cudaEventCreate(&b->t1));
+    int rc = b->precision == 64 ? batch_setup<double>(b) : batch_setup<float>(b);
+    if (rc) return rc;
+    BCK(cudaDeviceSynchronize());
+    return ESM_OK;
+}
+
+int esm_batch_destroy(esm_batch *b) {
+    if (!b) return ESM_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void *p : b->allocs) cudaFree(p);
+    if (b->ev) cudaEventDestroy(b->ev);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return ESM_OK;
+}
+
+const char *esm_batch_last_error(const esm_batch *b) { return b ? b->err.c_str() : "no batch"; }
+
+int esm_batch_sweeps(esm_batch *b, int32_t n, int64_t sweep0, int64_t *stats) {
+    if (!b) return ESM_EINVAL;
+    if (n < 0) return bfail(b, ESM_EINVAL, "n must be >= 0");
+    for (esm_ctx *c : b->ctx)
+        if (!c->has_state) return bfail(b, ESM_ESTATE, "a context has no state uploaded");
+    int rc;
+    if ((rc = batch_join_in(b))) return rc;
+    const size_t ns = 2 * (ESM_NFAM + 1) + 1;
+    for (esm_ctx *c : b->ctx) BCK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * ns, b->stream));
+    BCK(cudaEventRecord(b->t0, b->stream));
+    for (int s = 0; s < n; ++s)
+        if ((rc = batch_sweep(b, (uint32_t)(sweep0 + s)))) return rc;
+    BCK(cudaEventRecord(b->t1, b->stream));
+    if ((rc = batch_join_out(b))) return rc;
+    for (esm_ctx *c : b->ctx) c->has_scores = false;
+    if ((rc = batch_wait(b, 3600.0))) return rc;
+    BCK(cudaEventElapsedTime(&b->last_ms, b->t0, b->t1));
+    if (stats) {
+        std::vector<unsigned long long> h(ns);
+        for (int i = 0; i < b->n; ++i) {
+            BCK(cudaMemcpy(h.data(), b->ctx[i]->d_stats, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < ns; ++k) stats[(size_t)b->pos[i] * ns + k] = (int64_t)h[k];
+        }
+    }
+    return ESM_OK;
+}
+
+int esm_batch_set_grid(esm_batch *b, int32_t warps_per_block, int32_t warps_per_sm) {
+    if (!b) return ESM_EINVAL;
+    int wi = warps_per_block == 1 ? 0 : warps_per_block == 2 ? 1 : -1;
+    if (wi < 0) return bfail(b, ESM_EINVAL, "warps_per_block must be 1 or 2");
+    if (warps_per_sm < 0) return bfail(b, ESM_EINVAL, "warps_per_sm must be >= 0");
+    int cap = b->cap[wi];
+    int w = warps_per_sm == 0 ? cap : std::min(cap, std::max(4, warps_per_sm * b->nsm));
+    if (b->scratch_warps > 0) w = std::min(w, b->scratch_warps);
+    if (w == b->bl.warps && warps_per_block == b->bl.wpb) return ESM_OK;
+    int rc = batch_wait(b, 600.0);  // the captured sweep holds the old grid: drop it
+    if (rc) return rc;
+    if (b->graph) {
+        BCK(cudaGraphExecDestroy(b->graph));
+        b->graph = nullptr;
+    }
+    b->bl.wpb = warps_per_block;
+    b->bl.warps = w;
+    return ESM_OK;
+}
+
+int esm_batch_grid(const esm_batch *b, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limit_per_sm) {
+    if (!b || b->nsm < 1) return ESM_EINVAL;
+    if (warps_per_block) *warps_per_block = b->bl.wpb;
+    if (warps_per_sm) *warps_per_sm = (b->bl.warps + b->nsm - 1) / b->nsm;
+    if (limit_per_sm) *limit_per_sm = (b->cap[b->bl.wpb == 2 ? 1 : 0] + b->nsm - 1) / b->nsm;
+    return ESM_OK;
+}
+
+int64_t esm_batch_launch_count(const esm_batch *b) { return b ? b->launches : 0; }
+
+int esm_batch_time(const esm_batch *b, double *ms) {
+    if (!b || !ms) return ESM_EINVAL;
+    *ms = b->last_ms;
+    return ESM_OK;
+}
+
+int esm_batch_autotune(esm_batch *b, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand) {
+    if (!b) return ESM_EINVAL;
+    for (esm_ctx *c : b->ctx)
+        if (!c->has_state) return bfail(b, ESM_ESTATE, "a context has no state uploaded");
+    int list[ESM_TUNE_MAX][2], n = 0;
+    for (int wi = 0; wi < 2; ++wi) {
+        int lim = (b->cap[wi] + b->nsm - 1) / b->nsm;
+        for (int w : {8, 16, 24, 32})
+            if (w < lim && w % (1 << wi) == 0 && n < ESM_TUNE_MAX - 2 + wi) {
+                list[n][0] = 1 << wi;
+                list[n++][1] = w;
+            }
+        list[n][0] = 1 << wi;
+        list[n++][1] = lim;
+    }
+    int rc = 0;
+    for (esm_ctx *c : b->ctx)
+        if ((rc = esm_state_save(c))) return bfail(b, rc, "state save: %s", c->err.c_str());
+    if ((rc = batch_join_in(b))) return rc;
+    int bw = b->bl.wpb, bs = (b->bl.warps + b->nsm - 1) / b->nsm;
+    int nmove = std::min(b->bl.maxmoves, ESM_BATCH_TUNE_MOVES);
+    double tbest = 1e300;
+    for (int i = 0; i < n && !rc; ++i) {
+        if ((rc = esm_batch_set_grid(b, list[i][0], list[i][1]))) break;
+        float t = 0;
+        for (int rep = 0; rep < 2 && !rc; ++rep) {  // the first run loads and warms, the second is timed
+            k_set_word<<<1, 1, 0, b->stream>>>(b->d_sweep, (uint32_t)sweep);
+            if (cudaGetLastError() != cudaSuccess) rc = bfail(b, ESM_ECUDA, "launch");
+            if (!rc && cudaEventRecord(b->t0, b->stream) != cudaSuccess) rc = bfail(b, ESM_ECUDA, "event record");
+            if (!rc) rc = b->precision == 64 ? batch_record<double>(b, 1, nmove) : batch_record<float>(b, 1, nmove);
+            if (!rc && cudaEventRecord(b->t1, b->stream) != cudaSuccess) rc = bfail(b, ESM_ECUDA, "event record");
+            if (!rc) rc = batch_wait(b, 600.0);
+            if (!rc && cudaEventElapsedTime(&t, b->t0, b->t1) != cudaSuccess) rc = bfail(b, ESM_ECUDA, "event time");
+            if (!rc) rc = batch_join_out(b);
+            for (esm_ctx *c : b->ctx)
+                if (!rc && (rc = esm_state_restore(c))) rc = bfail(b, rc, "state restore: %s", c->err.c_str());
+            if (!rc) rc = batch_join_in(b);
+        }
+        if (rc) break;
+        if (cand) {
+            cand[2 * i] = list[i][0];
+            cand[2 * i + 1] = list[i][1];
+        }
+        if (ms) ms[i] = t;
+        if (t < tbest) {
+            tbest = t;
+            bw = list[i][0];
+            bs = list[i][1];
+        }
+    }
+    if (rc) return rc;
+    if (ncand) *ncand = n;
+    if (best) {
+        best[0] = bw;
+        best[1] = bs;
+    }
+    return esm_batch_set_grid(b, bw, bs);
 }

@@ -63,6 +63,34 @@ __host__ __device__ inline void uniform2(uint64_t seed, uint32_t tag, uint32_t c
     *u1 = u53(x[2], x[3]);
 }
 
+// The order of the colour classes in a sweep (local_sweep!, src/local.jl:1934: the parity
+// classes in random order, three of them when T is odd): order[0..ncls) from the sweep's stream.
+__host__ __device__ inline void class_order_of(uint64_t seed, int T, uint32_t sweep, int order[3], int *ncls) {
+    double u0, u1;
+    uniform2(seed, ESM_TAG_SWEEP, 0, 0, 0, sweep, &u0, &u1);
+    if (T % 2 == 0) {
+        *ncls = 2;
+        order[0] = u0 < 0.5 ? 0 : 1;
+        order[1] = 1 - order[0];
+        order[2] = 2;
+    } else {
+        *ncls = 3;
+        order[0] = 0;
+        order[1] = 1;
+        order[2] = 2;
+        int j = (int)floor(u0 * 3);
+        j = j < 2 ? j : 2;
+        int x = order[2];
+        order[2] = order[j];
+        order[j] = x;
+        j = (int)floor(u1 * 2);
+        j = j < 1 ? j : 1;
+        x = order[1];
+        order[1] = order[j];
+        order[j] = x;
+    }
+}
+
 __host__ __device__ inline double normal_at(uint64_t seed, uint32_t tag, uint32_t j, uint32_t c1, uint32_t c2,
                                             uint32_t c3) {
     double u0, u1;

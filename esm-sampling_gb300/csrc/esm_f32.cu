@@ -24,6 +24,9 @@ template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int
 template size_t sep_region_bytes<float>(const DevModel<float> &);
 template int sep_warps_per_sm<float>(const DevModel<float> &, int *);
 template int linemove_blocks_per_sm<float>(const DevModel<float> &, int);
+template cudaError_t launch_batch_passes<float>(const BatchModel<float> *, const BatchLaunch &, const uint32_t *,
+                                                cudaStream_t);
+template int batch_warps_per_sm<float>(int);
 template cudaError_t launch_rebuild<float>(const DevModel<float> &, cudaStream_t);
 template cudaError_t launch_score_finish<float>(const DevModel<float> &, const double *, const double *,
                                                 const double *, const double *, double, double, int, double *,

@@ -30,6 +30,9 @@ template cudaError_t launch_class_pass<double>(const DevModel<double> &, const i
 template size_t sep_region_bytes<double>(const DevModel<double> &);
 template int sep_warps_per_sm<double>(const DevModel<double> &, int *);
 template int linemove_blocks_per_sm<double>(const DevModel<double> &, int);
+template cudaError_t launch_batch_passes<double>(const BatchModel<double> *, const BatchLaunch &, const uint32_t *,
+                                                cudaStream_t);
+template int batch_warps_per_sm<double>(int);
 template cudaError_t launch_rebuild<double>(const DevModel<double> &, cudaStream_t);
 template cudaError_t launch_score_finish<double>(const DevModel<double> &, const double *, const double *,
                                                 const double *, const double *, double, double, int, double *,

@@ -33,6 +33,42 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
 template <class real>
 int linemove_blocks_per_sm(const DevModel<real> &M, int wpb);
 
+// ---- a batch of models whose class passes run together: per pass one descriptor launch for all
+// models and one k_move_batch launch per move index, each over the tasks of every model that has
+// that move (the models sorted by decreasing move count, so those are a prefix of the models)
+template <class real>
+struct BatchModel {
+    DevModel<real> M;           // the model (move log off)
+    const int *steps[3];        // the step lists of its colour classes
+    int nsteps[3];
+    int nmoves;                 // moves of one of its class passes (natoms + nextra)
+    char *descs;                // its descriptor buffer: nmoves descriptors of stride bytes
+    size_t stride;
+    unsigned long long *stats;  // its move counts, laid out as a context's
+};
+struct BatchLaunch {
+    int nm;                  // models
+    int maxpass;             // colour classes per sweep, the most of any model (2, or 3 with an odd T)
+    int maxmoves;            // moves per class pass of the first model (the most)
+    int npass, nmove;        // the passes and the moves per pass launched (maxpass, maxmoves: all)
+    const int *nact;         // host [maxmoves]: the models that have move mi (a prefix)
+    int wpb, warps;          // k_move_batch: warps per block (1 or 2) and warps launched
+    size_t prep_smem;        // the largest descriptor stride
+    void *scratch;           // global walk slabs for the models whose buffers exceed the local arrays
+    size_t scratch_per_warp; // reals of one warp's slab (0: no model needs one)
+    int *pass_cls;           // device [maxpass * nm]: the class model b runs in pass p (-1: none)
+    unsigned int *off;       // device [maxpass * (nm + 1)]: the item prefix over the models of pass p
+    unsigned int *counters;  // device [maxpass * maxmoves]: the item counters of the launches
+};
+// the passes of one sweep of every model of the batch (the sweep index read from *sweep on the
+// device, graph-capturable); the caching rebuild at the sweep start is the caller's
+template <class real>
+cudaError_t launch_batch_passes(const BatchModel<real> *bm, const BatchLaunch &bl, const uint32_t *sweep,
+                                cudaStream_t s);
+// resident k_move_batch warps per SM with blocks of wpb (1 or 2) warps; sets the kernels' limits
+template <class real>
+int batch_warps_per_sm(int wpb);
+
 // ---- storage multiscale sweep (esm_plateau.cuh)
 #define ESM_PLAT_MAXU 32  // units of one plateau move (a cell-class aggregate)
 #define ESM_PLAT_MAXK 8   // dispatchable units at one node taking part in the compensation

@@ -1586,12 +1586,11 @@ namespace esm {
 // every task of the class; the selection reads only capacities and static tables, so every
 // descriptor is the same for all tasks and is built once here, by one warp, in stream order.
 // Descriptor mi goes to descs + mi * stride; its header word 12 holds the family index (-1: no move).
+// The body of k_prep_moves for one model, run by one warp: smem is its descriptor workspace
+// (stride bytes), sd the shared Desc that carves it.
 template <class real>
-__global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevModel<real> M, const uint32_t *sweep_p, int cls,
-                                                  int nrun, char *descs, size_t stride) {
-    extern __shared__ __align__(16) char smem[];
-    __shared__ Desc<real> sd;
-    int lane = threadIdx.x;
+__device__ __forceinline__ void prep_class(const DevModel<real> &M, char *smem, Desc<real> &sd, uint32_t sweep, int cls,
+                                           int nrun, char *descs, size_t stride, int lane) {
     int nmoves = M.natoms + M.nextra;
     if (lane == 0) sd = carve_desc<real>(smem, M, nmoves);
     __syncwarp();
@@ -1603,7 +1602,6 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
     }
     for (int i = lane; i < M.L; i += 32) d.lmark[i] = 0;
     __syncwarp();
-    uint32_t sweep = *sweep_p;
     Stream st{M.seed, 0u, (uint32_t)cls, sweep, 0u};
     build_list(M, d, st, lane);
     for (int mi = 0; mi < nrun; ++mi) {
@@ -1615,6 +1613,14 @@ __global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevMo
         for (size_t i = lane; i < stride / 16; i += 32) dst[i] = src[i];
         __syncwarp();
     }
+}
+
+template <class real>
+__global__ void __launch_bounds__(32) k_prep_moves(const __grid_constant__ DevModel<real> M, const uint32_t *sweep_p, int cls,
+                                                  int nrun, char *descs, size_t stride) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ Desc<real> sd;
+    prep_class<real>(M, smem, sd, *sweep_p, cls, nrun, descs, stride, threadIdx.x);
 }
 
 // Move mi of the class (its descriptor built by k_prep_moves) for every (step, replica) task. One
@@ -1630,6 +1636,41 @@ template <int WPB>
 struct MoveBounds {
     static constexpr int min_blocks = WPB == 1 ? 24 : WPB == 2 ? 16 : 10;
 };
+
+// One task of move mi (family fi) at step tau for the lane's replica (Ln.rep): the kinks, the walk
+// and draw of t, the Jacobian test of the compensated families and the commit. Returns the t
+// taken (0: not moved); *guard on a walk buffer overflow.
+template <class real>
+__device__ __forceinline__ real move_task(Lane<real> &Ln, const DevModel<real> &M, const Desc<real> &d,
+                                          const LaneLayout &LL, int fi, int mi, int tau, uint32_t sweep, bool *guard) {
+    int T = M.T;
+    Ln.tau = tau;
+    Ln.taum = (Ln.tau - 1 + T) % T;
+    Ln.tau1 = (Ln.tau + 1) % T;
+    lane_kinks(Ln);
+    double uc, uo, uj, un;
+    uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
+    real t = Ln.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), guard);
+    bool compensated = fi == ESM_FAM_XLOCC || fi == ESM_FAM_TPOT || fi == ESM_FAM_TSOC;
+    if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041), in FP64 in both builds
+        int nk = d.hdr[3];
+        bool any = false;
+        double lj = 0;
+        for (int k = 0; k < nk; ++k) {
+            if (Ln.S(LL.kv, k) == 0) continue;
+            any = true;
+            double Q = Ln.S(LL.kq, k);
+            lj += (double)Ln.S(LL.knm, k) *
+                  log(fabs((fmax(Q + (double)d.kg[k] * (double)t, 0.0) + (double)Ln.S(LL.ke, k)) / (double)Ln.S(LL.kp, k)));
+        }
+        if (any) {
+            uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uj, &un);
+            if (uj >= exp(fmin(0.0, lj))) t = 0;
+        }
+    }
+    if (t != 0) Ln.commit(t);
+    return t;
+}
 
 template <class real, int WPB>
 __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
@@ -1678,35 +1719,9 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
         Ln.rep = task % M.R;
         int q = tile * M.span + sit;
         if (!(sit < M.span && q < nsteps)) continue;
-        int T = M.T;
-        Ln.tau = steps[q];
-        Ln.taum = (Ln.tau - 1 + T) % T;
-        Ln.tau1 = (Ln.tau + 1) % T;
-        lane_kinks(Ln);
-        double uc, uo, uj, un;
-        uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uc, &uo);
         bool guard;
-        real t = Ln.sample_line(unit_uniform<real>(uc), unit_uniform<real>(uo), &guard);
+        real t = move_task<real>(Ln, M, d, LL, fi, mi, steps[q], sweep, &guard);
         if (guard) ++guards;
-        bool compensated = fi == ESM_FAM_XLOCC || fi == ESM_FAM_TPOT || fi == ESM_FAM_TSOC;
-        if (compensated && t != 0) {  // Jacobian (logjac, src/local.jl:1871; :2041), in FP64 in both builds
-            int nk = d.hdr[3];
-            bool any = false;
-            double lj = 0;
-            for (int k = 0; k < nk; ++k) {
-                if (Ln.S(LL.kv, k) == 0) continue;
-                any = true;
-                double Q = Ln.S(LL.kq, k);
-                lj += (double)Ln.S(LL.knm, k) *
-                      log(fabs((fmax(Q + (double)d.kg[k] * (double)t, 0.0) + (double)Ln.S(LL.ke, k)) / (double)Ln.S(LL.kp, k)));
-            }
-            if (any) {
-                uniform2(M.seed, ESM_TAG_LANE, 2 * (uint32_t)mi + 1, (uint32_t)Ln.tau, (uint32_t)Ln.rep, sweep, &uj,
-                         &un);
-                if (uj >= exp(fmin(0.0, lj))) t = 0;
-            }
-        }
-        if (t != 0) Ln.commit(t);
         if (M.mlog && Ln.rep < M.mlog_nrep) M.mlog[((size_t)mi * nsteps + q) * M.mlog_nrep + Ln.rep] = (double)t;
         ++tried;
         if (t != 0) ++moved;
@@ -1819,6 +1834,173 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
         if (sepmin > 0 && sblocks > 0) {
             k_move_sep<real, 2><<<sblocks, 64, ssmem, s>>>(M, steps, nsteps, sweep, mi, descs, stride, sepmin,
                                                           sep.in_smem, sep.slab, stats, counters + mi);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------------------------
+// a batch of models
+// ---------------------------------------------------------------------------------------------
+// Pass p of every model of a batch: block b builds the descriptors of the class that model b runs
+// in pass p of the sweep (its own class order, class_order_of), exactly as k_prep_moves does for
+// the model alone; block 0 also writes every model's class of the pass and the pass's item prefix
+// over the models (items: the model's tiles of its class x the warps of a tile).
+template <class real>
+__global__ void __launch_bounds__(32) k_prep_batch(const BatchModel<real> *bm, int nm, const uint32_t *sweep_p, int p,
+                                                   int *pass_cls, unsigned int *off) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ Desc<real> sd;
+    int b = blockIdx.x, lane = threadIdx.x;
+    uint32_t sweep = *sweep_p;
+    const BatchModel<real> &B = bm[b];
+    int order[3], ncls;
+    class_order_of(B.M.seed, B.M.T, sweep, order, &ncls);
+    if (b == 0 && lane == 0) {
+        unsigned int acc = 0;
+        off[0] = 0;
+        for (int q = 0; q < nm; ++q) {
+            const BatchModel<real> &Q = bm[q];
+            int oq[3], nq;
+            class_order_of(Q.M.seed, Q.M.T, sweep, oq, &nq);
+            int c = p < nq ? oq[p] : -1;
+            pass_cls[q] = c;
+            if (c >= 0 && Q.nsteps[c] > 0) {
+                int ntile = (Q.nsteps[c] + Q.M.span - 1) / Q.M.span;
+                int wpt = (Q.M.span * Q.M.R + 31) / 32;
+                acc += (unsigned int)(ntile * wpt);
+            }
+            off[q + 1] = acc;
+        }
+    }
+    if (p >= ncls || B.nsteps[order[p]] == 0) return;
+    prep_class<real>(B.M, smem, sd, sweep, order[p], B.nmoves, B.descs, B.stride, lane);
+}
+
+// Move mi of the current pass for every task of the first nact models of the batch. A warp takes
+// items from the launch's counter; an item (32 tasks of one model's tile, as in k_move) belongs to
+// the model b with off[b] <= item < off[b + 1]. When a warp's item comes from another model than
+// its last one, the warp copies that model's tables and layout into its shared memory and points
+// its descriptor at the model's descriptor mi in global memory (read-only during the move), after
+// adding its counts so far to the previous model's statistics. Each task then runs exactly the
+// arithmetic of k_move (move_task), so a model's state after a batch pass is the state its own
+// class pass gives. The cooperative walk of separable moves is not used in a batch.
+template <class real, int WPB>
+__global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
+    k_move_batch(const BatchModel<real> *bm, int nact, const int *pass_cls, const unsigned int *off,
+                 const uint32_t *sweep_p, int mi, real *scratch, size_t scratch_per_warp, unsigned int *next_item) {
+    __shared__ DevModel<real> sM[WPB];
+    __shared__ Desc<real> sd[WPB];
+    __shared__ LaneLayout sLL[WPB];
+    int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t sweep = *sweep_p;
+    unsigned int total = off[nact];
+    real local[ESM_LANE_LOCAL];
+    int cur = -1, fi = -1, cls = 0, nsteps = 0;
+    const int *steps = nullptr;
+    unsigned long long tried = 0, moved = 0, guards = 0;
+    while (true) {
+        unsigned int it = 0;
+        if (lane == 0) it = atomicAdd(next_item, 1u);
+        unsigned int item = __shfl_sync(0xffffffffu, it, 0);
+        bool done = item >= total;
+        int b = cur;
+        if (!done) {  // the last model whose prefix is <= item
+            int lo = 0, hi = nact - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (off[mid] <= item)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            b = lo;
+        }
+        if (done || b != cur) {  // warp-uniform
+            for (int o = 16; o > 0; o >>= 1) {
+                tried += __shfl_xor_sync(0xffffffffu, tried, o);
+                moved += __shfl_xor_sync(0xffffffffu, moved, o);
+                guards += __shfl_xor_sync(0xffffffffu, guards, o);
+            }
+            if (lane == 0 && cur >= 0 && fi >= 0) {
+                unsigned long long *st = bm[cur].stats;
+                if (tried) atomicAdd(&st[2 * fi], tried);
+                if (moved) atomicAdd(&st[2 * fi + 1], moved);
+                if (guards) atomicAdd(&st[2 * (ESM_NFAM + 1)], guards);
+            }
+            tried = moved = guards = 0;
+            if (done) break;
+            const unsigned int *src = (const unsigned int *)&bm[b].M;
+            unsigned int *dst = (unsigned int *)&sM[wib];
+            for (int i = lane; i < (int)(sizeof(DevModel<real>) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
+            if (lane == 0) {
+                sd[wib] = carve_desc<real>(bm[b].descs + (size_t)mi * bm[b].stride, sM[wib], bm[b].nmoves);
+                const DevModel<real> &Mb = sM[wib];
+                sLL[wib] = lane_layout(Mb.maxpts, Mb.maxn, Mb.maxstu, linemove_maxroots(Mb), Mb.maxk, Mb.maxku);
+            }
+            __syncwarp();
+            cur = b;
+            fi = sd[wib].hdr[12];
+            cls = pass_cls[b];
+            nsteps = cls >= 0 ? bm[b].nsteps[cls] : 0;
+            steps = cls >= 0 ? bm[b].steps[cls] : nullptr;
+        }
+        if (fi < 0) continue;  // the model's move mi is not a valid move: its tasks do nothing
+        const DevModel<real> &M = sM[wib];
+        const LaneLayout &LL = sLL[wib];
+        unsigned int li = item - off[b];
+        int wpt = (M.span * M.R + 31) / 32;
+        int tile = (int)(li / wpt), grp = (int)(li % wpt);
+        int task = grp * 32 + lane;
+        int sit = task / M.R;
+        int q = tile * M.span + sit;
+        if (!(sit < M.span && q < nsteps)) continue;
+        bool loc = LL.total <= ESM_LANE_LOCAL;
+        real *slab = loc ? local : scratch + ((size_t)blockIdx.x * WPB + wib) * scratch_per_warp + lane;
+        Lane<real> Ln(M, sd[wib], slab, loc ? 1 : 32, lane, LL);
+        Ln.rep = task % M.R;
+        bool guard;
+        real t = move_task<real>(Ln, M, sd[wib], LL, fi, mi, steps[q], sweep, &guard);
+        if (guard) ++guards;
+        ++tried;
+        if (t != 0) ++moved;
+    }
+}
+
+template <class real>
+int batch_warps_per_sm(int wpb) {
+    int nb = 0;
+    cudaError_t e;
+    cudaFuncSetAttribute(k_prep_batch<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (wpb == 2)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move_batch<real, 2>, 64, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_move_batch<real, 1>, 32, 0);
+    if (e != cudaSuccess || nb < 1) nb = 16 / wpb;
+    return nb * wpb;
+}
+
+template <class real>
+cudaError_t launch_batch_passes(const BatchModel<real> *bm, const BatchLaunch &bl, const uint32_t *sweep,
+                                cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bl.counters, 0, sizeof(unsigned int) * bl.maxpass * bl.maxmoves, s);
+    if (e != cudaSuccess) return e;
+    int blocks = (bl.warps + bl.wpb - 1) / bl.wpb;
+    for (int p = 0; p < bl.npass; ++p) {
+        int *pc = bl.pass_cls + (size_t)p * bl.nm;
+        unsigned int *off = bl.off + (size_t)p * (bl.nm + 1);
+        k_prep_batch<real><<<bl.nm, 32, bl.prep_smem, s>>>(bm, bl.nm, sweep, p, pc, off);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        for (int mi = 0; mi < bl.nmove; ++mi) {
+            unsigned int *ctr = bl.counters + (size_t)p * bl.maxmoves + mi;
+            if (bl.wpb == 2)
+                k_move_batch<real, 2><<<blocks, 64, 0, s>>>(bm, bl.nact[mi], pc, off, sweep, mi, (real *)bl.scratch,
+                                                           bl.scratch_per_warp, ctr);
+            else
+                k_move_batch<real, 1><<<blocks, 32, 0, s>>>(bm, bl.nact[mi], pc, off, sweep, mi, (real *)bl.scratch,
+                                                           bl.scratch_per_warp, ctr);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
     }

@@ -24,7 +24,9 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_set_timing", "esm_timing", "esm_stream", "esm_capacity_scores_static", "esm_score_errors",
            "esm_follow_capacities", "esm_state_save", "esm_state_restore", "esm_regime_occupancy", "esm_set_move_grid", "esm_move_grid",
            "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe", "esm_set_sep_walk",
-           "esm_sep_walk", "esm_set_move_log", "esm_move_log")
+           "esm_sep_walk", "esm_set_move_log", "esm_move_log", "esm_batch_create", "esm_batch_destroy",
+           "esm_batch_last_error", "esm_batch_sweeps", "esm_batch_set_grid", "esm_batch_grid", "esm_batch_autotune",
+           "esm_batch_time", "esm_batch_launch_count")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -90,6 +92,17 @@ def load(build_if_missing=True):
     L.esm_timing.argtypes = [C.c_void_p, P_f64]
     L.esm_stream.restype = C.c_void_p
     L.esm_stream.argtypes = [C.c_void_p]
+    L.esm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
+    L.esm_batch_destroy.argtypes = [C.c_void_p]
+    L.esm_batch_last_error.restype = C.c_char_p
+    L.esm_batch_last_error.argtypes = [C.c_void_p]
+    L.esm_batch_sweeps.argtypes = [C.c_void_p, C.c_int32, C.c_int64, P_i64]
+    L.esm_batch_set_grid.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.esm_batch_grid.argtypes = [C.c_void_p, P_i32, P_i32, P_i32]
+    L.esm_batch_autotune.argtypes = [C.c_void_p, C.c_int64, P_i32, P_i32, P_f64, P_i32]
+    L.esm_batch_time.argtypes = [C.c_void_p, P_f64]
+    L.esm_batch_launch_count.restype = C.c_int64
+    L.esm_batch_launch_count.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -332,3 +345,70 @@ class DeviceChain:
 
     def launch_count(self):
         return int(self.L.esm_launch_count(self.h))
+
+
+class DeviceBatch:
+    """Chains of any sizes whose operation sweeps run together (an ``esm_batch`` over the chains'
+    contexts): one captured graph per sweep, one line-move launch per move index over the tasks of
+    every chain. The chains stay usable on their own; they must outlive the batch."""
+
+    def __init__(self, chains):
+        self.L = load()
+        self.chains = list(chains)
+        arr = (C.c_void_p * len(self.chains))(*[c.h for c in self.chains])
+        h = C.c_void_p()
+        rc = self.L.esm_batch_create(arr, len(self.chains), C.byref(h))
+        self.h = h
+        self._check(rc, "esm_batch_create")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.L.esm_batch_last_error(self.h).decode() if self.h else ""
+            raise EsmError(f"{what}: status {rc}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.esm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sweeps(self, n, sweep0=0, stats=True):
+        """n operation sweeps of every chain; the move counts per chain [chains, NSTAT] (or None)."""
+        st = np.zeros((len(self.chains), NSTAT), np.int64) if stats else None
+        self._check(self.L.esm_batch_sweeps(self.h, n, sweep0, _p(st, P_i64)), "esm_batch_sweeps")
+        return st
+
+    def set_grid(self, warps_per_block=1, warps_per_sm=0):
+        self._check(self.L.esm_batch_set_grid(self.h, int(warps_per_block), int(warps_per_sm)), "esm_batch_set_grid")
+
+    def grid(self):
+        """(warps per block, warps per SM, the resident limit per SM of that block shape)."""
+        b, w, lim = np.zeros(1, np.int32), np.zeros(1, np.int32), np.zeros(1, np.int32)
+        self._check(self.L.esm_batch_grid(self.h, _p(b, P_i32), _p(w, P_i32), _p(lim, P_i32)), "esm_batch_grid")
+        return int(b[0]), int(w[0]), int(lim[0])
+
+    def autotune(self, sweep=0):
+        """Pick the grid by timing one sweep of every chain per candidate (the states are restored
+        after each); returns ((warps per block, warps per SM), {(wpb, wps): ms})."""
+        best = np.zeros(2, np.int32)
+        cand = np.zeros(2 * TUNE_MAX, np.int32)
+        ms = np.zeros(TUNE_MAX)
+        n = np.zeros(1, np.int32)
+        self._check(self.L.esm_batch_autotune(self.h, sweep, _p(best, P_i32), _p(cand, P_i32), _p(ms), _p(n, P_i32)),
+                    "esm_batch_autotune")
+        return (int(best[0]), int(best[1])), {(int(cand[2 * i]), int(cand[2 * i + 1])): float(ms[i])
+                                              for i in range(int(n[0]))}
+
+    def last_ms(self):
+        """Device time (CUDA events) of the last sweeps call, ms."""
+        t = np.zeros(1)
+        self._check(self.L.esm_batch_time(self.h, _p(t)), "esm_batch_time")
+        return float(t[0])
+
+    def launch_count(self):
+        return int(self.L.esm_batch_launch_count(self.h))

@@ -345,6 +345,45 @@ int esm_sync(esm_ctx *ctx, double timeout_s);
 int64_t esm_launch_count(const esm_ctx *ctx);
 
 /* ------------------------------------------------------------------------------------------
+ * A batch of independent chains (models of any sizes, one context each, one precision) whose
+ * operation sweeps run together: the batch axis of the reference's GPU port (a batch of models
+ * in one program, device/src/replica_run.jl:84-108) over the local sweep (local_sweep!,
+ * src/local.jl:1927, as esm_operation_sweeps runs it without the storage sweeps). A sweep is one
+ * CUDA graph captured at the batch's first sweep: the caching rebuild of every model, then per
+ * colour-class pass one launch that builds every model's move descriptors and one line-move launch
+ * per move index, whose work items are the tasks of every model that has that move. Each task
+ * runs the arithmetic of the model's own class pass, so every model's state after
+ * esm_batch_sweeps equals the state esm_operation_sweeps gives it on its own context.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct esm_batch esm_batch;
+/* ctxs [n]: contexts created by esm_create with the same precision, states uploaded, the storage
+   sweeps off (esm_opts.storage_ms = storage_long = 0); they stay owned by the caller and must
+   outlive the batch. The batch runs on its own stream, ordered after and before each context's. */
+int esm_batch_create(esm_ctx *const *ctxs, int32_t n, esm_batch **out);
+int esm_batch_destroy(esm_batch *b);
+const char *esm_batch_last_error(const esm_batch *b);
+/* n operation sweeps (sweep indices sweep0 ... sweep0 + n - 1) of every chain; stats (may be NULL):
+   [n_models * (2 * (ESM_NFAM + 1) + 1)], chain i's counts at row i (the order of ctxs) in
+   esm_operation_sweeps' layout (tried and moved per family, then the guard events) */
+int esm_batch_sweeps(esm_batch *b, int32_t n, int64_t sweep0, int64_t *stats);
+/* The grid of the batch's line-move launches: warps per block (1 or 2) and warps per SM (0: the
+   resident limit); esm_batch_grid reads it back with the resident limit of that block shape. */
+int esm_batch_set_grid(esm_batch *b, int32_t warps_per_block, int32_t warps_per_sm);
+int esm_batch_grid(const esm_batch *b, int32_t *warps_per_block, int32_t *warps_per_sm, int32_t *limit_per_sm);
+/* Autotuner of the batch's grid: for both block shapes at 8, 16, 24, 32 warps per SM and at their
+   resident limits, the first ESM_BATCH_TUNE_MOVES line moves of the first colour-class pass of
+   sweep `sweep` of every chain are run twice and the second run is timed (CUDA events on the
+   batch's stream), each run from the current states, which are then restored; the fastest grid is
+   kept. The chains are unchanged; every context's esm_state_save slot is overwritten. Outputs as
+   esm_autotune_moves. */
+#define ESM_BATCH_TUNE_MOVES 64
+int esm_batch_autotune(esm_batch *b, int64_t sweep, int32_t *best, int32_t *cand, double *ms, int32_t *ncand);
+/* CUDA-event time of the batch's last esm_batch_sweeps call (ms, the device time of its sweeps). */
+int esm_batch_time(const esm_batch *b, double *ms);
+/* Kernels launched by the batch's sweeps since creation. */
+int64_t esm_batch_launch_count(const esm_batch *b);
+
+/* ------------------------------------------------------------------------------------------
  * Surrogate of the replica-averaged capacity score (no counterpart in the reference: the
  * learned proposal is an addition of this library). An MLP with nlayers linear layers of widths
  * dims[0] -> dims[1] -> ... -> dims[nlayers], SiLU between them, BF16 weights and activations
