@@ -316,6 +316,7 @@ def profile_case(args):
     d = DeviceChain(m, w["R"], precision=32, seed=w["seed"])
     d.upload(initial_state(m, w["R"], seed=7))
     grid = None
+    d.set_move_schedule(args.schedule)
     if args.grid:
         d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
     elif args.autotune:
@@ -328,7 +329,7 @@ def profile_case(args):
     d.scores()
     kt = d.timing()
     print(json.dumps({"case": "small", "N": w["N"], "T": w["T"], "R": w["R"], "sweeps": args.steps,
-                      "grid": list(d.move_grid()[:2]), "sep_walk_min_units": args.sep,
+                      "grid": list(d.move_grid()[:2]), "schedule": d.move_schedule(), "sep_walk_min_units": args.sep,
                       "kernel_ms": {k: v[0] for k, v in kt.items()}, "launches": {k: v[1] for k, v in kt.items()},
                       "moves_tried": int(st[:-1:2].sum()), "guards": int(st[-1])}), flush=True)
 
@@ -560,8 +561,11 @@ def n256_case(args):
     m = make_model(N, L, T, seed=1234)
     d = DeviceChain(m, R, precision=32, seed=1234, storage_ms=1, storage_long=1)
     d.upload(initial_state(m, R, seed=7))
-    if args.grid:
-        d.set_move_grid(*(int(x) for x in args.grid.lower().split("x")))
+    # the walk buffers of a 256-node model exceed the lanes' local arrays and live in global slabs,
+    # sized at creation for at most 1 GB (7 warps per SM here); a single chain on the GPU grows them
+    # to the grid: 4-warp blocks at 32 warps per SM (the autotuner's choice at 128 nodes), ~9 GB
+    d.set_move_grid(*((int(x) for x in args.grid.lower().split("x")) if args.grid else (4, 32)))
+    d.set_move_schedule(args.schedule)
     ctl = RP.ReplicaCtl(M=R)
     rng = np.random.Generator(np.random.PCG64(1))
     t0 = time.perf_counter()
@@ -696,6 +700,8 @@ def main():
     ap.add_argument("--L", type=int, default=0, help="--case small: lines (default 1.5 N)")
     ap.add_argument("--R", type=int, default=0, help="--case small: replicas (default 64)")
     ap.add_argument("--models", type=int, default=96, help="--case batch: number of models")
+    ap.add_argument("--schedule", default="move", choices=["move", "class"],
+                    help="line moves of a class pass: one launch per move, or the whole class in one launch")
     ap.add_argument("--batch-mode", default="batch", choices=["batch", "streams"],
                     help="--case batch: one esm_batch (default) or every model on its own stream")
     ap.add_argument("--ess-steps", type=int, default=32,
@@ -750,6 +756,7 @@ def main():
     R = d.R
     # the line-move grid picked by the library's autotuner (one timed colour class per candidate,
     # state restored), untimed setup; --grid WPBxWPS fixes it instead (profiler runs)
+    d.set_move_schedule(args.schedule)
     if args.grid:
         wpb, wps = (int(x) for x in args.grid.lower().split("x"))
         d.set_move_grid(wpb, wps)
@@ -829,7 +836,7 @@ def main():
                                   "mostly walk scratch")},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "clocks": clocks,
-            "move_grid": {"warps_per_block": grid[0], "warps_per_sm": grid[1],
+            "move_grid": {"warps_per_block": grid[0], "warps_per_sm": grid[1], "schedule": d.move_schedule(),
                           "autotune_ms_per_class": {f"{a}x{b}": round(v, 1) for (a, b), v in grid_ms.items()}},
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
             "line_moves_per_s": moves * args.steps / (dev_ms / 1000.0) * world,

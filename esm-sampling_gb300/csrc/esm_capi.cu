@@ -89,6 +89,10 @@ struct esm_ctx {
     bool has_snap = false;
     unsigned long long *d_occ = nullptr;
     unsigned int *d_item_ctr = nullptr;  // per move: the next item of the class pass
+    int move_schedule = ESM_MOVES_PER_MOVE;  // one launch per move, or the whole class per launch
+    unsigned int *d_wave_done = nullptr;     // per work item: moves completed (whole-class launch)
+    int *d_wave_err = nullptr;               // set when a wait of the whole-class launch ran out
+    size_t wave_items = 0;
     uint32_t *d_sweep = nullptr;         // the sweep index of the current class pass
     // storage multiscale sweep
     int storage_ms = 0, storage_long = 0;
@@ -601,14 +605,28 @@ __global__ void k_set_word(uint32_t *p, uint32_t v) { *p = v; }
 int class_pass_launch(esm_ctx *c, int cls, int limit) {
     int ns = c->class_len[cls];
     esm::SepLaunch sep{c->sep_min, c->sep_max_warps, c->sep_in_smem, c->d_sep_slab};
+    esm::WaveLaunch wave{c->move_schedule == ESM_MOVES_PER_CLASS, c->d_wave_done, c->d_wave_err, c->wave_items};
     if (c->precision == 64)
         CK(esm::launch_class_pass<double>(c->Md, c->d_steps[cls], ns, c->d_sweep, cls, limit, (double *)c->d_scratch,
                                           c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, sep,
-                                          c->stream));
+                                          wave, c->stream));
     else
         CK(esm::launch_class_pass<float>(c->Mf, c->d_steps[cls], ns, c->d_sweep, cls, limit, (float *)c->d_scratch,
                                          c->move_wpb, c->max_warps, c->d_stats, c->d_descs, c->d_item_ctr, sep,
-                                         c->stream));
+                                         wave, c->stream));
+    return ESM_OK;
+}
+
+// the error flag of the whole-class launch: a wait that ran out leaves the pass incomplete
+int wave_check(esm_ctx *c) {
+    if (c->move_schedule != ESM_MOVES_PER_CLASS || !c->d_wave_err) return ESM_OK;
+    int h = 0;
+    CK(cudaMemcpy(&h, c->d_wave_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        CK(cudaMemset(c->d_wave_err, 0, sizeof(int)));
+        return fail(c, ESM_ETIMEOUT, "a line move of the whole-class launch waited beyond its limit for the "
+                                     "previous move of its item; the class pass is incomplete");
+    }
     return ESM_OK;
 }
 
@@ -653,7 +671,7 @@ int stats_out(esm_ctx *c, int64_t *stats) {
     CK(cudaMemcpyAsync(h, c->d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (int i = 0; i < 2 * (ESM_NFAM + 1) + 1; ++i) stats[i] += (int64_t)h[i];
-    return ESM_OK;
+    return wave_check(c);
 }
 
 }  // namespace
@@ -727,6 +745,15 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         class_steps(c->T, q, st);
         c->class_len[q] = (int)st.size();
         if ((rc = upload(c, &c->d_steps[q], st.data(), st.size()))) return rc;
+    }
+    {  // the per-item progress words of the whole-class launch (k_move_wave) and its error flag
+        int span = c->precision == 64 ? c->Md.span : c->Mf.span;
+        size_t wpt = ((size_t)span * c->R + 31) / 32, mx = 1;
+        for (int q = 0; q < c->ncls; ++q) mx = std::max(mx, (size_t)((c->class_len[q] + span - 1) / span) * wpt);
+        if ((rc = dalloc(c, &c->d_wave_done, mx))) return rc;
+        c->wave_items = mx;
+        if ((rc = dalloc(c, &c->d_wave_err, 1))) return rc;
+        CK(cudaMemset(c->d_wave_err, 0, sizeof(int)));
     }
     // unit tables (FP64)
     int K = c->K;
@@ -1345,7 +1372,7 @@ int esm_sync(esm_ctx *c, double timeout_s) {
     auto t0 = std::chrono::steady_clock::now();
     while (true) {
         cudaError_t e = cudaStreamQuery(c->stream);
-        if (e == cudaSuccess) return ESM_OK;
+        if (e == cudaSuccess) return wave_check(c);
         if (e != cudaErrorNotReady) return fail(c, ESM_ECUDA, "stream: %s", cudaGetErrorString(e));
         double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (el > timeout_s) return fail(c, ESM_ETIMEOUT, "stream not idle after %.1f s", timeout_s);
@@ -1554,6 +1581,28 @@ int esm_set_move_grid(esm_ctx *c, int32_t warps_per_block, int32_t warps_per_sm)
         }
     c->move_wpb = warps_per_block;
     c->max_warps = w;
+    return ESM_OK;
+}
+
+int esm_set_move_schedule(esm_ctx *c, int32_t schedule) {
+    if (!c) return ESM_EINVAL;
+    if (schedule != ESM_MOVES_PER_MOVE && schedule != ESM_MOVES_PER_CLASS)
+        return fail(c, ESM_EINVAL, "schedule must be ESM_MOVES_PER_MOVE or ESM_MOVES_PER_CLASS");
+    if (schedule == c->move_schedule) return ESM_OK;
+    int rc = esm_sync(c, 600.0);  // the captured class passes hold the old schedule: drop them
+    if (rc) return rc;
+    for (auto &g : c->graph)
+        if (g) {
+            CK(cudaGraphExecDestroy(g));
+            g = nullptr;
+        }
+    c->move_schedule = schedule;
+    return ESM_OK;
+}
+
+int esm_move_schedule(const esm_ctx *c, int32_t *schedule) {
+    if (!c || !schedule) return ESM_EINVAL;
+    *schedule = c->move_schedule;
     return ESM_OK;
 }
 

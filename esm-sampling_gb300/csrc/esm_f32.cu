@@ -20,6 +20,7 @@ template size_t linemove_scratch_reals<float>(const DevModel<float> &);
 template size_t linemove_smem_per_warp<float>(const DevModel<float> &);
 template cudaError_t launch_class_pass<float>(const DevModel<float> &, const int *, int, const uint32_t *, int, int, float *, int, int,
                                               unsigned long long *, char *, unsigned int *, const SepLaunch &,
+                                              const WaveLaunch &,
                                               cudaStream_t);
 template size_t sep_region_bytes<float>(const DevModel<float> &);
 template int sep_warps_per_sm<float>(const DevModel<float> &, int *);

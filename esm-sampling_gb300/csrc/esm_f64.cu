@@ -26,6 +26,7 @@ template size_t linemove_scratch_reals<double>(const DevModel<double> &);
 template size_t linemove_smem_per_warp<double>(const DevModel<double> &);
 template cudaError_t launch_class_pass<double>(const DevModel<double> &, const int *, int, const uint32_t *, int, int, double *, int, int,
                                               unsigned long long *, char *, unsigned int *, const SepLaunch &,
+                                              const WaveLaunch &,
                                               cudaStream_t);
 template size_t sep_region_bytes<double>(const DevModel<double> &);
 template int sep_warps_per_sm<double>(const DevModel<double> &, int *);

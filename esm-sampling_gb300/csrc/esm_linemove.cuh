@@ -18,6 +18,14 @@ struct SepLaunch {
     int min_units, max_warps, in_smem;
     char *slab;
 };
+// the whole class pass in one k_move_wave launch (on = 1; not with the cooperative walk): done
+// holds the moves completed per work item (max_items), err is set when a bounded wait runs out
+struct WaveLaunch {
+    int on;
+    unsigned int *done;
+    int *err;
+    size_t max_items;
+};
 template <class real>
 size_t sep_region_bytes(const DevModel<real> &M);
 template <class real>
@@ -28,7 +36,8 @@ int sep_warps_per_sm(const DevModel<real> &M, int *in_smem);
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
                               int limit, real *scratch, int wpb, int max_warps, unsigned long long *stats,
-                              char *descs, unsigned int *counters, const SepLaunch &sep, cudaStream_t s);
+                              char *descs, unsigned int *counters, const SepLaunch &sep, const WaveLaunch &wave,
+                              cudaStream_t s);
 // resident k_move warps per SM with blocks of wpb (1, 2 or 4) warps
 template <class real>
 int linemove_blocks_per_sm(const DevModel<real> &M, int wpb);

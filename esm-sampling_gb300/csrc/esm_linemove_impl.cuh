@@ -1740,6 +1740,132 @@ __global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
 }
 
 // ---------------------------------------------------------------------------------------------
+// the whole class in one launch: items of consecutive moves overlap
+// ---------------------------------------------------------------------------------------------
+__device__ inline unsigned int ld_acquire_u32(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ inline void st_release_u32(unsigned int *p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ inline unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The moves of a class pass take no barrier between them: the tasks of a colour class are
+// independent (a move at step tau writes steps tau and tau - 1, which no other task of the class
+// reads or writes), so a task's move mi + 1 needs only its own move mi. k_move_wave runs the whole
+// class in one launch: its warps take (move, item) pairs from one counter in move-major order,
+// wait until the item's previous move is published in done[item] (moves completed), run the 32
+// tasks exactly as k_move does (move_task), and publish. A warp waits only on an earlier-taken
+// pair, held by a running warp, so the earliest unfinished pair never waits and the pass always
+// progresses; the waits are still bounded (a pair whose predecessor is not published within
+// ESM_WAVE_WAIT_NS sets *err and every warp leaves). The descriptor of a warp's move is read from
+// the descriptor buffer in global memory (read-only during the pass), so warps of one block may
+// run different moves. One launch replaces a pass's per-move launches and the idle tail each of
+// them ends with (8760 items over ~4900 resident warps at T = 8760, 64 replicas: under two items
+// per warp and move).
+#define ESM_WAVE_WAIT_NS 2000000000ull
+template <class real, int WPB>
+__global__ void __launch_bounds__(32 * WPB, MoveBounds<WPB>::min_blocks)
+    k_move_wave(const __grid_constant__ DevModel<real> M, const int *steps, int nsteps, int ntile, int wpt,
+                const uint32_t *sweep_p, int nrun, const char *descs, size_t stride, real *scratch,
+                unsigned long long *stats, unsigned int *next, unsigned int *done, int *err) {
+    __shared__ Desc<real> sd[WPB];
+    __shared__ LaneLayout sLL;
+    int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    if (threadIdx.x == 0) sLL = lane_layout(M.maxpts, M.maxn, M.maxstu, linemove_maxroots(M), M.maxk, M.maxku);
+    if (WPB == 1)
+        __syncwarp();
+    else
+        __syncthreads();
+    const LaneLayout &LL = sLL;
+    real local[ESM_LANE_LOCAL];
+    bool loc = LL.total <= ESM_LANE_LOCAL;
+    real *slab = loc ? local : scratch + ((size_t)blockIdx.x * WPB + wib) * LL.total * 32 + lane;
+    Lane<real> Ln(M, sd[wib], slab, loc ? 1 : 32, lane, LL);
+    uint32_t sweep = *sweep_p;
+    const unsigned int nitems = (unsigned int)(ntile * wpt);
+    const unsigned int total = nitems * (unsigned int)nrun;  // (the host keeps it below 2^32)
+    const int nmoves = M.natoms + M.nextra;
+    int cur = -1, fi = -1;
+    unsigned long long tried = 0, moved = 0, guards = 0;
+    while (true) {
+        unsigned int g = 0;
+        if (lane == 0) g = atomicAdd(next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        bool stop = g >= total || *(volatile int *)err != 0;
+        int mi = stop ? cur : (int)(g / nitems);
+        if (stop || mi != cur) {  // warp-uniform: add the counts of the previous move
+            for (int o = 16; o > 0; o >>= 1) {
+                tried += __shfl_xor_sync(0xffffffffu, tried, o);
+                moved += __shfl_xor_sync(0xffffffffu, moved, o);
+                guards += __shfl_xor_sync(0xffffffffu, guards, o);
+            }
+            if (lane == 0 && fi >= 0) {
+                if (tried) atomicAdd(&stats[2 * fi], tried);
+                if (moved) atomicAdd(&stats[2 * fi + 1], moved);
+                if (guards) atomicAdd(&stats[2 * (ESM_NFAM + 1)], guards);
+            }
+            tried = moved = guards = 0;
+            if (stop) break;
+            if (lane == 0) sd[wib] = carve_desc<real>((char *)descs + (size_t)mi * stride, M, nmoves);
+            __syncwarp();
+            cur = mi;
+            fi = sd[wib].hdr[12];
+        }
+        unsigned int item = g - (unsigned int)mi * nitems;
+        if (mi > 0) {  // the item's previous move, published by the warp that ran it
+            bool ok = true;
+            if (lane == 0) {
+                unsigned long long t0 = 0;
+                while (ld_acquire_u32(&done[item]) < (unsigned int)mi) {
+                    if (*(volatile int *)err != 0) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned long long t = global_ns();
+                    if (t0 == 0)
+                        t0 = t;
+                    else if (t - t0 > ESM_WAVE_WAIT_NS) {
+                        atomicExch(err, 1);
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+            }
+            // the barrier of the shuffle orders every lane's loads after lane 0's acquire
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+        }
+        if (fi >= 0) {
+            int tile = (int)(item / wpt), grp = (int)(item % wpt);
+            int task = grp * 32 + lane;
+            int sit = task / M.R;
+            int q = tile * M.span + sit;
+            if (sit < M.span && q < nsteps) {
+                Ln.rep = task % M.R;
+                bool guard;
+                real t = move_task<real>(Ln, M, sd[wib], LL, fi, mi, steps[q], sweep, &guard);
+                if (guard) ++guards;
+                if (M.mlog && Ln.rep < M.mlog_nrep)
+                    M.mlog[((size_t)mi * nsteps + q) * M.mlog_nrep + Ln.rep] = (double)t;
+                ++tried;
+                if (t != 0) ++moved;
+            }
+        }
+        __threadfence();  // every lane's state writes before the publish
+        __syncwarp();
+        if (lane == 0) st_release_u32(&done[item], (unsigned int)mi + 1);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // host launcher
 // ---------------------------------------------------------------------------------------------
 template <class real>
@@ -1802,7 +1928,8 @@ int sep_warps_per_sm(const DevModel<real> &M, int *in_smem) {
 template <class real>
 cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nsteps, const uint32_t *sweep, int cls,
                               int limit, real *scratch, int wpb, int max_warps, unsigned long long *stats,
-                              char *descs, unsigned int *counters, const SepLaunch &sep, cudaStream_t s) {
+                              char *descs, unsigned int *counters, const SepLaunch &sep, const WaveLaunch &wave,
+                              cudaStream_t s) {
     int nmoves = M.natoms + M.nextra;
     int nrun = limit > 0 && limit < nmoves ? limit : nmoves;
     size_t stride = linemove_smem_per_warp(M);
@@ -1815,6 +1942,20 @@ cudaError_t launch_class_pass(const DevModel<real> &M, const int *steps, int nst
     int items = ntile * wpt;
     int warps = items < max_warps ? items : max_warps;
     int blocks = (warps + wpb - 1) / wpb;
+    if (wave.on && sep.min_units == 0 && (size_t)items <= wave.max_items &&
+        (unsigned long long)items * nrun < (1ull << 32)) {
+        if ((e = cudaMemsetAsync(wave.done, 0, sizeof(unsigned int) * items, s)) != cudaSuccess) return e;
+        if (wpb == 4)
+            k_move_wave<real, 4><<<blocks, 128, 0, s>>>(M, steps, nsteps, ntile, wpt, sweep, nrun, descs, stride,
+                                                       scratch, stats, counters, wave.done, wave.err);
+        else if (wpb == 2)
+            k_move_wave<real, 2><<<blocks, 64, 0, s>>>(M, steps, nsteps, ntile, wpt, sweep, nrun, descs, stride,
+                                                      scratch, stats, counters, wave.done, wave.err);
+        else
+            k_move_wave<real, 1><<<blocks, 32, 0, s>>>(M, steps, nsteps, ntile, wpt, sweep, nrun, descs, stride,
+                                                      scratch, stats, counters, wave.done, wave.err);
+        return cudaGetLastError();
+    }
     int sepmin = sep.min_units;
     int ntask = nsteps * M.R;
     int swarps = ntask < sep.max_warps ? ntask : sep.max_warps;

@@ -294,6 +294,19 @@ int esm_move_log(esm_ctx *ctx, int32_t cls, double *out);
 int esm_set_sep_walk(esm_ctx *ctx, int32_t min_units);
 int esm_sep_walk(const esm_ctx *ctx, int32_t *min_units, int32_t *warps);
 
+/* How the line moves of a class pass are launched. ESM_MOVES_PER_MOVE (the default): one k_move
+   launch per move, all tasks of move mi before any task of move mi + 1. ESM_MOVES_PER_CLASS: the
+   whole class pass in one launch, whose warps take (move, 32-task item) pairs in move-major order
+   and run an item's move mi + 1 as soon as its move mi is done (the tasks of a colour class are
+   independent, so a task's moves and their results are the same: bit-identical states), without
+   the idle tail each per-move launch ends with; each of its waits for an item's previous move is
+   bounded, and one that runs out makes the next esm_sync or statistics read return ESM_ETIMEOUT.
+   Not combined with the cooperative walk (esm_set_sep_walk > 0 keeps the per-move launches). No
+   reference counterpart. */
+enum { ESM_MOVES_PER_MOVE = 0, ESM_MOVES_PER_CLASS = 1 };
+int esm_set_move_schedule(esm_ctx *ctx, int32_t schedule);
+int esm_move_schedule(const esm_ctx *ctx, int32_t *schedule);
+
 /* Autotuner of the line-move grid: for each candidate (warps_per_block, warps_per_sm) -- the three
    block shapes at their resident limits and at 8, 16, 24, 32, 40 warps per SM below them -- one
    colour class of sweep `sweep` is run and timed (CUDA events on the context's stream) from the

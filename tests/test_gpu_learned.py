@@ -78,10 +78,16 @@ def test_surrogate_learns_and_da_mechanics():
 
 
 def test_surrogate_langevin_mixing():
-    """SurrogateLangevin (the surrogate's drift at 4x the plain step, judged by the plain scores)
-    against the plain step from one saved state, one plain evaluation per iteration each: the mean
-    squared jump of w = log(k + kappa_s) per plain evaluation, printed with the share of iterations
-    that used the surrogate; asserted: the states stay finite and the bookkeeping adds up."""
+    """What the trained network gains, and what it costs. SurrogateLangevin (the surrogate's drift at
+    4x the plain step) against the plain step from one saved state, one plain evaluation per
+    iteration each. With its judge off the chain uses the surrogate's drift every iteration and its
+    capacities move much farther per plain evaluation than the plain step's (asserted: the mean
+    squared jump of w = log(k + kappa_s) per plain evaluation is at least twice the plain step's);
+    the carrier means it reaches are printed beside the plain chain's (the longer runs of
+    bench.py --case learned show them shifted by several MCSE: one sweep per step does not keep the
+    replicas' dispatch, on which the plain estimates are taken, in step with 4x faster capacities).
+    With its judge on, the surrogate is used only while its drift agrees with the plain estimates
+    within their noise (asserted: the bookkeeping of learned and plain iterations adds up)."""
     from esmgb.surrogate import SurrogateLangevin
     m, d, eta, ks = _setup()
     ug = np.asarray(m.unit_group)
@@ -97,26 +103,36 @@ def test_surrogate_langevin_mixing():
         d.langevin_step(w, eta, ks, 1.0, 0.02, True, None, it)
     d.state_save()
     n = 60
-    W = []
+    W, KT = [], []
     for it in range(n):
         d.sweeps(1, sweep0=2000 + it, stats=False)
         d.scores()
         k, _ = d.langevin_step(w, eta, ks, 1.0, 0.02, True, None, 2000 + it)
         W.append(np.log(k + ks[ug]))
+        KT.append(np.bincount(ug, weights=k, minlength=len(m.carriers)))
     msj_plain = np.mean(np.sum(np.diff(np.array(W)[:, mv], axis=0) ** 2, axis=1))
-    d.state_restore()
-    sl = SurrogateLangevin(d, m, sur, eta, ks, mult=4.0, seed=2, train_steps=2)
-    W = []
-    for it in range(n):
-        sl.step(2000 + it)
-        W.append(np.log(sl.k + ks[ug]))
-    W = np.array(W)
-    msj = np.mean(np.sum(np.diff(W[:, mv], axis=0) ** 2, axis=1))
-    st = sl.stats
-    print(f"surrogate drift vs plain: msjd per plain evaluation {msj:.3e} vs {msj_plain:.3e} "
-          f"(ratio {msj / msj_plain:.3f}); surrogate steps {st['learned']}/{st['iters']}, "
-          f"judged discrepancy {np.mean(np.abs(sl.z[mv])):.3f}")
-    assert np.all(np.isfinite(W))
-    assert st["plain_evals"] == st["iters"] + 1
+    kt_plain = np.mean(KT, axis=0)
+    out = {}
+    for tol in (float("inf"), 1.0):
+        d.state_restore()
+        sl = SurrogateLangevin(d, m, sur, eta, ks, mult=4.0, seed=2, train_steps=2, tol=tol)
+        W, KT = [], []
+        for it in range(n):
+            sl.step(2000 + it)
+            W.append(np.log(sl.k + ks[ug]))
+            KT.append(np.bincount(ug, weights=sl.k, minlength=len(m.carriers)))
+        W = np.array(W)
+        assert np.all(np.isfinite(W))
+        msj = np.mean(np.sum(np.diff(W[:, mv], axis=0) ** 2, axis=1))
+        st = sl.stats
+        assert st["plain_evals"] == st["iters"] + 1 == n + 1
+        assert 0 <= st["learned"] <= st["iters"]
+        out[tol] = (msj, st["learned"], np.mean(KT, axis=0))
+        print(f"surrogate drift (judge tolerance {tol}): msjd per plain evaluation {msj:.3e} vs plain "
+              f"{msj_plain:.3e} (ratio {msj / msj_plain:.2f}); surrogate steps {st['learned']}/{st['iters']}; "
+              f"carrier means / plain's: {np.round(out[tol][2] / kt_plain, 3).tolist()}")
+    msj_free, used_free, _ = out[float("inf")]
+    assert used_free >= 0.8 * n        # judge off: the surrogate's drift wherever its prediction is in range
+    assert msj_free >= 2.0 * msj_plain
     sur.close()
     d.close()
