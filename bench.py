@@ -123,18 +123,40 @@ def carrier_params(m):
     return eta, ks
 
 
-def device_loop(d, m, ctl, it0, n, rng, pre):
-    """The device-resident step: everything on the GPU, host arrays only for the schedule."""
+def device_loop(d, m, ctl, it0, n, rng, pre, counts=False):
+    """The device-resident step: everything on the GPU, host arrays only for the schedule. With
+    counts, the move counts of the sweeps (tried and taken per family, guard events) are read after
+    each sweep (one more short synchronisation per step: the score call synchronises anyway) and
+    returned summed."""
     eta, ks = carrier_params(m)
     w = np.full(d.R, 1.0 / d.R)
+    total = None
     for q in range(n):
         it = it0 + q
         moved, theta, window, wstart, _ = pre[q] if pre else schedule(ctl, it, d.R, rng)
         if moved.any():
             d.weather_step(moved, theta, window, wstart, it=it)
-        d.sweeps(1, sweep0=it, stats=False)
+        st = d.sweeps(1, sweep0=it, stats=counts)
+        if counts:
+            total = st if total is None else total + st
         d.scores()
         d.langevin_step(w, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
+    return total
+
+
+FAMILIES = ("unit", "pair", "xpair", "xlocc", "xloc", "potential", "cellpair", "cell", "spair", "tpot", "tsoc",
+            "atoms")  # the ESM_FAM_* order of the move counts, then the basis atoms
+
+
+def move_counts(st):
+    """The correctness counters of the bench line from esm_operation_sweeps' counts."""
+    st = np.asarray(st, np.int64)
+    fam = {f: [int(st[2 * i]), int(st[2 * i + 1])] for i, f in enumerate(FAMILIES) if st[2 * i] > 0}
+    tried = int(st[:-1:2].sum())
+    return {"tried": tried, "taken": int(st[1:-1:2].sum()), "guards": int(st[-1]),
+            "guard_rate": int(st[-1]) / max(tried, 1), "by_family": fam,
+            "note": "line moves of the timed sweeps, [tried, taken] per family; a guard event is a walk "
+                    "beyond the point cap, left at t = 0"}
 
 
 def e2e_loop(d, m, ctl, R_set, it0, n, rng):
@@ -778,7 +800,7 @@ def main():
     clk = Clocks()
     clk.start()
     t0 = time.perf_counter()
-    device_loop(d, m, ctl, it0 + args.warmup, args.steps, rng, pre)
+    counts = device_loop(d, m, ctl, it0 + args.warmup, args.steps, rng, pre, counts=True)
     d.sync(600.0)
     wall_dev = time.perf_counter() - t0
     clocks = clk.stop()
@@ -840,6 +862,7 @@ def main():
                           "autotune_ms_per_class": {f"{a}x{b}": round(v, 1) for (a, b), v in grid_ms.items()}},
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
             "line_moves_per_s": moves * args.steps / (dev_ms / 1000.0) * world,
+            "moves": move_counts(counts),
             "storage_ms": {"ms_per_sweep": sms_ms, "moves": int(sms[0]), "moves_taken": int(sms[1]),
                            "note": "storage multiscale sweep (plateau moves) timed alone; it runs in half of "
                                    "the operation sweeps with --storage-ms"},

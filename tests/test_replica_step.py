@@ -83,6 +83,20 @@ def test_bench_e2e_loop_on_the_oracle():
     assert h2d > 0 and d2h == 8 * (4 * m.Kunits + 3 * m.Kunits + 32)
 
 
+def test_bench_device_loop_counts_on_the_oracle():
+    """The bench's timed loop with its correctness counters: the move counts of every sweep, summed,
+    in the bench line's layout (tried and taken per family and for the atoms, guard events)."""
+    m, ch = chain()
+    ctl = RP.ReplicaCtl(M=4)
+    st = bench.device_loop(ch, m, ctl, 10, 2, np.random.Generator(np.random.PCG64(1)), None, counts=True)
+    mc = bench.move_counts(st)
+    assert mc["tried"] == int(np.asarray(st)[:-1:2].sum()) > 0
+    assert 0 < mc["taken"] <= mc["tried"] and mc["guards"] == 0
+    assert set(mc["by_family"]) <= set(bench.FAMILIES) and "atoms" in mc["by_family"]
+    assert sum(v[0] for v in mc["by_family"].values()) == mc["tried"]
+    assert bench.device_loop(ch, m, ctl, 12, 1, np.random.Generator(np.random.PCG64(1)), None) is None
+
+
 def test_lag_probe_per_field():
     class FakeDev:
         def lag_probe(self, j, n, tail, sweep0):
