@@ -33,6 +33,51 @@ def test_haar_atoms_orthonormal(small):
         assert abs(th.val[th.ptr[j]:th.ptr[j + 1]].sum()) < 1e-12
 
 
+def _dense(cols, n):
+    U = np.zeros((n, len(cols)))
+    for j, (rows, vals) in enumerate(cols):
+        U[rows, j] = vals
+    return U
+
+
+def test_haar_bases_reference_properties():
+    """test/test_local.jl:8-41 ("sparse graph Haar field bases") restated: a 30-node path graph
+    with three levels (one cell, countries, nodes). The basis is orthonormal with one column per
+    level cell beyond its parent; on a 17-node support it stays orthonormal and sparse (at most
+    |support| (ceil(log2 |support|) + 3) nonzeros); its first columns up to a level span the fields
+    constant on that level's cells; the angle basis without its top level has N - 2 columns, none
+    with a component constant."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    N = 30
+    country = rng.integers(1, 6, N)
+    parts = [np.ones(N, int), country, np.arange(N)]
+    edges = [(i, i + 1, 1.0) for i in range(N - 1)]
+    cols, gcounts, _ = haar_basis(parts, np.arange(N), edges=edges)
+    U = _dense(cols, N)
+    np.testing.assert_allclose(U.T @ U, np.eye(U.shape[1]), atol=1e-12)
+    assert gcounts == [1, len(np.unique(country)), N]
+    sup = np.sort(rng.permutation(N)[:17])
+    bcols, bcounts, _ = haar_basis(parts, sup, edges=edges)
+    B = _dense(bcols, len(sup))
+    np.testing.assert_allclose(B.T @ B, np.eye(B.shape[1]), atol=1e-12)
+    assert B.shape[1] == len(sup)
+    assert sum(len(r) for r, _ in bcols) <= len(sup) * (int(np.ceil(np.log2(len(sup)))) + 3)
+    for Mq in (1, gcounts[1], N):
+        q = max(i for i, g in enumerate(gcounts) if g <= Mq)   # the level of Mq modes
+        m = bcounts[q]
+        Um = B[:, :m]
+        keys = [tuple(int(p[n]) for p in parts[:q + 1]) for n in sup]
+        for c in set(keys):
+            v = np.array([k == c for k in keys], float)
+            np.testing.assert_allclose(Um @ (Um.T @ v), v, atol=1e-12)
+    comp = np.array([1 if i < 20 else 2 for i in range(N)])
+    tcols, _, _ = haar_basis([comp, country, np.arange(N)], np.arange(N), edges=edges, drop_top=True)
+    T = _dense(tcols, N)
+    assert T.shape[1] == N - 2
+    np.testing.assert_allclose(T.T @ T, np.eye(N - 2), atol=1e-12)
+    assert np.linalg.norm(T.T @ (comp == 1)) < 1e-10 and np.linalg.norm(T.T @ (comp == 2)) < 1e-10
+
+
 def test_move_tables(small):
     m, _ = small
     assert m.units_ptr[-1] == m.D and m.stor_ptr[-1] == m.S
