@@ -271,10 +271,10 @@ def ess_arms(d, m, ctl, it0, n, arms=("plain", "learned", "da")):
     return out
 
 
-def cpu_sample(threads, sweeps=1, R=2, storage_ms=0):
-    """The oracle on the host cores: operation sweeps from sweep 1 and the scores of R of the
-    replicas; with storage_ms, two sweeps (the storage multiscale sweep runs in sweep 1, not in 2:
-    its coin, probability 1/2)."""
+def cpu_sample(threads, sweeps=1, R=2, storage_ms=0, warm=1):
+    """The oracle on the host cores: `warm` untimed operation sweeps from sweep 1 (a worn state, as
+    the GPU chain's), then `sweeps` timed operation sweeps and the scores of R of the replicas; with
+    storage_ms, two timed sweeps (the storage multiscale sweep runs with probability 1/2)."""
     if storage_ms:
         sweeps = 2
     from esmgb.model import initial_state, make_model
@@ -284,39 +284,67 @@ def cpu_sample(threads, sweeps=1, R=2, storage_ms=0):
     st = initial_state(m, R, seed=7)
     o = Oracle(m, R, seed=w["seed"], threads=threads, storage_ms=storage_ms, storage_long=storage_ms)
     o.set_state(st)
+    if warm:
+        o.sweeps(warm, 1)
     t0 = time.perf_counter()
-    o.sweeps(sweeps, 1)
+    o.sweeps(sweeps, 1 + warm)
     o.scores()
     dt = time.perf_counter() - t0
     return sweeps * (R / w["R"]) / dt, dt
 
 
 def run_reference(args):
+    """The reference arm: the reference's algorithm (the FP64 restatement in oracle/, OpenMP over the
+    steps of a colour class) on all host cores, on a bounded sample of the workload -- one chain of 1
+    of the 64 replicas of the same model and start state. Its --warmup steps (untimed) wear the
+    sample's state as the GPU arm's warm-up wears its chain; each timed step is one operation sweep
+    of the sample (the next sweep index; with --storage-ms the storage sweeps as operation_sweep!
+    runs them) and its capacity scores. ms_per_step is the measured wall time of a sample step;
+    value is the workload's rate that the sample implies (the sample's sweeps/s over the replicas it
+    holds: x 64)."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     from oracle import oracle as O
     O.build()
+    from esmgb.model import initial_state, make_model
+    from oracle.oracle import Oracle
+    w = WORKLOAD
+    nrep = 1
+    sm = int(args.storage_ms)
+    m = make_model(w["N"], w["L"], w["T"], seed=w["seed"])
+    o = Oracle(m, nrep, seed=w["seed"], threads=threads, storage_ms=sm, storage_long=sm)
+    o.set_state(initial_state(m, nrep, seed=7))
+    sweep = 1
     for _ in range(args.warmup):
-        cpu_sample(threads, 1, 1, int(args.storage_ms))
-    vals = []
+        o.sweeps(1, sweep)
+        o.scores()
+        sweep += 1
+    dts = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, _ = cpu_sample(threads, 1, 1, int(args.storage_ms))
-        vals.append(v)
+        t1 = time.perf_counter()
+        o.sweeps(1, sweep)
+        o.scores()
+        dts.append(time.perf_counter() - t1)
+        sweep += 1
     wall = time.perf_counter() - t0
-    value = args.steps / sum(1.0 / v for v in vals)
-    sample = (f"each step: one operation sweep (with --storage-ms: sweeps 1 and 2, the storage multiscale sweep "
-              f"in the first) and the capacity scores of 1 of the 64 replicas (T = 8760), scaled to 64 replicas")
+    scale = w["R"] / nrep
+    value = len(dts) / (sum(dts) * scale)
+    sample = (f"one chain of {nrep} of the {w['R']} replicas (T = {w['T']}), worn by {args.warmup} untimed steps; "
+              f"each step one operation sweep{' with the storage sweeps' if sm else ''} and the capacity scores "
+              f"of the sample ({1000.0 * sum(dts) / max(len(dts), 1):.0f} ms per step), scaled x{scale:g} to the "
+              f"workload's replicas")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(dts) / max(len(dts), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(), "sample_scale": scale,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": ("the reference is a Julia package (no Julia on this machine): its algorithm is timed through "
-                     "the FP64 C++ restatement in oracle/, OpenMP over the steps of a colour class"),
+                     "the FP64 C++ restatement in oracle/, OpenMP over the steps of a colour class; ms_per_step is "
+                     "the wall time of a step of the sample, value the workload's rate the sample implies"),
             "wall_s": wall}
     print(json.dumps(line), flush=True)
 
@@ -888,8 +916,9 @@ def main():
             threads = os.cpu_count() or 1
             v, dt = cpu_sample(threads, 1, args.cpu_replicas, int(args.storage_ms))
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": f"operation sweep(s) from sweep 1 and the scores of {args.cpu_replicas} "
-                                              f"of the 64 replicas at T = 8760 ({dt:.1f} s), scaled to 64 replicas"}
+                                    "sample": f"after one untimed operation sweep from the start state, the next "
+                                              f"operation sweep(s) and the scores of {args.cpu_replicas} of the 64 "
+                                              f"replicas at T = 8760 ({dt:.1f} s), scaled to 64 replicas"}
         except Exception as e:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
     print(json.dumps(line), flush=True)
