@@ -93,6 +93,11 @@ struct esm_ctx {
     unsigned int *d_wave_done = nullptr;     // per work item: moves completed (whole-class launch)
     int *d_wave_err = nullptr;               // set when a wait of the whole-class launch ran out
     size_t wave_items = 0;
+    // weather features of the replicas (esm_replica_features): the renewable units' flat indices and
+    // carriers (their groups, numbered in increasing group order), and lazily allocated buffers
+    std::vector<int> ren_unit, ren_car, car_units;
+    double *d_wf_kref = nullptr, *d_wf_buf = nullptr, *d_wf_out = nullptr;
+    int *d_wf_car = nullptr, *d_wf_ncar = nullptr;
     uint32_t *d_sweep = nullptr;         // the sweep index of the current class pass
     // storage multiscale sweep
     int storage_ms = 0, storage_long = 0;
@@ -766,6 +771,21 @@ int esm_create(const esm_model *m, const esm_opts *o, esm_ctx **out) {
         ng = std::max(ng, gq + 1);
     }
     c->ngroups = ng;
+    {  // the renewable units (their order is the kernels' renewable index) and their carriers
+        std::vector<int> gmap(64, -1);
+        int nc = 0;
+        for (int u = 0; u < K; ++u)
+            if (m->unit_kind[u] == ESM_UNIT_REN && gmap[m->unit_group[u]] < 0) gmap[m->unit_group[u]] = 0;
+        for (int gq = 0; gq < 64; ++gq)
+            if (gmap[gq] == 0) gmap[gq] = nc++;
+        c->car_units.assign(nc, 0);
+        for (int u = 0; u < K; ++u)
+            if (m->unit_kind[u] == ESM_UNIT_REN) {
+                c->ren_unit.push_back(u);
+                c->ren_car.push_back(gmap[m->unit_group[u]]);
+                c->car_units[gmap[m->unit_group[u]]] += 1;
+            }
+    }
     vector<int> uloc(K, -1);
     {
         int nr = 0;
@@ -1743,6 +1763,40 @@ __global__ void k_occupancy(int T, int R, int nreg, double h, const int32_t *reg
     if (k >= 0 && k < nreg) atomicAdd(&cnt[k * 4 + sea], 1ull);
 }
 }  // namespace
+
+int esm_replica_features(esm_ctx *c, const double *kref, double *out, int32_t *nfeat) {
+    if (!c) return ESM_EINVAL;
+    int C = (int)c->car_units.size(), nren = (int)c->ren_unit.size();
+    int nf = 5 + C + c->nreg;
+    if (nfeat) *nfeat = nf;
+    if (!out) return ESM_OK;
+    if (!kref) return fail(c, ESM_EINVAL, "kref is required");
+    if (!c->has_state) return fail(c, ESM_ESTATE, "no state uploaded");
+    int rc;
+    size_t TR = (size_t)c->T * c->R;
+    if (!c->d_wf_buf) {
+        if ((rc = dalloc(c, &c->d_wf_kref, (size_t)std::max(nren, 1)))) return rc;
+        if ((rc = dalloc(c, &c->d_wf_car, (size_t)std::max(nren, 1)))) return rc;
+        if ((rc = dalloc(c, &c->d_wf_ncar, (size_t)std::max(C, 1)))) return rc;
+        if ((rc = dalloc(c, &c->d_wf_buf, (size_t)(2 + C) * TR))) return rc;
+        if ((rc = dalloc(c, &c->d_wf_out, (size_t)c->R * nf))) return rc;
+        if (nren) CK(cudaMemcpy(c->d_wf_car, c->ren_car.data(), sizeof(int) * nren, cudaMemcpyHostToDevice));
+        if (C) CK(cudaMemcpy(c->d_wf_ncar, c->car_units.data(), sizeof(int) * C, cudaMemcpyHostToDevice));
+    }
+    std::vector<double> kr(std::max(nren, 1), 0.0);
+    for (int j = 0; j < nren; ++j) kr[j] = kref[c->ren_unit[j]];
+    CK(cudaMemcpyAsync(c->d_wf_kref, kr.data(), sizeof(double) * kr.size(), cudaMemcpyHostToDevice, c->stream));
+    if (c->precision == 64)
+        CK(esm::launch_weather_features<double>(c->Md, c->d_wf_kref, c->d_wf_car, C, c->d_wf_ncar, c->d_reg, c->d_wf_buf,
+                                                c->d_wf_out, c->stream));
+    else
+        CK(esm::launch_weather_features<float>(c->Mf, c->d_wf_kref, c->d_wf_car, C, c->d_wf_ncar, c->d_reg, c->d_wf_buf,
+                                               c->d_wf_out, c->stream));
+    c->launches += 2;
+    CK(cudaMemcpyAsync(out, c->d_wf_out, sizeof(double) * c->R * nf, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return ESM_OK;
+}
 
 int esm_regime_occupancy(esm_ctx *c, double *occ) {
     if (!c || !occ) return ESM_EINVAL;

@@ -42,5 +42,7 @@ template cudaError_t launch_weather_z<float>(const DevModel<float> &, const doub
                                              const double *, const double *, const double *, const int *,
                                              const double *, const int *, const int *, const double *, uint64_t,
                                              uint32_t, int, cudaStream_t);
+template cudaError_t launch_weather_features<float>(const DevModel<float> &, const double *, const int *, int,
+                                                    const int *, const int32_t *, double *, double *, cudaStream_t);
 template cudaError_t launch_compensate<float>(const DevModel<float> &, const int *, const float *, cudaStream_t);
 }  // namespace esm

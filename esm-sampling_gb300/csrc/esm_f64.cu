@@ -48,5 +48,7 @@ template cudaError_t launch_weather_z<double>(const DevModel<double> &, const do
                                              const double *, const double *, const double *, const int *,
                                              const double *, const int *, const int *, const double *, uint64_t,
                                              uint32_t, int, cudaStream_t);
+template cudaError_t launch_weather_features<double>(const DevModel<double> &, const double *, const int *, int,
+                                                    const int *, const int32_t *, double *, double *, cudaStream_t);
 template cudaError_t launch_compensate<double>(const DevModel<double> &, const int *, const double *, cudaStream_t);
 }  // namespace esm

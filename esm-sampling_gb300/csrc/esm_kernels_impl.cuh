@@ -1015,4 +1015,113 @@ cudaError_t launch_compensate(const DevModel<real> &M, const int *moved, const r
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Weather features of every replica (weather_features / replica_features, src/replicas.jl:246-276):
+// the system load D_t = sum_n (load of node n)+, the availability of every weather-dependent
+// carrier, and the residual load D_t - sum_j kref_j A_j,t at fixed reference capacities of the
+// renewable units, from the replica's weather X = xbar + s z and the data map (k_rebuild's).
+// Pass 1, one thread per (step, replica): per step the load and residual load in GW and the
+// carriers' summed availabilities, into buf [(2 + C) x T x R] (replica fastest). Pass 2, one block
+// per replica: the means over the year, the residual load's peak and worst cyclic 7-step mean, the
+// regime frequencies and the number of regime switches, every sum in a fixed order (bitwise
+// repeatable).
+// ---------------------------------------------------------------------------------------------
+template <class real>
+__global__ void k_wfeat_steps(DevModel<real> M, const double *kref_r, const int *carrier_r, int C, double *buf) {
+    size_t TR = (size_t)M.T * M.R;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= TR) return;
+    int t = (int)(i / M.R), rep = (int)(i % M.R);
+    double D = 0;
+    for (int n = 0; n < M.N; ++n) {
+        double x = (double)wraw(M, n, t, rep);
+        D += x > 0 ? x : 0.0;
+    }
+    double Rs = 0;
+    for (int c = 0; c < C; ++c) buf[(size_t)(2 + c) * TR + i] = 0;
+    for (int j = 0; j < M.Nren; ++j) {
+        double A = (double)avail_map<real>(wraw(M, M.r_series[j], t, rep));
+        Rs += kref_r[j] * A;
+        int c = carrier_r[j];
+        buf[(size_t)(2 + c) * TR + i] += A;
+    }
+    buf[i] = D / 1e3;
+    buf[TR + i] = (D - Rs) / 1e3;
+}
+
+#define ESM_WFEAT_THREADS 256
+template <class real>
+__global__ void __launch_bounds__(ESM_WFEAT_THREADS) k_wfeat_reduce(int T, int R, int C, const int *ncar,
+                                                                   const double *buf, const int32_t *reg, int nreg,
+                                                                   double *out) {
+    __shared__ double sh[ESM_WFEAT_THREADS];
+    int rep = blockIdx.x, tid = threadIdx.x;
+    size_t TR = (size_t)T * R;
+    int nf = 5 + C + nreg;
+    double *o = out + (size_t)rep * nf;
+    // a fixed-order block sum (each thread's strided steps in order, then a tree) of f(t)
+    auto bsum = [&](auto f) -> double {
+        double a = 0;
+        for (int t = tid; t < T; t += ESM_WFEAT_THREADS) a += f(t);
+        sh[tid] = a;
+        __syncthreads();
+        for (int w = ESM_WFEAT_THREADS / 2; w > 0; w >>= 1) {
+            if (tid < w) sh[tid] += sh[tid + w];
+            __syncthreads();
+        }
+        double v = sh[0];
+        __syncthreads();
+        return v;
+    };
+    auto bmax = [&](auto f) -> double {
+        double a = -INFINITY;
+        for (int t = tid; t < T; t += ESM_WFEAT_THREADS) a = fmax(a, f(t));
+        sh[tid] = a;
+        __syncthreads();
+        for (int w = ESM_WFEAT_THREADS / 2; w > 0; w >>= 1) {
+            if (tid < w) sh[tid] = fmax(sh[tid], sh[tid + w]);
+            __syncthreads();
+        }
+        double v = sh[0];
+        __syncthreads();
+        return v;
+    };
+    auto at = [&](int f, int t) { return buf[(size_t)f * TR + (size_t)t * R + rep]; };
+    double load = bsum([&](int t) { return at(0, t); });
+    double res = bsum([&](int t) { return at(1, t); });
+    double peak = bmax([&](int t) { return at(1, t); });
+    double w7 = bmax([&](int t) {
+        double a = 0;
+        for (int q = 0; q < 7; ++q) a += at(1, (t + q) % T);
+        return a / 7.0;
+    });
+    if (tid == 0) {
+        o[0] = load / T;
+        o[1 + C] = res / T;
+        o[2 + C] = peak;
+        o[3 + C] = w7;
+    }
+    for (int c = 0; c < C; ++c) {
+        double a = bsum([&](int t) { return at(2 + c, t); });
+        if (tid == 0) o[1 + c] = ncar[c] > 0 ? a / ((double)T * ncar[c]) : 0.0;
+    }
+    for (int k = 0; k < nreg; ++k) {
+        double a = bsum([&](int t) { return reg[(size_t)t * R + rep] == k ? 1.0 : 0.0; });
+        if (tid == 0) o[4 + C + k] = a / T;
+    }
+    double sw = bsum([&](int t) { return t + 1 < T && reg[(size_t)(t + 1) * R + rep] != reg[(size_t)t * R + rep] ? 1.0 : 0.0; });
+    if (tid == 0) o[4 + C + nreg] = sw;
+}
+
+template <class real>
+cudaError_t launch_weather_features(const DevModel<real> &M, const double *kref_r, const int *carrier_r, int C,
+                                    const int *ncar, const int32_t *reg, double *buf, double *out, cudaStream_t s) {
+    size_t TR = (size_t)M.T * M.R;
+    k_wfeat_steps<real><<<(unsigned)((TR + 255) / 256), 256, 0, s>>>(M, kref_r, carrier_r, C, buf);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_wfeat_reduce<real><<<M.R, ESM_WFEAT_THREADS, 0, s>>>(M.T, M.R, C, ncar, buf, reg, M.nreg, out);
+    return cudaGetLastError();
+}
+
 }  // namespace esm

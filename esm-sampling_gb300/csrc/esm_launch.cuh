@@ -42,4 +42,9 @@ cudaError_t launch_weather_z(const DevModel<real> &M, const double *phi, const d
                              int use_theta, cudaStream_t s);
 template <class real>
 cudaError_t launch_compensate(const DevModel<real> &M, const int *moved, const real *r0, cudaStream_t s);
+// the weather features of every replica (esm_kernels_impl.cuh): per-step pass into buf
+// [(2 + C) * T * R], then one block per replica into out [R * (5 + C + nreg)]
+template <class real>
+cudaError_t launch_weather_features(const DevModel<real> &M, const double *kref_r, const int *carrier_r, int C,
+                                    const int *ncar, const int32_t *reg, double *buf, double *out, cudaStream_t s);
 }  // namespace esm

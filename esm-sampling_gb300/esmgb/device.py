@@ -26,7 +26,8 @@ EXPORTS = ("esm_create", "esm_destroy", "esm_last_error", "esm_upload_state", "e
            "esm_autotune_moves", "esm_storage_ms", "esm_storage_long", "esm_lag_probe", "esm_set_sep_walk",
            "esm_sep_walk", "esm_set_move_log", "esm_move_log", "esm_batch_create", "esm_batch_destroy",
            "esm_batch_last_error", "esm_batch_sweeps", "esm_batch_set_grid", "esm_batch_grid", "esm_batch_autotune",
-           "esm_batch_time", "esm_batch_launch_count", "esm_set_move_schedule", "esm_move_schedule")
+           "esm_batch_time", "esm_batch_launch_count", "esm_set_move_schedule", "esm_move_schedule",
+           "esm_replica_features")
 TUNE_MAX = 16  # ESM_TUNE_MAX
 KERNEL_FAMILIES = ("class_pass", "rebuild", "score", "langevin_follow", "weather", "storage")
 
@@ -92,6 +93,7 @@ def load(build_if_missing=True):
     L.esm_timing.argtypes = [C.c_void_p, P_f64]
     L.esm_stream.restype = C.c_void_p
     L.esm_stream.argtypes = [C.c_void_p]
+    L.esm_replica_features.argtypes = [C.c_void_p, P_f64, P_f64, P_i32]
     L.esm_set_move_schedule.argtypes = [C.c_void_p, C.c_int32]
     L.esm_move_schedule.argtypes = [C.c_void_p, P_i32]
     L.esm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
@@ -282,6 +284,16 @@ class DeviceChain:
     def set_move_grid(self, warps_per_block=1, warps_per_sm=0):
         """Line-move grid: blocks of 1, 2 or 4 warps, resident warps per SM (0: that shape's limit)."""
         self._check(self.L.esm_set_move_grid(self.h, int(warps_per_block), int(warps_per_sm)), "esm_set_move_grid")
+
+    def replica_features(self, kref):
+        """esm_replica_features: the weather features of every replica [R, nfeat] at the reference
+        capacities kref [K] (columns: replicas.replica_feature_names)."""
+        nf = np.zeros(1, np.int32)
+        self._check(self.L.esm_replica_features(self.h, None, None, _p(nf, P_i32)), "esm_replica_features")
+        out = np.zeros((self.R, int(nf[0])))
+        kr = np.ascontiguousarray(kref, dtype=np.float64)
+        self._check(self.L.esm_replica_features(self.h, _p(kr), _p(out), _p(nf, P_i32)), "esm_replica_features")
+        return out
 
     def set_move_schedule(self, schedule):
         """How a class pass launches its line moves: "move" (one launch per move) or "class" (the

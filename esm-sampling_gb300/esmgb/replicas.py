@@ -158,6 +158,56 @@ def drift_weights(ctl: ReplicaCtl, Phis, active):
     return uniform_weights(active) if ctl.Phi is None else tilt_weights(ctl.lam, Phis, active)
 
 
+def replica_feature_names(m):
+    """``src/replicas.jl:277`` replica_feature_names: the order of esm_replica_features' columns."""
+    ren = sorted({int(g) for g, k in zip(m.unit_group, m.unit_kind) if k == 0})
+    return (["load_GW"] + ["cf_" + m.carriers[g] for g in ren] + ["resload_mean_GW", "resload_peak_GW",
+            "resload_7step_GW"] + [f"regime_{k + 1}" for k in range(m.K)] + ["regime_switches"])
+
+
+def weather_features(m, z, reg, kref):
+    """``src/replicas.jl:246`` weather_features and ``:274`` replica_features of one weather path
+    (anomalies z [n0, T], regimes reg [T]) on the host, as esm_replica_features computes them on the
+    device for every replica: the nodes' loads are series 0 .. N-1, the data map is the model's
+    (load (x)+, availability logistic(x)), the residual load is taken at the reference capacities
+    kref [K] of the renewable units. Used for the prior statistics of the tilt functional."""
+    X = m.xbar + m.wscale[:, None] * np.asarray(z, float)
+    D = np.maximum(X[: m.N], 0.0).sum(axis=0)
+    kind = np.asarray(m.unit_kind)
+    ren = np.flatnonzero(kind == 0)
+    A = 1.0 / (1.0 + np.exp(-X[np.asarray(m.unit_series)[ren]]))
+    Rs = (np.asarray(kref, float)[ren][:, None] * A).sum(axis=0)
+    res = (D - Rs) / 1e3
+    T = len(res)
+    w7 = max(np.mean(res[np.arange(t, t + 7) % T]) for t in range(T))
+    groups = np.asarray(m.unit_group)[ren]
+    cf = [float(A[groups == g].mean()) for g in sorted(set(groups.tolist()))]
+    reg = np.asarray(reg)
+    freq = [float(np.mean(reg == k)) for k in range(m.K)]
+    return np.array([D.mean() / 1e3, *cf, res.mean(), res.max(), w7, *freq, float(np.count_nonzero(np.diff(reg)))])
+
+
+class TiltFunctional:
+    """``src/replicas.jl:278`` TiltFunctional: Phi(x) = the annual mean residual load of a replica's
+    weather at the fixed reference capacities kref [K], standardised by its prior mean and standard
+    deviation, estimated from n exact prior draws (``:291``, stream rng). Called with a chain, it
+    evaluates Phi for every replica of the chain (esm_replica_features)."""
+
+    def __init__(self, m, kref, rng, n: int = 200):
+        from .model import sample_weather
+        self.kref = np.asarray(kref, float).copy()
+        self.col = replica_feature_names(m).index("resload_mean_GW")
+        v = []
+        for _ in range(n):
+            reg, z = sample_weather(m, rng)
+            v.append(weather_features(m, z, reg, self.kref)[self.col])
+        self.mu = float(np.mean(v))
+        self.sigma = float(np.std(v, ddof=1))
+
+    def __call__(self, dev):
+        return (np.asarray(dev.replica_features(self.kref))[:, self.col] - self.mu) / self.sigma
+
+
 def adapt_step(R: ReplicaSet, gap, ctl: ReplicaCtl) -> bool:
     """``src/replicas.jl:758`` adapt_step!: shrink/grow eta_w per k field from probe_avg probes."""
     R.gaps.append(list(gap))
@@ -339,14 +389,17 @@ def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, rat
     for j in range(M):
         update_gate(R, j, [_div(a, b) for a, b in zip(rs_all[j].tolist(), fkm)], ctl)
         record_hist(R, j, rsk[j], ctl)
-    wts = drift_weights(ctl, np.zeros(M) if Phis is None else Phis, R.active)
+    if Phis is None:   # Phi of every replica's weather after its weather step (src/replicas.jl:691)
+        Phis = np.zeros(M) if ctl.Phi is None else np.asarray(ctl.Phi(dev), float)
+    wts = drift_weights(ctl, Phis, R.active)
     eta = np.asarray(R.eta_w, float)
     ks = np.asarray(kappa_s, float)
     knew, nclip = dev.langevin_step(wts, eta, ks, ctl.kappa_min, ctl.clip, ctl.box, None, it)
     h2d += wts.nbytes + eta.nbytes + ks.nbytes
     d2h += knew.nbytes
     sbar = np.asarray(wts) @ sk
-    return {"it": it, "moved": moved.astype(bool), "sk": sk, "fk": fk, "parts": parts, "wts": wts, "kraw": kraw,
+    return {"it": it, "moved": moved.astype(bool), "sk": sk, "fk": fk, "parts": parts, "wts": wts, "Phis": Phis,
+            "kraw": kraw,
             "knew": knew, "nclip": nclip, "rs": masked_means(ratio * sbar, mask, groups, nf), "fkm": fkm,
             "h2d": h2d, "d2h": d2h}
 

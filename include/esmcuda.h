@@ -331,6 +331,18 @@ int esm_lag_probe(esm_ctx *ctx, int32_t j, int32_t nsweeps, int32_t tail, int64_
    season of a step as season (src/weather.jl:50). The regime summary fed to the surrogate. */
 int esm_regime_occupancy(esm_ctx *ctx, double *occ);
 
+/* Weather features of every replica (replica_features / weather_features, src/replicas.jl:246-276),
+   from its weather anomalies through the model's data map: per replica r, out[r * nfeat + i] is
+   [0] the annual mean system load (GW: the sum over nodes of the positive load, / 1e3), [1 .. C]
+   the annual mean availability of each weather-dependent carrier (the carriers of the renewable
+   units in increasing group order, averaged over their units), [1 + C] the annual mean residual
+   load at the reference capacities kref [K] (load minus the sum over renewable units of kref times
+   availability, GW), [2 + C] its peak step, [3 + C] its worst cyclic 7-step mean, [4 + C .. 3 + C +
+   nreg] the frequency of each regime over the steps, [4 + C + nreg] the number of regime switches;
+   nfeat = 5 + C + nreg (written whenever nfeat is not NULL; out NULL: only nfeat). The declared
+   tilt functional of the replica step (TiltFunctional, :278) is the standardised feature [1 + C]. */
+int esm_replica_features(esm_ctx *ctx, const double *kref, double *out, int32_t *nfeat);
+
 /* Weather step of the replicas flagged in `moved` [R] (0/1): pCN of angle theta[r] in the VAR
    innovations (src/replicas.jl:105 pcn_weather), then with window[r] > 0 a regime window move of
    that length starting at wstart[r] (:156 regime_window, uniforms from the stream), then the

@@ -5,6 +5,7 @@ Langevin step, and the bytes each way are those of the arrays copied."""
 import math
 
 import numpy as np
+import pytest
 
 import bench
 from esmgb import replicas as RP
@@ -32,6 +33,10 @@ class OracleChain:
 
     def langevin_step(self, *a, **kw):
         return self.o.langevin_step(*a, **kw)
+
+    def replica_features(self, kref):
+        st = self.o.get_state()
+        return np.stack([RP.weather_features(self.m, st["z"][:, :, j], st["reg"][:, j], kref) for j in range(self.R)])
 
 
 def chain(R=4, T=40):
@@ -95,6 +100,59 @@ def test_bench_device_loop_counts_on_the_oracle():
     assert set(mc["by_family"]) <= set(bench.FAMILIES) and "atoms" in mc["by_family"]
     assert sum(v[0] for v in mc["by_family"].values()) == mc["tried"]
     assert bench.device_loop(ch, m, ctl, 12, 1, np.random.Generator(np.random.PCG64(1)), None) is None
+
+
+def test_weather_features_host():
+    """weather_features (src/replicas.jl:246, :274) on the host: the load and residual-load columns
+    from the data map directly, the residual load equal to the load without reference capacities,
+    the regime frequencies summing to 1, the peak above the worst 7-step mean above the mean."""
+    m, ch = chain()
+    st = ch.o.get_state()
+    z, reg = st["z"][:, :, 1], st["reg"][:, 1]
+    names = RP.replica_feature_names(m)
+    kref = np.asarray(m.unit_hi, float) * 0.3
+    f = RP.weather_features(m, z, reg, kref)
+    assert len(f) == len(names)
+    X = m.xbar + m.wscale[:, None] * z
+    D = np.maximum(X[: m.N], 0).sum(0)
+    assert f[names.index("load_GW")] == pytest.approx(D.mean() / 1e3, rel=1e-13)
+    f0 = RP.weather_features(m, z, reg, np.zeros(m.Kunits))
+    assert f0[names.index("resload_mean_GW")] == pytest.approx(f0[names.index("load_GW")], rel=1e-13)
+    i = names.index("resload_mean_GW")
+    assert f[i + 1] >= f[i + 2] >= f[i] and f[i] < f0[i]
+    freq = [f[names.index(f"regime_{k + 1}")] for k in range(m.K)]
+    assert sum(freq) == pytest.approx(1.0) and f[-1] == np.count_nonzero(np.diff(reg))
+    cfs = [f[j] for j, nm in enumerate(names) if nm.startswith("cf_")]
+    assert len(cfs) >= 2 and all(0 < c < 1 for c in cfs)
+
+
+def test_replica_step_stress_tilt():
+    """replica_step with a declared tilt functional (TiltFunctional, src/replicas.jl:278; the
+    reference's check "one step; lambda = 0 is the untilted step bitwise", test/test_replicas.jl:249):
+    Phi of every replica from its weather, standardised by the prior statistics; at lambda = 0 the
+    weights and the new capacities are those of the untilted step bit for bit; at lambda = 2 the
+    weights are exp(lambda Phi) over the active replicas and the capacities move differently."""
+    m, _ = chain()
+    kref = np.asarray(m.unit_hi, float) * 0.3
+    Phi = RP.TiltFunctional(m, kref, np.random.Generator(np.random.PCG64(2)), n=20)
+    assert math.isfinite(Phi.mu) and Phi.sigma > 0
+    ks = np.array([LANGEVIN_KAPPA.get(c, 100.0) for c in m.carriers])
+    out = {}
+    for lab, phi, lam in (("none", None, 0.0), ("zero", Phi, 0.0), ("two", Phi, 2.0)):
+        _, ch = chain()
+        ctl = RP.ReplicaCtl(M=4, burst_every=3, Phi=phi, lam=lam)
+        Rs = RP.ReplicaSet(M=4, eta_w=[5e-4] * len(m.carriers))
+        rec = RP.replica_step(ch, Rs, ctl, 1, np.random.Generator(np.random.PCG64(5)), ks, m.beta_k / m.beta_v,
+                              m.unit_hi, m.unit_group)
+        out[lab] = (rec, ch)
+    (rn, _), (rz, chz), (r2, _) = out["none"], out["zero"], out["two"]
+    assert np.array_equal(rz["wts"], rn["wts"]) and np.array_equal(rz["knew"], rn["knew"])
+    assert np.allclose(rz["Phis"], (chz.replica_features(kref)[:, Phi.col] - Phi.mu) / Phi.sigma)
+    assert np.all(rn["Phis"] == 0)
+    act = rn["wts"] > 0
+    w = np.where(act, np.exp(2.0 * r2["Phis"] - (2.0 * r2["Phis"][act]).max()), 0.0)
+    np.testing.assert_allclose(r2["wts"], w / w.sum(), rtol=1e-14)
+    assert not np.array_equal(r2["wts"], rz["wts"]) and not np.array_equal(r2["knew"], rz["knew"])
 
 
 def test_lag_probe_per_field():
