@@ -407,20 +407,55 @@ def replica_step(dev, R: ReplicaSet, ctl: ReplicaCtl, it: int, rng, kappa_s, rat
 LANGEVIN_ETA = 5e-4   # the initial Langevin step of every k field (langevin_eta, src/run.jl:105)
 
 
+REPLICA_TRACE_KEYS = ("ktot", "capex", "op", "shed", "penalty", "pfcost", "weights", "active", "since", "phi", "rs",
+                      "fk", "eta_w", "nclip", "moved", "time", "features")   # src/replicas.jl:807
+
+
+def replica_record(dev, R: ReplicaSet, rec, kref, groups, nf, t):
+    """``src/replicas.jl:811`` replica_record: the per-step record of a chain's replicas, keyed as
+    REPLICA_TRACE_KEYS -- the capacity totals per k field, the capex and per replica the operational
+    cost, shed, penalty and generation-plus-storage-plus-capex cost (the cost parts of the step's
+    score call: capex, op, gen, storage, shed, dump, penalty), the drift weights, gates and Phi, the
+    field means, the step sizes, the clip count, the weather moves, the times (since the run's start
+    and of the step) and the replicas' weather features at the reference capacities, stacked
+    replica by replica."""
+    parts = np.asarray(rec["parts"], float)
+    knew = np.asarray(rec["knew"], float)
+    feats = np.asarray(dev.replica_features(kref), float).reshape(-1)
+    return {"ktot": [float(np.sum(knew[groups == f])) for f in range(nf)], "capex": [float(parts[0, 0])],
+            "op": parts[:, 1], "shed": parts[:, 4], "penalty": parts[:, 6],
+            "pfcost": parts[:, 0] + parts[:, 2] + parts[:, 3], "weights": np.asarray(rec["wts"], float),
+            "active": np.asarray(R.active, float), "since": np.minimum(np.asarray(R.since, float), 1e6),
+            "phi": np.asarray(rec["Phis"], float), "rs": rec["rs"], "fk": rec["fkm"], "eta_w": list(R.eta_w),
+            "nclip": [float(rec["nclip"])], "moved": np.asarray(rec["moved"], float), "time": t, "features": feats}
+
+
 def run_replicas(dev, s0, ctl: ReplicaCtl, nwarm: int, nprod: int, rng, *, kappa_s, ratio: float, hi, groups,
-                 seed: int, init_sweeps: int = 2, snapshot_path=None, snapshot_every: int = 0):
+                 seed: int, init_sweeps: int = 2, snapshot_path=None, snapshot_every: int = 0,
+                 tilt_functional=None, tilt_samples: int = 200):
     """``src/replicas.jl:841`` run_replicas for one chain on `dev` (the C ABI's calls; no
     configuration system, logs or output files): resume from ``snapshot_path`` when it holds a
     snapshot of this chain (read_replica_snapshot with its checks), else init_replicas from `s0`;
-    then the steps up to nwarm + nprod (replica_step); every ``probe_every`` steps the lag probe of
-    probe_candidate (the chain must be created with the probe context) with the step adaptation
-    during the warm-up (adapt_step, ``:921-926``); a snapshot every ``snapshot_every`` steps before
-    the last (boundary!). Returns (ReplicaSet, step records, probe records), the records as
-    dictionaries of per-step vectors, as the snapshot's trace and probe groups keep them."""
+    then the steps up to nwarm + nprod (replica_step), each recorded by replica_record; every
+    ``probe_every`` steps the lag probe of probe_candidate (the chain must be created with the probe
+    context) with the step adaptation during the warm-up (adapt_step, ``:921-926``); a snapshot
+    every ``snapshot_every`` steps before the last (boundary!). The reference capacities of the
+    features and of the tilt are s0's (``:863``); tilt_functional "resload_mean" declares the tilt
+    (TiltFunctional from tilt_samples exact draws of the stream seed + 5151, ``:865``; its lambda is
+    ctl.lam). Returns (ReplicaSet, step records, probe records), the records as dictionaries of
+    per-step vectors, as the snapshot's trace and probe groups keep them."""
+    import time as _time
+
     from . import snapshot as SN
     groups = np.asarray(groups)
     nf = int(groups.max()) + 1
     eta_w = list(ctl.eta_w) if ctl.eta_w else [LANGEVIN_ETA] * nf
+    kref = np.asarray(s0["k"] if isinstance(s0, dict) else s0.k, float).copy()
+    if tilt_functional is not None:
+        if tilt_functional != "resload_mean":
+            raise ValueError(f"unknown tilt functional {tilt_functional!r} (the reference's: 'resload_mean')")
+        ctl.Phi = TiltFunctional(dev.m, kref, np.random.Generator(np.random.PCG64(seed + 5151)), n=tilt_samples)
+    t_start = _time.perf_counter()
     snap = SN.read_replica_snapshot(snapshot_path, seed=seed, shapes=dev.shapes()) if snapshot_path else None
     if snap is not None:
         R = ReplicaSet(M=dev.R, eta_w=eta_w)
@@ -432,10 +467,11 @@ def run_replicas(dev, s0, ctl: ReplicaCtl, nwarm: int, nprod: int, rng, *, kappa
         R.eta_w = eta_w
         it0, trace, probes, restarts = 0, {}, {}, 0
     for it in range(it0 + 1, nwarm + nprod + 1):
+        t1 = _time.perf_counter()
         rec = replica_step(dev, R, ctl, it, rng, kappa_s, ratio, hi, groups)
-        for key, val in (("it", [it]), ("ktot", [float(np.sum(rec["knew"][groups == f])) for f in range(nf)]),
-                         ("rs", rec["rs"]), ("fk", rec["fkm"]), ("active", [float(sum(R.active))]),
-                         ("nclip", [rec["nclip"]])):
+        t2 = _time.perf_counter()
+        trace.setdefault("it", []).append(np.asarray([it], float))
+        for key, val in replica_record(dev, R, rec, kref, groups, nf, [t2 - t_start, t2 - t1]).items():
             trace.setdefault(key, []).append(np.asarray(val, float))
         if ctl.probe_every > 0 and it % ctl.probe_every == 0:
             j = probe_candidate(R, ctl)

@@ -42,6 +42,10 @@ class OracleChain:
     def langevin_step(self, *a, **kw):
         return self.o.langevin_step(*a, **kw)
 
+    def replica_features(self, kref):
+        st = self.o.get_state()
+        return np.stack([RP.weather_features(self.m, st["z"][:, :, j], st["reg"][:, j], kref) for j in range(self.R)])
+
     def lag_probe(self, j, nsweeps, tail, sweep0):
         s = self.o.get_state()
         c = Oracle(self.m, 1, seed=probe_seed(SEED))
@@ -86,6 +90,34 @@ def test_run_replicas_probes_adapt_in_warmup_only(tmp_path):
         else:
             np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(R.eta_w, probes["eta_after"][-1])
+    # the per-step record of the reference's driver (replica_record, src/replicas.jl:807-819)
+    assert set(RP.REPLICA_TRACE_KEYS) <= set(trace)
+    nfeat = len(RP.replica_feature_names(m))
+    for key, n in (("capex", 1), ("op", 4), ("shed", 4), ("penalty", 4), ("pfcost", 4), ("weights", 4), ("active", 4),
+                   ("since", 4), ("phi", 4), ("moved", 4), ("time", 2), ("features", 4 * nfeat),
+                   ("eta_w", len(m.carriers)), ("nclip", 1)):
+        assert all(len(v) == n for v in trace[key]), key
+    assert all(np.all(v == 0) for v in trace["phi"])          # no tilt declared
+    assert all(abs(v.sum() - 1) < 1e-12 for v in trace["weights"])
+    k0 = np.asarray(s0.k, float)
+    f0 = RP.weather_features(m, ch.o.get_state()["z"][:, :, 0], ch.o.get_state()["reg"][:, 0], k0)
+    np.testing.assert_allclose(trace["features"][-1][:nfeat], f0, rtol=1e-12)
+
+
+def test_run_replicas_declared_tilt():
+    """tilt_functional "resload_mean" (src/replicas.jl:865): Phi from the replicas' weather, the
+    drift weights exp(lambda Phi) over the active replicas, both recorded."""
+    m, s0, ch, kw = setup()
+    ctl = ctl_for(4)
+    ctl.lam = 1.0
+    R, trace, _ = RP.run_replicas(ch, s0, ctl, 2, 1, np.random.Generator(np.random.PCG64(1)),
+                                  tilt_functional="resload_mean", tilt_samples=20, **kw)
+    assert isinstance(ctl.Phi, RP.TiltFunctional)
+    for phi, w, act in zip(trace["phi"], trace["weights"], trace["active"]):
+        a = act > 0 if act.any() else np.ones(4, bool)
+        e = np.where(a, np.exp(phi - phi[a].max()), 0.0)
+        np.testing.assert_allclose(w, e / e.sum(), rtol=1e-13)
+    assert np.ptp(trace["phi"][-1]) > 0
 
 
 def test_run_replicas_snapshot_and_resume(tmp_path):
