@@ -569,9 +569,15 @@ struct Lane {
         }
     }
 
-    // logseg, trexp_offset (src/local.jl:1099, :1106)
+    // logseg, trexp_offset (src/local.jl:1099, :1106). For x > 0 the FP32 build takes the log of
+    // the product, L (1 - e^-x) / x, whose factors stay inside the FP32 range (the second lies in
+    // (0, 1]): one logarithm instead of three, the same value to a few ulp; the FP64 build keeps the
+    // reference's sum of logarithms, as the oracle does.
     __device__ static real logseg(real L, real x) {
         if (fabs(x) < real(1e-10)) return log(L) - x / 2;
+        if constexpr (sizeof(real) == 4) {
+            if (x > 0) return log(L * (-expm1(-x)) / x);
+        }
         if (x > 0) return log(L) + log(-expm1(-x)) - log(x);
         return log(L) - x + log(-expm1(x)) - log(-x);
     }
@@ -902,11 +908,15 @@ struct Lane {
             mx = fmax(mx, lm);
         }
         real tot = 0;
-        for (int j = 0; j < nseg; ++j) tot += exp(S(LL.lm, j) - mx);
+        for (int j = 0; j < nseg; ++j) {  // the masses relative to the largest, kept for the inversion
+            real e = exp(S(LL.lm, j) - mx);
+            S(LL.lm, j) = e;
+            tot += e;
+        }
         real u = ucat * tot, acc = 0;
         int jj = nseg - 1;
         for (int q = 0; q < nseg; ++q) {
-            acc += exp(S(LL.lm, q) - mx);
+            acc += S(LL.lm, q);
             if (u <= acc) {
                 jj = q;
                 break;
