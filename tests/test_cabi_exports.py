@@ -44,3 +44,33 @@ def test_header_constants_match_the_binding():
     assert DV.NSTAT == O.NSTAT == 2 * (cabi.NFAM + 1) + 1
     xor = int(re.search(r"esm_probe_seed\(uint64_t seed\) \{ return seed \^ (0x[0-9A-Fa-f]+)ull; \}", src).group(1), 16)
     assert cabi.probe_seed(12345) == 12345 ^ xor
+
+
+def _device_count():
+    try:
+        rt = ctypes.CDLL("libcudart.so")
+    except OSError:
+        for name in ("libcudart.so.13", "libcudart.so.12"):
+            try:
+                rt = ctypes.CDLL(name)
+                break
+            except OSError:
+                rt = None
+        if rt is None:
+            return 0
+    n = ctypes.c_int(0)
+    return n.value if rt.cudaGetDeviceCount(ctypes.byref(n)) == 0 else 0
+
+
+def test_no_gpu_fails_loudly():
+    """Without a usable GPU every entry point that needs one returns an error with the CUDA
+    message (no CPU fallback): creating a chain and a batch raises EsmError."""
+    if _device_count() > 0:
+        pytest.skip("a GPU is present")
+    from esmgb.model import make_model
+    m = make_model(10, 15, 24, seed=1)
+    with pytest.raises(DV.EsmError, match="esm_create: status -2: .*CUDA|cuda"):
+        DV.DeviceChain(m, 4, precision=32, seed=1)
+    L = DV.load()
+    h = ctypes.c_void_p()
+    assert L.esm_batch_create(None, 0, ctypes.byref(h)) != 0     # no contexts: refused, not a crash
