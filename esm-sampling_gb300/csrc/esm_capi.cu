@@ -2061,10 +2061,12 @@ int esm_batch_sweeps(esm_batch *b, int32_t n, int64_t sweep0, int64_t *stats) {
     const size_t ns = 2 * (ESM_NFAM + 1) + 1;
     for (esm_ctx *c : b->ctx) BCK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * ns, b->stream));
     BCK(cudaEventRecord(b->t0, b->stream));
-    for (int s = 0; s < n; ++s)
-        if ((rc = batch_sweep(b, (uint32_t)(sweep0 + s)))) return rc;
-    BCK(cudaEventRecord(b->t1, b->stream));
+    int rs = 0;
+    for (int s = 0; s < n && !rs; ++s) rs = batch_sweep(b, (uint32_t)(sweep0 + s));
+    if (!rs) BCK(cudaEventRecord(b->t1, b->stream));
+    // the contexts' later work waits for what the batch enqueued, also after a failed sweep
     if ((rc = batch_join_out(b))) return rc;
+    if (rs) return rs;
     for (esm_ctx *c : b->ctx) c->has_scores = false;
     if ((rc = batch_wait(b, 3600.0))) return rc;
     BCK(cudaEventElapsedTime(&b->last_ms, b->t0, b->t1));
